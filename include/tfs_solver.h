@@ -1,0 +1,196 @@
+/*
+ * tfs_solver.h -- C ABI of the GB300 (sm_103a) Krylov solver library
+ * libtfs_gb300.so.
+ *
+ * The library replaces the sequential linear-solver module of the T-FlowS
+ * flow solver (Sources/Process/Solvers_Mod.f90 with the routines included at
+ * Solvers_Mod.f90:16-21).  The flow solver keeps calling
+ *
+ *     call Cg  (A, x, r1, prec, niter, tol, ini_res, fin_res)
+ *     call Bicg(A, x, r1, prec, niter, tol, ini_res, fin_res)
+ *     call Cgs (A, x, r1, prec, niter, tol, ini_res, fin_res)
+ *
+ * through an ISO_C_BINDING module that expands `A` (type Matrix_Type,
+ * Matrix_Mod.f90:36-49) into its compressed-row arrays.  Everything below uses
+ * plain pointers and sizes:
+ *
+ *   n       number of cells = rows      (A % pnt_grid % n_cells)
+ *   nnz     stored entries = row(n+1)-1 (the reference allocates nnz+1)
+ *   row1    A % row(1:n+1), 1-based, int32
+ *   col1    A % col(1:nnz), 1-based column numbers, ascending within a row
+ *   dia1    A % dia(1:n),   1-based position of the diagonal in each row
+ *   val     A % val(1:nnz), float64
+ *   x       x(1:n), the interior part of x(-NB:N); in/out
+ *   r1      on entry b(1:n); on return the final recursive residual (F3)
+ *   prec    0 none, 1 diagonal, 2 diagonal incomplete Cholesky (DIC)
+ *   niter   in: iteration limit; out: iterations done, or limit+1 if the
+ *           solve did not converge (Fortran DO-loop exit value)
+ *   tol     ABSOLUTE tolerance on ||r||_2 (the reference does not scale it)
+ *   ini_res out: ||b - A x0||_2 (left untouched when ||b|| < tol)
+ *   fin_res out: last ||r||_2 (||b||_2 on the ||b|| < tol exit, where the
+ *           reference returns an uninitialised local)
+ *
+ * All calls return an int status (TFS_OK = 0).  A non-finite residual is
+ * reported as TFS_ERR_NONFINITE with fin_res = NaN and niter = limit+1; the
+ * contents of x and r1 are then unspecified (the reference carries the NaN
+ * through every remaining iteration; this library stops at the first one).
+ *
+ * Threading: a handle is used by one host thread at a time; every handle owns
+ * one CUDA stream.  Different handles may be used concurrently.
+ */
+#ifndef TFS_SOLVER_H
+#define TFS_SOLVER_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define TFS_OK             0
+#define TFS_ERR_ARG        1  /* null pointer, bad size, unknown method/prec  */
+#define TFS_ERR_MATRIX     2  /* malformed CSR: range, unsorted row, no diag   */
+#define TFS_ERR_CUDA       3  /* CUDA runtime failure (no device, OOM, ...)    */
+#define TFS_ERR_NONFINITE  4  /* breakdown: NaN/Inf residual, rho or (p,q)     */
+#define TFS_ERR_TOPOLOGY   5  /* arrays do not match the registered topology   */
+#define TFS_ERR_TIMEOUT    6  /* a bounded device-side wait expired            */
+#define TFS_ERR_BUDGET     7  /* request refused by the device-memory budget   */
+
+/* ---- methods (the three Solvers_Mod routines) and preconditioners ----- */
+#define TFS_CG    0   /* Cg.f90:2   */
+#define TFS_BICG  1   /* Bicg.f90:2 */
+#define TFS_CGS   2   /* Cgs.f90:2  */
+
+#define TFS_PREC_NONE 0   /* Prec_Form.f90:45-49 / Prec_Solve.f90:71-74 */
+#define TFS_PREC_DIAG 1   /* Prec_Form.f90:24-27 / Prec_Solve.f90:35-38 */
+#define TFS_PREC_DIC  2   /* Prec_Form.f90:32-40 / Prec_Solve.f90:43-67 */
+
+/* ---- arithmetic of the Krylov iterations ------------------------------ */
+#define TFS_FP64  0   /* every operation in binary64, per-row arithmetic of the reference */
+#define TFS_MIXED 1   /* binary32 matrix and vectors inside the iteration; binary64
+                         true residual b-Ax, alpha/beta reductions and solution */
+
+typedef struct tfs_handle tfs_handle;
+
+/* Statistics of the last solve on a handle (device-measured). */
+typedef struct tfs_stats {
+    int32_t  iterations;        /* Krylov iterations executed                   */
+    int32_t  true_residuals;    /* binary64 b-Ax evaluations (TFS_MIXED)        */
+    int32_t  n_levels;          /* DIC level-schedule depth of the topology     */
+    int32_t  status;            /* status of the last solve                     */
+    double   solve_ms;          /* device time of the last solve (CUDA events)  */
+    double   spmv_ns_total;     /* summed duration of the SpMV launches          */
+    int64_t  spmv_launches;     /* number of SpMV launches timed                 */
+    double   sweep_ns_total;    /* summed duration of DIC sweep launches         */
+    int64_t  sweep_launches;
+    int64_t  kernel_launches;   /* kernels launched by the last solve            */
+    int64_t  device_bytes;      /* device memory held by the handle             */
+} tfs_stats;
+
+/* ---- topology ----------------------------------------------------------- */
+
+/* Register a CSR topology (row1/col1/dia1, 1-based) and build its device
+ * layout: 0-based sliced-ELL storage, the DIC level schedule (computed on the
+ * device) and the Krylov work vectors.  The topology of T-FlowS is built once
+ * at start-up (Main.f90:141-142, Matrix_Mod/Topology.f90:2-127) and only the
+ * values change between solves, so a handle is built once per mesh.
+ * Replaces: the device-side counterpart of Matrix_Mod_Topology's output. */
+int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1,
+                          const int32_t *col1, const int32_t *dia1,
+                          tfs_handle **out);
+
+/* Free every device and host resource of a handle. */
+int tfs_release(tfs_handle *h);
+
+/* Arithmetic of the Krylov iterations for later solves on h: TFS_FP64 or
+ * TFS_MIXED.  Replaces nothing in the reference (it has binary64 only). */
+int tfs_set_precision(tfs_handle *h, int mode);
+
+/* ---- solves ------------------------------------------------------------- */
+
+/* One preconditioned Krylov solve with host arrays (val, x, r1 host memory).
+ * method: TFS_CG / TFS_BICG / TFS_CGS.  h may be NULL: the library then
+ * keeps one handle per (row1, col1, n, nnz) and builds it on first use.
+ * Replaces: Cg.f90:2-4, Bicg.f90:2-4, Cgs.f90:2-4 (same argument meaning). */
+int tfs_solve(int method, tfs_handle *h, int32_t n, int32_t nnz,
+              const int32_t *row1, const int32_t *col1, const int32_t *dia1,
+              const double *val, double *x, double *r1, int32_t prec,
+              int32_t *niter, double tol, double *ini_res, double *fin_res);
+
+/* The three Fortran-shaped entry points the ISO_C_BINDING shim binds.
+ * Replace Cg.f90:2-4, Bicg.f90:2-4 and Cgs.f90:2-4 respectively. */
+int tfs_cg(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+           const int32_t *dia1, const double *val, double *x, double *r1,
+           int32_t prec, int32_t *niter, double tol, double *ini_res,
+           double *fin_res);
+int tfs_bicg(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+             const int32_t *dia1, const double *val, double *x, double *r1,
+             int32_t prec, int32_t *niter, double tol, double *ini_res,
+             double *fin_res);
+int tfs_cgs(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+            const int32_t *dia1, const double *val, double *x, double *r1,
+            int32_t prec, int32_t *niter, double tol, double *ini_res,
+            double *fin_res);
+
+/* The same solve on device-resident arrays (natural cell order, 0-based
+ * C arrays of length nnz / n).  Used by callers that assemble on the GPU.
+ * Replaces: Cg.f90:2-4, Bicg.f90:2-4, Cgs.f90:2-4. */
+int tfs_solve_device(int method, tfs_handle *h, const double *d_val,
+                     double *d_x, double *d_r1, int32_t prec, int32_t *niter,
+                     double tol, double *ini_res, double *fin_res);
+
+/* ---- single routines (host arrays), for callers and parity checks ------ */
+
+/* q = A p (the product loop of Cg.f90:128-134, per-row arithmetic kept). */
+int tfs_spmv(tfs_handle *h, const double *val, const double *p, double *q);
+
+/* r1 <- r1 - A x.  Replaces Residual.f90:2-40 (n_proc = 0). */
+int tfs_residual(tfs_handle *h, const double *val, const double *x, double *r1);
+
+/* d(i) = D % val(D % dia(i)) after Prec_Form.  Replaces Prec_Form.f90:2-51. */
+int tfs_prec_form(tfs_handle *h, const double *val, int32_t prec, double *d);
+
+/* x = M^-1 b for the preconditioner formed from val.
+ * Replaces Prec_Form.f90:2-51 followed by Prec_Solve.f90:2-78. */
+int tfs_prec_solve(tfs_handle *h, const double *val, int32_t prec,
+                   const double *b, double *x);
+
+/* ---- introspection ------------------------------------------------------ */
+int tfs_get_stats(const tfs_handle *h, tfs_stats *out);
+
+/* Level of every row (0-based levels, natural row order) of the DIC
+ * dependency analysis done on the device at registration. */
+int tfs_get_levels(const tfs_handle *h, int32_t *levels);
+
+/* Device time of one SpMV launch averaged over `reps` back-to-back launches
+ * on the handle's stream (CUDA events), with values val (host, nnz), in the
+ * given arithmetic (TFS_FP64 or TFS_MIXED). */
+int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int reps,
+                  double *ms_per_launch);
+
+/* Human-readable text for a status code. */
+const char *tfs_status_string(int status);
+
+/* Text of the last error recorded by this thread (CUDA error names etc.). */
+const char *tfs_last_error(void);
+
+/* ---- host-side mesh utilities ------------------------------------------ */
+
+/* Count of stored entries of the face-connectivity matrix (one per cell plus
+ * two per interior face).  faces_c: 2*n_faces 1-based cell numbers (c1, c2);
+ * c2 <= 0 marks a boundary face.  Replaces Topology.f90:33-47. */
+int32_t tfs_topology_count(int32_t n_cells, int32_t n_faces,
+                           const int32_t *faces_c);
+
+/* Build row/col/dia/mir/pos exactly as Matrix_Mod_Topology does (rows
+ * sorted, 1-based).  col and mir have nnz entries, pos 2*n_faces (0 for
+ * boundary faces).  Replaces Matrix_Mod/Topology.f90:2-127. */
+int tfs_topology_build(int32_t n_cells, int32_t n_faces, const int32_t *faces_c,
+                       int32_t *row1, int32_t *col1, int32_t *dia1,
+                       int32_t *mir1, int32_t *pos1);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TFS_SOLVER_H */

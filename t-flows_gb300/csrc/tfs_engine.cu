@@ -1,0 +1,936 @@
+// tfs_engine.cu -- handles, device layout, CUDA-graph solve loop and the
+// C ABI of libtfs_gb300.so (declared in include/tfs_solver.h).
+//
+// One solve is one CUDA graph launch:
+//   prologue  k_init, k_gather_val, k_load (||b||), DIC form by levels,
+//             k_residual (r = b - A x, ||r0||)
+//   WHILE     conditional node; its body is one Krylov iteration and the
+//             body's last kernel sets the condition from the convergence test
+//   epilogue  k_store (x and r1 back to natural order)
+// The graph of each (method, prec, arithmetic) is built once per handle and
+// reused; per-call arguments go through a small DevParams block copied in
+// before the launch.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "tfs_internal.h"
+#include "tfs_kernels.cuh"
+#include "tfs_mixed.cuh"
+
+using namespace tfs;
+
+// ------------------------------------------------------------ errors
+
+static thread_local std::string g_err;
+
+void tfs_set_error_text(const char *msg) { g_err = msg ? msg : ""; }
+
+int tfs_engine_error(cudaError_t e, const char *what)
+{
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    g_err = buf;
+    return TFS_ERR_CUDA;
+}
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return tfs_engine_error(_e, #call);      \
+    } while (0)
+
+#define CKL(what)                                                       \
+    do {                                                                \
+        cudaError_t _e = cudaGetLastError();                            \
+        if (_e != cudaSuccess) return tfs_engine_error(_e, what);       \
+    } while (0)
+
+extern "C" const char *tfs_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char *tfs_status_string(int s)
+{
+    switch (s) {
+    case TFS_OK: return "ok";
+    case TFS_ERR_ARG: return "invalid argument";
+    case TFS_ERR_MATRIX: return "malformed matrix";
+    case TFS_ERR_CUDA: return "CUDA error";
+    case TFS_ERR_NONFINITE: return "non-finite residual (breakdown)";
+    case TFS_ERR_TOPOLOGY: return "arrays do not match the registered topology";
+    case TFS_ERR_TIMEOUT: return "device-side iteration guard expired";
+    case TFS_ERR_BUDGET: return "device memory budget exceeded";
+    default: return "unknown status";
+    }
+}
+
+// ------------------------------------------------------------ helpers
+
+static SellDev sell_of(const tfs_handle *h)
+{
+    SellDev A;
+    A.n_int = h->n_int;
+    A.n_chunks = h->n_chunks;
+    A.rowinfo = h->rowinfo;
+    A.slice_off = h->slice_off;
+    A.col = h->col;
+    return A;
+}
+
+template <typename T>
+static int dalloc(tfs_handle *h, T **p, size_t count)
+{
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = sizeof(T);
+    CK(cudaMalloc((void **)p, bytes));
+    h->device_bytes += (int64_t)bytes;
+    return TFS_OK;
+}
+
+static uint64_t fingerprint(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                            const int32_t *dia1)
+{
+    uint64_t f = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { f = (f ^ v) * 1099511628211ull; };
+    mix((uint64_t)n);
+    mix((uint64_t)nnz);
+    for (int k = 0; k < 64; k++) {
+        int64_t i = (int64_t)n * k / 64, j = (int64_t)nnz * k / 64;
+        mix((uint64_t)row1[i]);
+        mix((uint64_t)col1[j]);
+        mix((uint64_t)dia1[i]);
+    }
+    mix((uint64_t)row1[n]);
+    return f;
+}
+
+// Checks the Matrix_Type invariants the kernels rely on.
+static int validate_csr(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                        const int32_t *dia1)
+{
+    if (n <= 0 || nnz < n || !row1 || !col1 || !dia1) {
+        tfs_set_error_text("n must be positive, nnz >= n, arrays non-null");
+        return TFS_ERR_ARG;
+    }
+    if (row1[0] != 1 || row1[n] - 1 != nnz) {
+        tfs_set_error_text("row(1) must be 1 and row(n+1)-1 must equal nnz");
+        return TFS_ERR_MATRIX;
+    }
+    for (int32_t i = 0; i < n; i++) {
+        int32_t a = row1[i], b = row1[i + 1];
+        if (b <= a || b - a > 65535) {
+            tfs_set_error_text("every row needs 1..65535 entries (the diagonal at least)");
+            return TFS_ERR_MATRIX;
+        }
+        for (int32_t p = a; p < b; p++) {
+            int32_t c = col1[p - 1];
+            if (c < 1 || c > n || (p > a && c <= col1[p - 2])) {
+                tfs_set_error_text("column numbers must lie in 1..n and ascend within a row");
+                return TFS_ERR_MATRIX;
+            }
+        }
+        int32_t d = dia1[i];
+        if (d < a || d >= b || col1[d - 1] != i + 1) {
+            tfs_set_error_text("dia(i) must point at column i inside row i");
+            return TFS_ERR_MATRIX;
+        }
+    }
+    return TFS_OK;
+}
+
+// ------------------------------------------------------- registration
+
+static int compute_levels(tfs_handle *h, const std::vector<int> &row0, const std::vector<int> &col0,
+                          const std::vector<int> &dia0, std::vector<int32_t> &level)
+{
+    const int n = h->n;
+    int *d_row = nullptr, *d_col = nullptr, *d_dia = nullptr, *d_lvl = nullptr, *d_chg = nullptr;
+    int rc = TFS_OK;
+    const int PASSES = 8;
+    auto cleanup = [&]() {
+        cudaFree(d_row); cudaFree(d_col); cudaFree(d_dia); cudaFree(d_lvl); cudaFree(d_chg);
+    };
+#define CKC(call)                                                       \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) { rc = tfs_engine_error(_e, #call); cleanup(); return rc; } \
+    } while (0)
+    CKC(cudaMalloc(&d_row, sizeof(int) * (n + 1)));
+    CKC(cudaMalloc(&d_col, sizeof(int) * (size_t)h->nnz));
+    CKC(cudaMalloc(&d_dia, sizeof(int) * n));
+    CKC(cudaMalloc(&d_lvl, sizeof(int) * n));
+    CKC(cudaMalloc(&d_chg, sizeof(int) * PASSES));
+    CKC(cudaMemcpyAsync(d_row, row0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
+    CKC(cudaMemcpyAsync(d_col, col0.data(), sizeof(int) * (size_t)h->nnz, cudaMemcpyHostToDevice, h->stream));
+    CKC(cudaMemcpyAsync(d_dia, dia0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+    CKC(cudaMemsetAsync(d_lvl, 0, sizeof(int) * n, h->stream));
+    int grid = (n + 255) / 256;
+    if (grid > h->sm_count * 8) grid = h->sm_count * 8;
+    // The longest dependency chain bounds the passes: at most n + 1.
+    for (int64_t done_passes = 0; done_passes <= (int64_t)n + PASSES; done_passes += PASSES) {
+        CKC(cudaMemsetAsync(d_chg, 0, sizeof(int) * PASSES, h->stream));
+        for (int p = 0; p < PASSES; p++)
+            k_level_pass<<<grid, 256, 0, h->stream>>>(n, d_row, d_col, d_dia, d_lvl, d_chg + p);
+        CKC(cudaGetLastError());
+        int chg[PASSES];
+        CKC(cudaMemcpyAsync(chg, d_chg, sizeof chg, cudaMemcpyDeviceToHost, h->stream));
+        CKC(cudaStreamSynchronize(h->stream));
+        if (chg[PASSES - 1] == 0) break;
+    }
+    level.resize(n);
+    CKC(cudaMemcpyAsync(level.data(), d_lvl, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+    CKC(cudaStreamSynchronize(h->stream));
+#undef CKC
+    cleanup();
+    return TFS_OK;
+}
+
+static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1, const int32_t *dia1)
+{
+    const int n = h->n, nnz = h->nnz;
+    std::vector<int> row0(n + 1), col0((size_t)nnz), dia0(n);
+    for (int i = 0; i <= n; i++) row0[i] = row1[i] - 1;
+    for (int j = 0; j < nnz; j++) col0[j] = col1[j] - 1;
+    for (int i = 0; i < n; i++) dia0[i] = dia1[i] - 1;
+
+    std::vector<int32_t> level;
+    int rc = compute_levels(h, row0, col0, dia0, level);
+    if (rc) return rc;
+    int nl = 0;
+    for (int i = 0; i < n; i++) {
+        if (level[i] < 0 || level[i] >= n) { tfs_set_error_text("level analysis failed"); return TFS_ERR_CUDA; }
+        if (level[i] + 1 > nl) nl = level[i] + 1;
+    }
+    // Bucket rows by level (stable), each level padded to a multiple of 32.
+    std::vector<int> cnt(nl, 0);
+    for (int i = 0; i < n; i++) cnt[level[i]]++;
+    h->lvl_begin.assign(nl + 1, 0);
+    for (int l = 0; l < nl; l++) h->lvl_begin[l + 1] = h->lvl_begin[l] + ((cnt[l] + 31) & ~31);
+    int64_t n_int64 = ((int64_t)h->lvl_begin[nl] + TFS_TPB - 1) / TFS_TPB * TFS_TPB;
+    if (n_int64 > INT32_MAX / 2) { tfs_set_error_text("matrix too large"); return TFS_ERR_ARG; }
+    const int n_int = (int)n_int64;
+    std::vector<int> perm(n_int, -1), iperm(n), fillp(nl);
+    for (int l = 0; l < nl; l++) fillp[l] = h->lvl_begin[l];
+    for (int i = 0; i < n; i++) {
+        int p = fillp[level[i]]++;
+        perm[p] = i;
+        iperm[i] = p;
+    }
+    // SELL-32 slices.
+    const int n_slices = n_int / 32;
+    std::vector<uint32_t> rowinfo(n_int, 0u);
+    std::vector<int> slice_off(n_slices + 1, 0);
+    for (int p = 0; p < n_int; p++) {
+        int o = perm[p];
+        if (o >= 0) rowinfo[p] = (uint32_t)(row0[o + 1] - row0[o]) | ((uint32_t)(dia0[o] - row0[o]) << 16);
+    }
+    int64_t off = 0;
+    for (int s = 0; s < n_slices; s++) {
+        int w = 0;
+        for (int t = 0; t < 32; t++) {
+            int len = (int)(rowinfo[32 * s + t] & 0xffffu);
+            if (len > w) w = len;
+        }
+        slice_off[s] = (int)off;
+        off += 32 * (int64_t)w;
+        if (off > INT32_MAX) { tfs_set_error_text("padded matrix exceeds 2^31 entries"); return TFS_ERR_ARG; }
+    }
+    slice_off[n_slices] = (int)off;
+    const int nnz_pad = (int)off;
+    std::vector<int> colx((size_t)nnz_pad, 0), vmap((size_t)nnz_pad, -1);
+    for (int p = 0; p < n_int; p++) {
+        int o = perm[p];
+        if (o < 0) continue;
+        int base = slice_off[p >> 5] + (p & 31);
+        for (int j = 0; j < row0[o + 1] - row0[o]; j++) {
+            colx[(size_t)base + 32 * (size_t)j] = iperm[col0[row0[o] + j]];
+            vmap[(size_t)base + 32 * (size_t)j] = row0[o] + j;
+        }
+    }
+    h->n_int = n_int;
+    h->n_chunks = n_int / TFS_TPB;
+    h->n_slices = n_slices;
+    h->nnz_pad = nnz_pad;
+    h->n_levels = nl;
+    h->levels_nat.assign(level.begin(), level.end());
+    int g = h->sm_count * 8;
+    h->grid = h->n_chunks < g ? h->n_chunks : g;
+    if (h->grid < 1) h->grid = 1;
+
+    if ((rc = dalloc(h, &h->perm, n_int)) || (rc = dalloc(h, &h->iperm, n)) ||
+        (rc = dalloc(h, &h->rowinfo, n_int)) || (rc = dalloc(h, &h->slice_off, n_slices + 1)) ||
+        (rc = dalloc(h, &h->col, nnz_pad)) || (rc = dalloc(h, &h->vmap, nnz_pad)) ||
+        (rc = dalloc(h, &h->val, nnz_pad)) || (rc = dalloc(h, &h->val32, nnz_pad)) ||
+        (rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
+        (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)) ||
+        (rc = dalloc(h, &h->st, 1)) || (rc = dalloc(h, &h->params, 1)))
+        return rc;
+    CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->rowinfo, rowinfo.data(), sizeof(uint32_t) * n_int, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->slice_off, slice_off.data(), sizeof(int) * (n_slices + 1), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->col, colx.data(), sizeof(int) * (size_t)nnz_pad, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->vmap, vmap.data(), sizeof(int) * (size_t)nnz_pad, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->val, 0, sizeof(double) * (size_t)nnz_pad, h->stream));
+    CK(cudaMemsetAsync(h->val32, 0, sizeof(float) * (size_t)nnz_pad, h->stream));
+    CK(cudaMemsetAsync(h->part, 0, sizeof(double) * (TFS_NPART * (size_t)h->grid + 64), h->stream));
+    CK(cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream));
+
+    // Work vectors: 16 binary64 + 15 binary32, zero so padding rows stay zero.
+    const size_t nv64 = 16, nv32 = 15;
+    double *pool = nullptr;
+    float *pool32 = nullptr;
+    if ((rc = dalloc(h, &pool, nv64 * (size_t)n_int)) || (rc = dalloc(h, &pool32, nv32 * (size_t)n_int)))
+        return rc;
+    h->vec_pool = pool;
+    h->vec32_pool = pool32;
+    CK(cudaMemsetAsync(pool, 0, sizeof(double) * nv64 * (size_t)n_int, h->stream));
+    CK(cudaMemsetAsync(pool32, 0, sizeof(float) * nv32 * (size_t)n_int, h->stream));
+    double *v[16];
+    for (size_t k = 0; k < nv64; k++) v[k] = pool + k * (size_t)n_int;
+    h->v = Vec64{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12], v[13], v[14], v[15]};
+    float *f[15];
+    for (size_t k = 0; k < nv32; k++) f[k] = pool32 + k * (size_t)n_int;
+    h->f = Vec32{f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10], f[11], f[12], f[13], f[14]};
+    CK(cudaStreamSynchronize(h->stream));
+    return TFS_OK;
+}
+
+static void free_handle(tfs_handle *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &kv : h->graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
+                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params,
+                    h->vec_pool, h->vec32_pool};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->h_params) cudaFreeHost(h->h_params);
+    if (h->h_state) cudaFreeHost(h->h_state);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream2) cudaStreamDestroy(h->stream2);
+    delete h;
+}
+
+extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1,
+                                     const int32_t *col1, const int32_t *dia1, tfs_handle **out)
+{
+    if (!out) return TFS_ERR_ARG;
+    *out = nullptr;
+    int rc = validate_csr(n, nnz, row1, col1, dia1);
+    if (rc) return rc;
+    tfs_handle *h = new tfs_handle;
+    h->n = n;
+    h->nnz = nnz;
+    h->fingerprint = fingerprint(n, nnz, row1, col1, dia1);
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return tfs_engine_error(e, "cudaGetDevice"); }
+    e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+    if (e != cudaSuccess) { delete h; return tfs_engine_error(e, "cudaDeviceGetAttribute"); }
+#define CKH(call)                                                              \
+    do {                                                                       \
+        cudaError_t _e = (call);                                               \
+        if (_e != cudaSuccess) { int _r = tfs_engine_error(_e, #call); free_handle(h); return _r; } \
+    } while (0)
+    CKH(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CKH(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+    CKH(cudaEventCreate(&h->ev0));
+    CKH(cudaEventCreate(&h->ev1));
+    CKH(cudaMallocHost((void **)&h->h_params, sizeof(DevParams)));
+    CKH(cudaMallocHost((void **)&h->h_state, sizeof(DevState)));
+#undef CKH
+    rc = build_layout(h, row1, col1, dia1);
+    if (rc) { free_handle(h); return rc; }
+    h->stats.n_levels = h->n_levels;
+    h->stats.device_bytes = h->device_bytes;
+    *out = h;
+    return TFS_OK;
+}
+
+extern "C" int tfs_release(tfs_handle *h)
+{
+    if (!h) return TFS_ERR_ARG;
+    free_handle(h);
+    return TFS_OK;
+}
+
+extern "C" int tfs_set_precision(tfs_handle *h, int mode)
+{
+    if (!h || (mode != TFS_FP64 && mode != TFS_MIXED)) return TFS_ERR_ARG;
+    h->precision = mode;
+    return TFS_OK;
+}
+
+// ------------------------------------------------------ graph capture
+
+static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond);
+static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count);
+static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst);
+static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s);
+
+static int launch_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+{
+    cudaStream_t s = h->stream;
+    SellDev A = sell_of(h);
+    const int G = h->grid, T = TFS_TPB;
+    int gv = (h->nnz_pad + T - 1) / T;
+    if (gv > h->sm_count * 16) gv = h->sm_count * 16;
+    k_init<<<1, 1, 0, s>>>(h->st, h->params, prec);
+    k_gather_val<<<gv, T, 0, s>>>(h->vmap, h->params, h->val,
+                                  h->precision == TFS_MIXED ? h->val32 : nullptr, h->nnz_pad);
+    k_load<<<G, T, 0, s>>>(A, h->val, h->perm, h->params, h->v, h->st, h->part, prec);
+    *count = 3;
+    if (prec == 2) {
+        for (int l = 0; l < h->n_levels; l++) {
+            int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+            k_dic_form<<<(r1 - r0 + T - 1) / T, T, 0, s>>>(A, h->val, h->v.d, r0, r1, h->st);
+        }
+        *count += h->n_levels;
+    }
+    if (h->precision == TFS_MIXED) {
+        tfs_mixed_prologue(h, method, prec, cond);
+        *count += 2;
+    } else {
+        if (method == TFS_CG) k_residual<0><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
+        else if (method == TFS_BICG) k_residual<1><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
+        else k_residual<2><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
+        *count += 1;
+    }
+    CKL("prologue launch");
+    return TFS_OK;
+}
+
+// Forward and backward level sweeps: z = M^-1 b for NR right-hand sides, in
+// binary64 (val, d of the handle) or binary32 (val32, d32).
+template <typename T>
+static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, const T *b2,
+                         T *y1, T *y2, T *z1, T *z2, int *count)
+{
+    SellDev A = sell_of(h);
+    const int T_ = TFS_TPB;
+    const T *val, *d;
+    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
+    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
+    for (int l = 0; l < h->n_levels; l++) {
+        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+        int g = (r1 - r0 + T_ - 1) / T_;
+        if (nr == 1) k_fwd<T, 1><<<g, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, r0, r1, h->st, l == 0);
+        else k_fwd<T, 2><<<g, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, r0, r1, h->st, l == 0);
+    }
+    for (int l = h->n_levels - 1; l >= 0; l--) {
+        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+        int g = (r1 - r0 + T_ - 1) / T_;
+        if (nr == 1) k_bwd<T, 1><<<g, T_, 0, s>>>(A, val, d, y1, y2, z1, z2, r0, r1, h->st);
+        else k_bwd<T, 2><<<g, T_, 0, s>>>(A, val, d, y1, y2, z1, z2, r0, r1, h->st);
+    }
+    *count += 2 * h->n_levels;
+    CKL("sweep launch");
+    return TFS_OK;
+}
+
+// ------------------------------------------------ mixed-precision graphs
+
+// After the binary64 preconditioner is formed: d32 = (float) d, then the
+// binary64 initial residual (k_mx_true<INIT>).
+static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond)
+{
+    cudaStream_t s = h->stream;
+    SellDev A = sell_of(h);
+    const int G = h->grid, T = TFS_TPB;
+    k_mx_cast<<<G, T, 0, s>>>(h->n_int, h->v.d, h->f.d);
+    if (method == TFS_CG) k_mx_true<0, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
+    else if (method == TFS_BICG) k_mx_true<1, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
+    else k_mx_true<2, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
+    CKL("mixed prologue");
+    return TFS_OK;
+}
+
+static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+{
+    cudaStream_t s = h->stream2;
+    SellDev A = sell_of(h);
+    const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
+    Vec64 &V = h->v;
+    Vec32 &F = h->f;
+    const float *v32 = h->val32;
+    int rc;
+    *count = 0;
+    if (method == TFS_CG) {
+        if (prec == 2) {
+            if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
+            k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
+            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        } else {
+            k_mx_cg_p<false><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 4;
+        }
+    } else if (method == TFS_BICG) {
+        if (prec == 2) {
+            if ((rc = launch_sweeps<float>(h, s, 2, F.r, F.r2, F.y, F.y2, F.z, F.z2, count))) return rc;
+            k_mx_dot_rho<1><<<G, T, 0, s>>>(nc, F, h->st, h->part);
+            k_mx_bicg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_bicg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        } else {
+            k_mx_bicg_p<false><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_bicg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 4;
+        }
+    } else {
+        if (prec == 2) {
+            k_mx_cgs_u<false><<<G, T, 0, s>>>(nc, F, h->st);
+            if ((rc = launch_sweeps<float>(h, s, 1, F.u2, nullptr, F.y, nullptr, F.p2, nullptr, count))) return rc;
+            k_mx_spmv_v<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_cgs_q<false><<<G, T, 0, s>>>(nc, F, h->st);
+            if ((rc = launch_sweeps<float>(h, s, 1, F.w, nullptr, F.y, nullptr, F.p, nullptr, count))) return rc;
+            k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        } else {
+            k_mx_cgs_u<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv_v<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_cgs_q<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        }
+    }
+    CKL("mixed body launch");
+    return TFS_OK;
+}
+
+static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst)
+{
+    k_mx_cast<<<h->grid, TFS_TPB, 0, h->stream>>>(h->n_int, src, dst);
+}
+
+static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s)
+{
+    k_mx_spmv_pq<<<h->grid, TFS_TPB, 0, s>>>(sell_of(h), h->val32, h->f.p, h->f.q, h->st, h->part);
+}
+
+static int launch_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+{
+    cudaStream_t s = h->stream2;
+    SellDev A = sell_of(h);
+    const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
+    Vec64 &V = h->v;
+    int rc;
+    *count = 0;
+    if (method == TFS_CG) {
+        if (prec == 2) {
+            if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
+            k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);
+            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv_pq<<<G, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            *count += 4;
+        } else {
+            k_cg_p<false><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv_pq<<<G, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_cg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            *count += 3;
+        }
+    } else if (method == TFS_BICG) {
+        if (prec == 2) {
+            if ((rc = launch_sweeps<double>(h, s, 2, V.r, V.r2, V.y, V.y2, V.z, V.z2, count))) return rc;
+            k_dot_rho<1><<<G, T, 0, s>>>(nc, V, h->st, h->part);
+            k_bicg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv2_pq<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_bicg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            *count += 4;
+        } else {
+            k_bicg_p<false><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv2_pq<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_bicg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            *count += 3;
+        }
+    } else {
+        if (prec == 2) {
+            k_cgs_u<false><<<G, T, 0, s>>>(nc, V, h->st);
+            if ((rc = launch_sweeps<double>(h, s, 1, V.u2, nullptr, V.y, nullptr, V.p2, nullptr, count))) return rc;
+            k_spmv_v<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_cgs_q<false><<<G, T, 0, s>>>(nc, V, h->st);
+            if ((rc = launch_sweeps<double>(h, s, 1, V.w, nullptr, V.y, nullptr, V.p, nullptr, count))) return rc;
+            k_cgs_spmv_r<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
+            *count += 4;
+        } else {
+            k_cgs_u<true><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv_v<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_cgs_q<true><<<G, T, 0, s>>>(nc, V, h->st);
+            k_cgs_spmv_r<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
+            *count += 4;
+        }
+    }
+    CKL("body launch");
+    return TFS_OK;
+}
+
+static int launch_epilogue(tfs_handle *h, int *count)
+{
+    int g = (h->n_int + 255) / 256;
+    if (g > h->sm_count * 8) g = h->sm_count * 8;
+    k_store<<<g, 256, 0, h->stream>>>(h->n_int, h->perm, h->v.x, h->v.r, h->params);
+    *count = 1;
+    CKL("epilogue launch");
+    return TFS_OK;
+}
+
+static int build_graph(tfs_handle *h, int method, int prec, GraphEntry &ge)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return tfs_engine_error(e, "cudaGraphConditionalHandleCreate"); }
+    int rc = TFS_OK;
+    auto fail = [&](cudaError_t err, const char *what) {
+        cudaGraph_t tmp;
+        cudaStreamEndCapture(h->stream, &tmp);
+        cudaStreamEndCapture(h->stream2, &tmp);
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        return tfs_engine_error(err, what);
+    };
+    e = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(e, "begin capture");
+    if ((rc = launch_prologue(h, method, prec, cond, &ge.prologue_kernels))) { fail(cudaErrorUnknown, "prologue"); return rc; }
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    e = cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return fail(e, "cudaStreamGetCaptureInfo");
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    e = cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &np);
+    if (e != cudaSuccess) return fail(e, "cudaGraphAddNode(while)");
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(h->stream, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return fail(e, "cudaStreamUpdateCaptureDependencies");
+    // Body, captured on the second stream into the conditional node's graph.
+    e = cudaStreamBeginCaptureToGraph(h->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(e, "begin body capture");
+    if (h->precision == TFS_MIXED) rc = tfs_mixed_body(h, method, prec, cond, &ge.body_kernels);
+    else rc = launch_body(h, method, prec, cond, &ge.body_kernels);
+    if (rc) { fail(cudaErrorUnknown, "body"); return rc; }
+    cudaGraph_t btmp;
+    e = cudaStreamEndCapture(h->stream2, &btmp);
+    if (e != cudaSuccess) return fail(e, "end body capture");
+    if ((rc = launch_epilogue(h, &ge.epilogue_kernels))) { fail(cudaErrorUnknown, "epilogue"); return rc; }
+    cudaGraph_t gtmp;
+    e = cudaStreamEndCapture(h->stream, &gtmp);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return tfs_engine_error(e, "end capture"); }
+    e = cudaGraphInstantiate(&ge.exec, g, 0);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return tfs_engine_error(e, "cudaGraphInstantiate"); }
+    ge.graph = g;
+    return TFS_OK;
+}
+
+static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
+{
+    int key = method | (prec << 4) | (h->precision << 8);
+    auto it = h->graphs.find(key);
+    if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
+    GraphEntry ge;
+    int rc = build_graph(h, method, prec, ge);
+    if (rc) return rc;
+    h->graphs[key] = ge;
+    *out = &h->graphs[key];
+    return TFS_OK;
+}
+
+// --------------------------------------------------------------- solve
+
+static int solve_impl(int method, tfs_handle *h, const double *val, double *x, double *r1,
+                      int32_t prec, int32_t *niter, double tol, double *ini_res, double *fin_res,
+                      bool device_ptrs)
+{
+    if (!h || !val || !x || !r1 || !niter || !ini_res || !fin_res) return TFS_ERR_ARG;
+    if (method < TFS_CG || method > TFS_CGS || prec < 0 || prec > 2) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    GraphEntry *ge = nullptr;
+    int rc = get_graph(h, method, prec, &ge);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    DevParams &P = *h->h_params;
+    P.tol = tol;
+    P.niter_max = *niter;
+    P.val_csr = device_ptrs ? val : h->stage_val;
+    P.b = device_ptrs ? r1 : h->stage_b;
+    P.x = device_ptrs ? x : h->stage_x;
+    P.r_out = device_ptrs ? r1 : h->stage_b;
+    CK(cudaMemcpyAsync(h->params, h->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s));
+    if (!device_ptrs) {
+        CK(cudaMemcpyAsync(h->stage_val, val, sizeof(double) * (size_t)h->nnz, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->stage_b, r1, sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->stage_x, x, sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaEventRecord(h->ev0, s));
+    CK(cudaGraphLaunch(ge->exec, s));
+    CK(cudaEventRecord(h->ev1, s));
+    if (!device_ptrs) {
+        CK(cudaMemcpyAsync(x, h->stage_x, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(r1, h->stage_b, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaMemcpyAsync(h->h_state, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const DevState &S = *h->h_state;
+    if (S.early != 1) *ini_res = S.ini_res;
+    *fin_res = S.fin_res;
+    *niter = S.niter_out;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    tfs_stats &T = h->stats;
+    T.iterations = S.loops;
+    T.true_residuals = S.true_res;
+    T.status = S.status;
+    T.solve_ms = ms;
+    T.spmv_ns_total = (double)S.spmv_ns;
+    T.spmv_launches = (int64_t)S.spmv_n;
+    T.sweep_ns_total = (double)S.sweep_ns;
+    T.sweep_launches = (int64_t)S.sweep_n;
+    T.kernel_launches = ge->prologue_kernels + (int64_t)S.loops * ge->body_kernels + ge->epilogue_kernels;
+    T.device_bytes = h->device_bytes;
+    return S.status;
+}
+
+extern "C" int tfs_solve_device(int method, tfs_handle *h, const double *d_val, double *d_x,
+                                double *d_r1, int32_t prec, int32_t *niter, double tol,
+                                double *ini_res, double *fin_res)
+{
+    return solve_impl(method, h, d_val, d_x, d_r1, prec, niter, tol, ini_res, fin_res, true);
+}
+
+// Handles built on demand for tfs_solve(h = NULL) and the Fortran-shaped
+// entry points, keyed by the topology arrays the caller passes.
+namespace {
+std::mutex g_cache_mu;
+std::map<std::tuple<const int32_t *, const int32_t *, int32_t, int32_t, int>, tfs_handle *> g_cache;
+}
+
+static int cached_handle(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                         const int32_t *dia1, tfs_handle **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return tfs_engine_error(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto key = std::make_tuple(row1, col1, n, nnz, dev);
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+        if (it->second->fingerprint == fingerprint(n, nnz, row1, col1, dia1)) { *out = it->second; return TFS_OK; }
+        free_handle(it->second);
+        g_cache.erase(it);
+    }
+    tfs_handle *h = nullptr;
+    int rc = tfs_topology_register(n, nnz, row1, col1, dia1, &h);
+    if (rc) return rc;
+    const char *env = getenv("TFS_PRECISION");
+    if (env && strcmp(env, "mixed") == 0) h->precision = TFS_MIXED;
+    g_cache[key] = h;
+    *out = h;
+    return TFS_OK;
+}
+
+extern "C" int tfs_solve(int method, tfs_handle *h, int32_t n, int32_t nnz, const int32_t *row1,
+                         const int32_t *col1, const int32_t *dia1, const double *val, double *x,
+                         double *r1, int32_t prec, int32_t *niter, double tol, double *ini_res,
+                         double *fin_res)
+{
+    if (!h) {
+        int rc = cached_handle(n, nnz, row1, col1, dia1, &h);
+        if (rc) return rc;
+    } else if (h->n != n || h->nnz != nnz) {
+        tfs_set_error_text("n/nnz differ from the registered topology");
+        return TFS_ERR_TOPOLOGY;
+    }
+    return solve_impl(method, h, val, x, r1, prec, niter, tol, ini_res, fin_res, false);
+}
+
+extern "C" int tfs_cg(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                      const int32_t *dia1, const double *val, double *x, double *r1, int32_t prec,
+                      int32_t *niter, double tol, double *ini_res, double *fin_res)
+{
+    return tfs_solve(TFS_CG, nullptr, n, nnz, row1, col1, dia1, val, x, r1, prec, niter, tol, ini_res, fin_res);
+}
+extern "C" int tfs_bicg(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                        const int32_t *dia1, const double *val, double *x, double *r1, int32_t prec,
+                        int32_t *niter, double tol, double *ini_res, double *fin_res)
+{
+    return tfs_solve(TFS_BICG, nullptr, n, nnz, row1, col1, dia1, val, x, r1, prec, niter, tol, ini_res, fin_res);
+}
+extern "C" int tfs_cgs(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
+                       const int32_t *dia1, const double *val, double *x, double *r1, int32_t prec,
+                       int32_t *niter, double tol, double *ini_res, double *fin_res)
+{
+    return tfs_solve(TFS_CGS, nullptr, n, nnz, row1, col1, dia1, val, x, r1, prec, niter, tol, ini_res, fin_res);
+}
+
+// ------------------------------------------------------ single routines
+
+// Uploads val and runs the gather with a fresh DevState (tol 0, one iteration).
+static int prepare_values(tfs_handle *h, const double *val)
+{
+    cudaStream_t s = h->stream;
+    DevParams &P = *h->h_params;
+    P.tol = 0.0;
+    P.niter_max = 1;
+    P.val_csr = h->stage_val;
+    P.b = h->stage_b;
+    P.x = h->stage_x;
+    P.r_out = h->stage_b;
+    CK(cudaMemcpyAsync(h->params, h->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->stage_val, val, sizeof(double) * (size_t)h->nnz, cudaMemcpyHostToDevice, s));
+    int gv = (h->nnz_pad + 255) / 256;
+    if (gv > h->sm_count * 16) gv = h->sm_count * 16;
+    k_init<<<1, 1, 0, s>>>(h->st, h->params, 0);
+    k_gather_val<<<gv, 256, 0, s>>>(h->vmap, h->params, h->val, h->val32, h->nnz_pad);
+    CKL("gather");
+    return TFS_OK;
+}
+
+static int vec_in(tfs_handle *h, const double *host, double *dst)
+{
+    CK(cudaMemcpyAsync(h->stage_x, host, sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, h->stream));
+    k_perm_in<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(h->n_int, h->perm, h->stage_x, dst);
+    CKL("perm in");
+    return TFS_OK;
+}
+
+static int vec_out(tfs_handle *h, const double *src, double *host)
+{
+    k_perm_out<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(h->n_int, h->perm, src, h->stage_x);
+    CKL("perm out");
+    CK(cudaMemcpyAsync(host, h->stage_x, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return TFS_OK;
+}
+
+static int form_prec(tfs_handle *h, int prec)
+{
+    SellDev A = sell_of(h);
+    k_diag_form<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(A, h->val, h->v.d, prec == 1 ? 1 : 0);
+    if (prec == 2) {
+        for (int l = 0; l < h->n_levels; l++) {
+            int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+            k_dic_form<<<(r1 - r0 + 255) / 256, 256, 0, h->stream>>>(A, h->val, h->v.d, r0, r1, h->st);
+        }
+    }
+    CKL("prec form");
+    return TFS_OK;
+}
+
+extern "C" int tfs_spmv(tfs_handle *h, const double *val, const double *p, double *q)
+{
+    if (!h || !val || !p || !q) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if ((rc = prepare_values(h, val)) || (rc = vec_in(h, p, h->v.p))) return rc;
+    k_spmv_pq<<<h->grid, TFS_TPB, 0, h->stream>>>(sell_of(h), h->val, h->v.p, h->v.q, h->st, h->part);
+    CKL("spmv");
+    return vec_out(h, h->v.q, q);
+}
+
+extern "C" int tfs_residual(tfs_handle *h, const double *val, const double *x, double *r1)
+{
+    if (!h || !val || !x || !r1) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if ((rc = prepare_values(h, val)) || (rc = vec_in(h, x, h->v.x)) || (rc = vec_in(h, r1, h->v.r))) return rc;
+    k_diag_form<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(sell_of(h), h->val, h->v.d, 0);
+    k_residual<0><<<h->grid, TFS_TPB, 0, h->stream>>>(sell_of(h), h->val, h->v, h->st, h->part, 0, 0);
+    CKL("residual");
+    return vec_out(h, h->v.r, r1);
+}
+
+extern "C" int tfs_prec_form(tfs_handle *h, const double *val, int32_t prec, double *d)
+{
+    if (!h || !val || !d || prec < 0 || prec > 2) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if ((rc = prepare_values(h, val)) || (rc = form_prec(h, prec))) return rc;
+    return vec_out(h, h->v.d, d);
+}
+
+extern "C" int tfs_prec_solve(tfs_handle *h, const double *val, int32_t prec, const double *b, double *x)
+{
+    if (!h || !val || !b || !x || prec < 0 || prec > 2) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if ((rc = prepare_values(h, val)) || (rc = form_prec(h, prec)) || (rc = vec_in(h, b, h->v.r))) return rc;
+    if (prec == 2) {
+        int cnt = 0;
+        if ((rc = launch_sweeps<double>(h, h->stream, 1, h->v.r, nullptr, h->v.y, nullptr, h->v.z, nullptr, &cnt))) return rc;
+    } else {
+        k_diag_apply<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(h->n_int, h->v.d, h->v.r, h->v.z);
+        CKL("diag apply");
+    }
+    return vec_out(h, h->v.z, x);
+}
+
+extern "C" int tfs_get_stats(const tfs_handle *h, tfs_stats *out)
+{
+    if (!h || !out) return TFS_ERR_ARG;
+    *out = h->stats;
+    return TFS_OK;
+}
+
+extern "C" int tfs_get_levels(const tfs_handle *h, int32_t *levels)
+{
+    if (!h || !levels) return TFS_ERR_ARG;
+    memcpy(levels, h->levels_nat.data(), sizeof(int32_t) * (size_t)h->n);
+    return TFS_OK;
+}
+
+extern "C" int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int reps, double *ms)
+{
+    if (!h || !val || !ms || reps < 1 || (mode != TFS_FP64 && mode != TFS_MIXED)) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = prepare_values(h, val);
+    if (rc) return rc;
+    SellDev A = sell_of(h);
+    cudaStream_t s = h->stream;
+    // p = 1 on real rows so the products are finite.
+    k_diag_form<<<(h->n_int + 255) / 256, 256, 0, s>>>(A, h->val, h->v.p, 0);
+    tfs_mixed_fill32(h, h->v.p, h->f.p);
+    auto launch = [&]() {
+        if (mode == TFS_FP64) k_spmv_pq<<<h->grid, TFS_TPB, 0, s>>>(A, h->val, h->v.p, h->v.q, h->st, h->part);
+        else tfs_mixed_spmv_only(h, s);
+    };
+    for (int w = 0; w < 3; w++) launch();
+    CKL("spmv warm-up");
+    CK(cudaEventRecord(h->ev0, s));
+    for (int r = 0; r < reps; r++) launch();
+    CK(cudaEventRecord(h->ev1, s));
+    CK(cudaEventSynchronize(h->ev1));
+    CKL("spmv timing");
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
+    *ms = (double)t / reps;
+    return TFS_OK;
+}

@@ -1,0 +1,118 @@
+// tfs_internal.h -- device layout and per-handle state of libtfs_gb300.
+//
+// Layout in HBM (one handle = one registered topology):
+//   internal row order   rows sorted by DIC level (level 0 first), natural
+//                        order inside a level, each level padded with empty
+//                        rows to a multiple of 32, the total padded to a
+//                        multiple of TFS_TPB.  perm[internal] = natural row
+//                        (or -1 for a padding row), iperm[natural] = internal.
+//   SELL-32 matrix       slice s = internal rows 32s..32s+31, entries stored
+//                        column-major: entry j of the row in lane t sits at
+//                        slice_off[s] + 32*j + t.  Entries keep the reference's
+//                        ascending column order, so j < dpos are the lower
+//                        triangle, j == dpos the diagonal, j > dpos the upper.
+//                        col[] holds internal column numbers.
+//   rowinfo[i]           len | dpos << 16 (len == 0 marks a padding row).
+//   vectors              binary64 (and binary32 for TFS_MIXED), n_int long,
+//                        in internal order; padding rows stay exactly zero.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <map>
+#include <vector>
+
+#include "../../include/tfs_solver.h"
+
+#define TFS_TPB 256           // threads per block = rows per chunk
+#define TFS_NPART 4           // values reduced at once, at most
+
+// Device-resident state of one solve.  Written by k_init from DevParams and
+// then only by the last block of each reducing kernel.
+struct DevState {
+    double tol;
+    int niter_max;
+    int prec;
+    double bnrm2, ini_res, error, fin_res;
+    double rho, rho_old, alpha, beta;
+    int iter, done, niter_out, status;
+    int early, loops, loop_limit, true_res;
+    unsigned int counter;
+    unsigned int pad0;
+    unsigned long long t_spmv0, t_sweep0;
+    unsigned long long spmv_ns, spmv_n, sweep_ns, sweep_n;
+    // TFS_MIXED bookkeeping
+    double r_true;       // norm of the last binary64 true residual
+    double delta;        // reliable-update threshold
+    int need_true;       // the next true-residual step must run
+    int pad1;
+};
+
+// Per-call arguments, written by the host before every graph launch.
+struct DevParams {
+    double tol;
+    int niter_max;
+    int pad;
+    const double *val_csr;   // natural CSR order, nnz
+    const double *b;         // natural order, n (r1 on entry)
+    double *x;               // natural order, n (in/out)
+    double *r_out;           // natural order, n (r1 on return)
+};
+
+struct SellDev {
+    int n_int;
+    int n_chunks;
+    const uint32_t *rowinfo;
+    const int *slice_off;
+    const int *col;
+};
+
+// Work vectors (binary64).
+struct Vec64 {
+    double *x, *r, *r2, *p, *p2, *q, *q2, *u1, *u2, *v2, *w, *d, *y, *y2, *z, *z2;
+};
+// Work vectors (binary32) of the mixed-precision inner iteration.
+struct Vec32 {
+    float *r, *r2, *p, *p2, *q, *q2, *u1, *u2, *v2, *w, *d, *y, *y2, *z, *z2;
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    int prologue_kernels = 0, body_kernels = 0, epilogue_kernels = 0;
+};
+
+struct tfs_handle {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr, stream2 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int32_t n = 0, nnz = 0;
+    int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
+    int grid = 0;                      // blocks of the chunk kernels
+    int precision = TFS_FP64;
+    std::vector<int> lvl_begin;        // internal row offset of every level (+end)
+    std::vector<int32_t> levels_nat;   // level per natural row
+    uint64_t fingerprint = 0;
+    // device arrays
+    int *perm = nullptr, *iperm = nullptr, *slice_off = nullptr, *col = nullptr, *vmap = nullptr;
+    uint32_t *rowinfo = nullptr;
+    double *val = nullptr;
+    float *val32 = nullptr;
+    double *stage_val = nullptr, *stage_b = nullptr, *stage_x = nullptr;
+    double *part = nullptr;
+    DevState *st = nullptr;
+    DevParams *params = nullptr;
+    void *vec_pool = nullptr, *vec32_pool = nullptr;
+    Vec64 v{};
+    Vec32 f{};
+    // pinned host mirror of params and state
+    DevParams *h_params = nullptr;
+    DevState *h_state = nullptr;
+    std::map<int, GraphEntry> graphs;  // key: method | prec << 4 | precision << 8
+    tfs_stats stats{};
+    int64_t device_bytes = 0;
+};
+
+// tfs_engine.cu
+int tfs_engine_error(cudaError_t e, const char *what);
+void tfs_set_error_text(const char *msg);

@@ -1,0 +1,704 @@
+// tfs_kernels.cuh -- binary64 kernels of the preconditioned Krylov solves.
+//
+// Every kernel keeps the reference's per-row arithmetic: a row sum starts
+// where the Fortran loop starts (0.0, b(i) or x(i)) and adds the products of
+// the row one at a time in ascending column order; products and sums are
+// rounded separately (the library is compiled with --fmad=false); divisions
+// and square roots are the IEEE-rounded operators.  Only the order of the dot
+// product sums differs from the sequential i = 1..N loops of the reference:
+// they are fixed-shape tree reductions (warp shuffles, then one partial per
+// block, then the last block to finish sums the partials in block order), so
+// a solve is bitwise reproducible from run to run.
+#pragma once
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "tfs_internal.h"
+
+namespace tfs {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr double TINY = 1.e-30;   // Sources/Shared/allp_mod.f90:40
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+struct RowGeom {
+    int len, dpos, off;
+};
+__device__ __forceinline__ RowGeom row_geom(const SellDev &A, int i)
+{
+    uint32_t info = __ldg(A.rowinfo + i);
+    RowGeom g;
+    g.len = (int)(info & 0xffffu);
+    g.dpos = (int)(info >> 16);
+    g.off = __ldg(A.slice_off + (i >> 5)) + (i & 31);
+    return g;
+}
+
+// Sequential sum s - sum_{j0<=j<j1} a_j x_col(j) (SUB) or s + ... (ADD),
+// loads of four entries issued before their products are summed in order.
+template <bool SUB, typename VT, typename XT, typename AT>
+__device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
+                                        const VT *__restrict__ val,
+                                        const XT *__restrict__ x, int off, int j0, int j1)
+{
+    int j = j0;
+    for (; j + 4 <= j1; j += 4) {
+        int e0 = off + (j << 5), e1 = e0 + 32, e2 = e0 + 64, e3 = e0 + 96;
+        int k0 = __ldg(col + e0), k1 = __ldg(col + e1), k2 = __ldg(col + e2), k3 = __ldg(col + e3);
+        AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1), a2 = (AT)__ldg(val + e2), a3 = (AT)__ldg(val + e3);
+        AT x0 = (AT)x[k0], x1 = (AT)x[k1], x2 = (AT)x[k2], x3 = (AT)x[k3];
+        if (SUB) { s = s - a0 * x0; s = s - a1 * x1; s = s - a2 * x2; s = s - a3 * x3; }
+        else     { s = s + a0 * x0; s = s + a1 * x1; s = s + a2 * x2; s = s + a3 * x3; }
+    }
+    for (; j < j1; j++) {
+        int e = off + (j << 5);
+        AT a = (AT)__ldg(val + e), xv = (AT)x[__ldg(col + e)];
+        if (SUB) s = s - a * xv; else s = s + a * xv;
+    }
+    return s;
+}
+
+// Two right-hand sides through one pass over the row (Bicg.f90:136-144).
+template <bool SUB, typename VT, typename XT, typename AT>
+__device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict__ col,
+                                           const VT *__restrict__ val, const XT *__restrict__ x1,
+                                           const XT *__restrict__ x2, int off, int j0, int j1)
+{
+    int j = j0;
+    for (; j + 2 <= j1; j += 2) {
+        int e0 = off + (j << 5), e1 = e0 + 32;
+        int k0 = __ldg(col + e0), k1 = __ldg(col + e1);
+        AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1);
+        AT p0 = (AT)x1[k0], p1 = (AT)x1[k1], q0 = (AT)x2[k0], q1 = (AT)x2[k1];
+        if (SUB) { s1 = s1 - a0 * p0; s2 = s2 - a0 * q0; s1 = s1 - a1 * p1; s2 = s2 - a1 * q1; }
+        else     { s1 = s1 + a0 * p0; s2 = s2 + a0 * q0; s1 = s1 + a1 * p1; s2 = s2 + a1 * q1; }
+    }
+    for (; j < j1; j++) {
+        int e = off + (j << 5);
+        int k = __ldg(col + e);
+        AT a = (AT)__ldg(val + e);
+        if (SUB) { s1 = s1 - a * (AT)x1[k]; s2 = s2 - a * (AT)x2[k]; }
+        else     { s1 = s1 + a * (AT)x1[k]; s2 = s2 + a * (AT)x2[k]; }
+    }
+}
+
+// Fixed-shape block sum of NV values; the result is valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*sm)[TFS_TPB / 32])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = v[k] + __shfl_down_sync(FULL, v[k], o);
+        if (lane == 0) sm[k][warp] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = sm[k][0];
+#pragma unroll
+            for (int w = 1; w < TFS_TPB / 32; w++) s = s + sm[k][w];
+            v[k] = s;
+        }
+    }
+}
+
+// Single-pass grid reduction: every block publishes one partial per value,
+// the last block to arrive sums the partials in block order.  Returns true
+// in thread 0 of that last block, with the totals in v.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict__ part,
+                                            unsigned int *counter)
+{
+    __shared__ double sm[NV][TFS_TPB / 32];
+    __shared__ unsigned int is_last;
+    block_sum<NV>(v, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        is_last = (atomicAdd(counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double a[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) a[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += TFS_TPB) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) a[k] = a[k] + __ldcg(part + k * gridDim.x + b);
+    }
+    __syncthreads();  // sm is reused
+    block_sum<NV>(a, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] = a[k];
+        *counter = 0u;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void set_cond(cudaGraphConditionalHandle cond, unsigned v)
+{
+    if (cond) cudaGraphSetConditional(cond, v);
+}
+
+// Convergence test and bookkeeping at the end of one iteration, run by one
+// thread: Cg.f90:167-176 (Bicg.f90:180-189, Cgs.f90:212-221).
+__device__ __forceinline__ void finish_iteration(DevState *st, double e2, double rho_next,
+                                                 bool fused_rho, cudaGraphConditionalHandle cond)
+{
+    double err = sqrt(e2);
+    st->error = err;
+    st->fin_res = err;
+    int it = st->iter;
+    if (!(err <= DBL_MAX)) {                 // NaN or Inf: breakdown
+        st->status = TFS_ERR_NONFINITE;
+        st->done = 1;
+        st->niter_out = (st->niter_max > 0 ? st->niter_max : 0) + 1;
+    } else if (err < st->tol) {
+        st->done = 1;
+        st->niter_out = it;
+    } else if (it >= st->niter_max) {        // DO loop exhausted: iter = niter + 1
+        st->done = 1;
+        st->niter_out = it + 1;
+    } else {
+        st->iter = it + 1;
+        st->rho_old = st->rho;               // Cg.f90:176
+        if (fused_rho) st->rho = rho_next;
+    }
+    st->loops = st->loops + 1;
+    if (!st->done && st->loops >= st->loop_limit) {
+        st->done = 1;
+        st->status = TFS_ERR_TIMEOUT;
+        st->niter_out = it + 1;
+    }
+    set_cond(cond, st->done ? 0u : 1u);
+}
+
+// ---------------------------------------------------------------- prologue
+
+__global__ void k_init(DevState *st, const DevParams *prm, int prec)
+{
+    DevState s = {};
+    s.tol = prm->tol;
+    s.niter_max = prm->niter_max;
+    s.prec = prec;
+    s.iter = 1;
+    s.loop_limit = (prm->niter_max > 0 ? prm->niter_max : 0) + 8;
+    s.delta = 0.1;
+    *st = s;
+}
+
+// val (internal SELL order) <- val_csr (natural CSR order) through vmap.
+__global__ void k_gather_val(const int *__restrict__ vmap, const DevParams *prm,
+                             double *__restrict__ val, float *__restrict__ val32, int nnz_pad)
+{
+    const double *src = prm->val_csr;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nnz_pad; e += gridDim.x * blockDim.x) {
+        int m = __ldg(vmap + e);
+        double v = m >= 0 ? src[m] : 0.0;
+        val[e] = v;
+        if (val32) val32[e] = (float)v;
+    }
+}
+
+// r <- b, x <- x0 in internal order; d <- a_ii (prec 1) or 1; ||b|| and the
+// first early exit (Cg.f90:48-58).
+__global__ void __launch_bounds__(TFS_TPB)
+k_load(SellDev A, const double *__restrict__ val, const int *__restrict__ perm,
+       const DevParams *prm, Vec64 V, DevState *st, double *part, int prec)
+{
+    const double *b = prm->b, *x0 = prm->x;
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        int o = __ldg(perm + i);
+        double bi = 0.0, xi = 0.0;
+        if (o >= 0) { bi = b[o]; xi = x0[o]; }
+        V.r[i] = bi;
+        V.x[i] = xi;
+        acc = acc + bi * bi;
+        RowGeom g = row_geom(A, i);
+        V.d[i] = (prec == 1 && g.len > 0) ? val[g.off + (g.dpos << 5)] : 1.0;
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        double bnrm2 = sqrt(v[0]);
+        st->bnrm2 = bnrm2;
+        if (bnrm2 < st->tol) {
+            st->done = 1;
+            st->early = 1;
+            st->niter_out = 0;
+            st->error = bnrm2;
+            st->fin_res = bnrm2;
+        }
+    }
+}
+
+// Diagonal incomplete Cholesky, one level of rows (Prec_Form.f90:32-40):
+// D_i = 1 / (a_ii - sum_{lower j} D_col(j) a_j a_j).
+__global__ void __launch_bounds__(TFS_TPB)
+k_dic_form(SellDev A, const double *__restrict__ val, double *d, int row0, int row1,
+           const DevState *st)
+{
+    if (st->done) return;
+    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
+    if (i >= row1) return;
+    RowGeom g = row_geom(A, i);
+    if (g.len == 0) { d[i] = 1.0; return; }
+    double sum1 = __ldg(val + g.off + (g.dpos << 5));
+    for (int j = 0; j < g.dpos; j++) {
+        int e = g.off + (j << 5);
+        int k = __ldg(A.col + e);
+        double a = __ldg(val + e);
+        sum1 = sum1 - d[k] * a * a;
+    }
+    d[i] = 1.0 / sum1;
+}
+
+// r1 <- r1 - A x (Residual.f90:22-27), ||r0|| and the second early exit
+// (Cg.f90:63-90).  For BiCG/CGS also r2 = r1 (Bicg.f90:91-93, Cgs.f90:71-73).
+// rho of the first iteration is computed here when it needs no sweep.
+// method: 0 CG, 1 BiCG, 2 CGS.
+template <int METHOD>
+__global__ void __launch_bounds__(TFS_TPB)
+k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, double *part,
+           int prec, cudaGraphConditionalHandle cond)
+{
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
+    const bool fused = (METHOD == 2) || prec != 2;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        double r = row_accum<true, double, double, double>(V.r[i], A.col, val, V.x, g.off, 0, g.len);
+        V.r[i] = r;
+        if (METHOD != 0) V.r2[i] = r;
+        e2 = e2 + r * r;
+        if (METHOD == 2) rz = rz + r * r;               // Cgs.f90:105-109, r2 = r1
+        else if (fused) { double z = r / V.d[i]; rz = rz + (METHOD == 0 ? r * z : z * r); }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) {
+        double err = sqrt(v[0]);
+        st->error = err;
+        st->fin_res = err;
+        st->ini_res = err;
+        if (!(err <= DBL_MAX)) {
+            st->status = TFS_ERR_NONFINITE;
+            st->done = 1;
+            st->niter_out = (st->niter_max > 0 ? st->niter_max : 0) + 1;
+        } else if (err < st->tol) {
+            st->done = 1;
+            st->early = 2;
+            st->niter_out = 0;
+        } else if (st->niter_max <= 0) {     // zero-trip DO loop leaves iter = 1
+            st->done = 1;
+            st->niter_out = 1;
+        } else if (fused) {
+            st->rho = v[1];
+        }
+        set_cond(cond, st->done ? 0u : 1u);
+    }
+}
+
+// ------------------------------------------------------- level-scheduled DIC
+
+// Forward sweep of one level (Prec_Solve.f90:46-53) for NR right-hand sides:
+// y_i = (b_i - sum_{lower j} a_j y_col(j)) * D_i.  T = double is the
+// reference arithmetic; T = float serves the mixed-precision inner loop.
+template <typename T, int NR>
+__global__ void __launch_bounds__(TFS_TPB)
+k_fwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
+      const T *b1, const T *b2, T *y1, T *y2, int row0, int row1,
+      DevState *st, int first)
+{
+    if (st->done) return;
+    if (first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
+    if (i >= row1) return;
+    RowGeom g = row_geom(A, i);
+    if (g.len == 0) {
+        y1[i] = (T)0;
+        if (NR == 2) y2[i] = (T)0;
+        return;
+    }
+    T di = d[i];
+    if (NR == 1) {
+        T s = row_accum<true, T, T, T>(b1[i], A.col, val, y1, g.off, 0, g.dpos);
+        y1[i] = s * di;
+    } else {
+        T s1 = b1[i], s2 = b2[i];
+        row_accum2<true, T, T, T>(s1, s2, A.col, val, y1, y2, g.off, 0, g.dpos);
+        y1[i] = s1 * di;
+        y2[i] = s2 * di;
+    }
+}
+
+// Scaling and backward sweep of one level (Prec_Solve.f90:55-67):
+// z_i = (y_i / (D_i + TINY) - sum_{upper j} a_j z_col(j)) * D_i.
+template <typename T, int NR>
+__global__ void __launch_bounds__(TFS_TPB)
+k_bwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
+      const T *y1, const T *y2, T *z1, T *z2, int row0, int row1,
+      DevState *st)
+{
+    if (st->done) return;
+    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
+    if (i >= row1) return;
+    RowGeom g = row_geom(A, i);
+    if (g.len == 0) {
+        z1[i] = (T)0;
+        if (NR == 2) z2[i] = (T)0;
+        return;
+    }
+    T di = d[i];
+    const T tiny = (T)TINY;
+    if (NR == 1) {
+        T s = y1[i] / (di + tiny);
+        s = row_accum<true, T, T, T>(s, A.col, val, z1, g.off, g.dpos + 1, g.len);
+        z1[i] = s * di;
+    } else {
+        T s1 = y1[i] / (di + tiny), s2 = y2[i] / (di + tiny);
+        row_accum2<true, T, T, T>(s1, s2, A.col, val, z1, z2, g.off, g.dpos + 1, g.len);
+        z1[i] = s1 * di;
+        z2[i] = s2 * di;
+    }
+}
+
+// rho after the sweeps: CG (r, z) (Cg.f90:108-112); BiCG (z1, r2) (Bicg.f90:113-117).
+template <int METHOD>
+__global__ void __launch_bounds__(TFS_TPB)
+k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
+{
+    if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
+    }
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        acc = acc + (METHOD == 0 ? V.r[i] * V.z[i] : V.z[i] * V.r2[i]);
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
+}
+
+// ---------------------------------------------------------------- CG body
+
+// p = z (first iteration) or z + beta p (Cg.f90:114-123); z = r/d unless the
+// DIC sweeps produced it (FROMZ).
+template <bool FROMZ>
+__global__ void __launch_bounds__(TFS_TPB) k_cg_p(int n_chunks, Vec64 V, const DevState *st)
+{
+    if (st->done) return;
+    const int it = st->iter;
+    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        double z = FROMZ ? V.z[i] : V.r[i] / V.d[i];
+        V.p[i] = it == 1 ? z : z + beta * V.p[i];
+    }
+}
+
+// q = A p (Cg.f90:128-134) fused with (p, q) and alpha = rho / (p, q)
+// (Cg.f90:148-153).
+__global__ void __launch_bounds__(TFS_TPB)
+k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ p,
+          double *__restrict__ q, DevState *st, double *part)
+{
+    if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        double s = row_accum<false, double, double, double>(0.0, A.col, val, p, g.off, 0, g.len);
+        q[i] = s;
+        acc = acc + p[i] * s;
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+// x += alpha p, r -= alpha q (Cg.f90:159-162), ||r|| and the test; with
+// FUSED also rho of the next iteration, (r, r/d).
+template <bool FUSED>
+__global__ void __launch_bounds__(TFS_TPB)
+k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond)
+{
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
+    const double alfa = st->alpha;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * V.p[i];
+        double r = V.r[i] - alfa * V.q[i];
+        V.r[i] = r;
+        e2 = e2 + r * r;
+        if (FUSED) { double z = r / V.d[i]; rz = rz + r * z; }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
+}
+
+// -------------------------------------------------------------- BiCG body
+
+template <bool FROMZ>
+__global__ void __launch_bounds__(TFS_TPB) k_bicg_p(int n_chunks, Vec64 V, const DevState *st)
+{
+    if (st->done) return;
+    const int it = st->iter;
+    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        double z1, z2;
+        if (FROMZ) { z1 = V.z[i]; z2 = V.z2[i]; }
+        else { double di = V.d[i]; z1 = V.r[i] / di; z2 = V.r2[i] / di; }
+        if (it == 1) { V.p[i] = z1; V.p2[i] = z2; }
+        else { V.p[i] = z1 + beta * V.p[i]; V.p2[i] = z2 + beta * V.p2[i]; }
+    }
+}
+
+// q1 = A p1 and q2 = A p2 in one pass over A (Bicg.f90:136-144), fused with
+// (p2, q1) and alpha (Bicg.f90:160-165).
+__global__ void __launch_bounds__(TFS_TPB)
+k_spmv2_pq(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, double *part)
+{
+    if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        double s1 = 0.0, s2 = 0.0;
+        row_accum2<false, double, double, double>(s1, s2, A.col, val, V.p, V.p2, g.off, 0, g.len);
+        V.q[i] = s1;
+        V.q2[i] = s2;
+        acc = acc + V.p2[i] * s1;
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+// x += alpha p1, r1 -= alpha q1, r2 -= alpha q2 (Bicg.f90:171-175), ||r1||,
+// test; with FUSED rho of the next iteration (r1/d, r2).
+template <bool FUSED>
+__global__ void __launch_bounds__(TFS_TPB)
+k_bicg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond)
+{
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
+    const double alfa = st->alpha;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * V.p[i];
+        double r1 = V.r[i] - alfa * V.q[i];
+        double r2 = V.r2[i] - alfa * V.q2[i];
+        V.r[i] = r1;
+        V.r2[i] = r2;
+        e2 = e2 + r1 * r1;
+        if (FUSED) { double z1 = r1 / V.d[i]; rz = rz + z1 * r2; }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
+}
+
+// --------------------------------------------------------------- CGS body
+
+// u1 = r1 + beta q1, u2 = u1 + beta (q1 + beta u2) (Cgs.f90:111-122); with
+// FUSEDP also p2 = u2 / d (Prec_Solve for prec 0/1).
+template <bool FUSEDP>
+__global__ void __launch_bounds__(TFS_TPB) k_cgs_u(int n_chunks, Vec64 V, const DevState *st)
+{
+    if (st->done) return;
+    const int it = st->iter;
+    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        double u1, u2;
+        if (it == 1) { u1 = V.r[i]; u2 = u1; }
+        else {
+            double q1 = V.q[i];
+            u1 = V.r[i] + beta * q1;
+            u2 = u1 + beta * (q1 + beta * V.u2[i]);
+        }
+        V.u1[i] = u1;
+        V.u2[i] = u2;
+        if (FUSEDP) V.p2[i] = u2 / V.d[i];
+    }
+}
+
+// v2 = A p2 (Cgs.f90:132-139) with (r2, v2) and alpha (Cgs.f90:153-158).
+__global__ void __launch_bounds__(TFS_TPB)
+k_spmv_v(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, double *part)
+{
+    if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        double s = row_accum<false, double, double, double>(0.0, A.col, val, V.p2, g.off, 0, g.len);
+        V.v2[i] = s;
+        acc = acc + V.r2[i] * s;
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+// q1 = u1 - alpha v2 (Cgs.f90:163-165), w = u1 + q1 (Cgs.f90:170-172); with
+// FUSEDP p1 = w / d, else w is stored for the DIC sweeps.
+template <bool FUSEDP>
+__global__ void __launch_bounds__(TFS_TPB) k_cgs_q(int n_chunks, Vec64 V, const DevState *st)
+{
+    if (st->done) return;
+    const double alfa = st->alpha;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        double u1 = V.u1[i];
+        double q1 = u1 - alfa * V.v2[i];
+        V.q[i] = q1;
+        double w = u1 + q1;
+        if (FUSEDP) V.p[i] = w / V.d[i];
+        else V.w[i] = w;
+    }
+}
+
+// x += alpha p1 (Cgs.f90:178-180); q2 = A p1 (Cgs.f90:185-191);
+// r1 -= alpha q2 (Cgs.f90:205-207); ||r1||, test, rho = (r1, r2) of the next
+// iteration.  q2 is used only here and is not stored.
+__global__ void __launch_bounds__(TFS_TPB)
+k_cgs_spmv_r(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, double *part,
+             cudaGraphConditionalHandle cond)
+{
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    const double alfa = st->alpha;
+    double e2 = 0.0, rr = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * V.p[i];
+        RowGeom g = row_geom(A, i);
+        double q2 = row_accum<false, double, double, double>(0.0, A.col, val, V.p, g.off, 0, g.len);
+        double r1 = V.r[i] - alfa * q2;
+        V.r[i] = r1;
+        e2 = e2 + r1 * r1;
+        rr = rr + r1 * V.r2[i];
+    }
+    double v[2] = {e2, rr};
+    if (grid_reduce<2>(v, part, &st->counter)) {
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+        finish_iteration(st, v[0], v[1], true, cond);
+    }
+}
+
+// --------------------------------------------------------------- epilogue
+
+// x and r1 back to natural order.
+__global__ void k_store(int n_int, const int *__restrict__ perm, const double *__restrict__ x,
+                        const double *__restrict__ r, const DevParams *prm)
+{
+    double *xo = prm->x, *ro = prm->r_out;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x) {
+        int o = __ldg(perm + i);
+        if (o >= 0) { xo[o] = x[i]; ro[o] = r[i]; }
+    }
+}
+
+// ------------------------------------------------------ single routines
+
+__global__ void k_perm_in(int n_int, const int *__restrict__ perm, const double *__restrict__ src,
+                          double *__restrict__ dst)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x) {
+        int o = __ldg(perm + i);
+        dst[i] = o >= 0 ? src[o] : 0.0;
+    }
+}
+
+__global__ void k_perm_out(int n_int, const int *__restrict__ perm, const double *__restrict__ src,
+                           double *__restrict__ dst)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x) {
+        int o = __ldg(perm + i);
+        if (o >= 0) dst[o] = src[i];
+    }
+}
+
+// Diagonal of the preconditioner for prec 0 / 1 (Prec_Form.f90:24-27, 45-49).
+__global__ void k_diag_form(SellDev A, const double *__restrict__ val, double *d, int prec)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n_int; i += gridDim.x * blockDim.x) {
+        RowGeom g = row_geom(A, i);
+        d[i] = (prec == 1 && g.len > 0) ? val[g.off + (g.dpos << 5)] : 1.0;
+    }
+}
+
+// x = b / d (Prec_Solve.f90:35-38; with d = 1 the copy of :71-74).
+__global__ void k_diag_apply(int n_int, const double *__restrict__ d, const double *__restrict__ b,
+                             double *__restrict__ x)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x)
+        x[i] = b[i] / d[i];
+}
+
+// ------------------------------------------------- dependency analysis
+
+// One relaxation pass of level(i) = max(0, 1 + max_{lower j} level(col j)).
+// Levels only grow and never exceed their fixed point, so passes run in
+// place until one changes nothing.
+__global__ void k_level_pass(int n, const int *__restrict__ row0, const int *__restrict__ col0,
+                             const int *__restrict__ dia0, int *level, int *changed)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int l = 0;
+        for (int j = __ldg(row0 + i); j < __ldg(dia0 + i); j++) {
+            int lk = ((volatile int *)level)[__ldg(col0 + j)] + 1;
+            l = lk > l ? lk : l;
+        }
+        if (l > level[i]) {
+            level[i] = l;
+            *changed = 1;
+        }
+    }
+}
+
+}  // namespace tfs

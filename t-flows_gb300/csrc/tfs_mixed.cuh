@@ -1,0 +1,340 @@
+// tfs_mixed.cuh -- kernels of the mixed-precision (TFS_MIXED) Krylov solves.
+//
+// The Krylov recurrences run on binary32 matrix values and binary32 vectors
+// (r, p, q, z, ...), which cuts the bytes per iteration by about a third.
+// Binary64 is kept where the accuracy is decided:
+//   - every dot product (rho, (p,q), ||r||) accumulates in binary64;
+//   - alpha and beta are binary64 scalars;
+//   - the solution x is binary64 and takes x += alpha * p in binary64;
+//   - the true residual r = b - A x is recomputed in binary64 with the
+//     binary64 matrix ("reliable update" defect correction) whenever the
+//     binary32 recursive residual has dropped by the factor delta (0.1) since
+//     the last true residual, or claims convergence, or the iteration limit
+//     is reached.  The binary32 residual is then replaced by the true one and
+//     the search direction is kept, so the Krylov space is not restarted.
+// Convergence is declared only on a binary64 true residual, so fin_res and
+// r1 on return are b - A x in binary64.
+#pragma once
+#include "tfs_kernels.cuh"
+
+namespace tfs {
+
+__global__ void k_mx_cast(int n_int, const double *__restrict__ src, float *__restrict__ dst)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+// Binary64 true residual r = b - A x (b kept in V.u1), copied to the binary32
+// residual, with ||r|| and the next rho.  INIT: the first residual of the
+// solve (Residual.f90 + Cg.f90:75-90 semantics, b saved first, shadow r2 set).
+template <int METHOD, bool INIT>
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState *st,
+          double *part, int prec, cudaGraphConditionalHandle cond)
+{
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
+    if (!INIT && !st->need_true) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 1u);
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    const bool fused = (METHOD == 2) || prec != 2;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        double b;
+        if (INIT) { b = V.r[i]; V.u1[i] = b; } else b = V.u1[i];
+        RowGeom g = row_geom(A, i);
+        double r = row_accum<true, double, double, double>(b, A.col, val, V.x, g.off, 0, g.len);
+        V.r[i] = r;
+        float r32 = (float)r;
+        F.r[i] = r32;
+        if (INIT && METHOD != 0) F.r2[i] = r32;
+        e2 = e2 + r * r;
+        if (METHOD == 2) rz = rz + (double)r32 * (double)F.r2[i];
+        else if (fused) {
+            float z = r32 / F.d[i];
+            rz = rz + (METHOD == 0 ? (double)r32 * (double)z : (double)z * (double)F.r2[i]);
+        }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) {
+        double err = sqrt(v[0]);
+        st->r_true = err;
+        st->true_res += 1;
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+        if (INIT) {
+            st->error = err;
+            st->fin_res = err;
+            st->ini_res = err;
+            if (!(err <= DBL_MAX)) {
+                st->status = TFS_ERR_NONFINITE;
+                st->done = 1;
+                st->niter_out = (st->niter_max > 0 ? st->niter_max : 0) + 1;
+            } else if (err < st->tol) {
+                st->done = 1;
+                st->early = 2;
+                st->niter_out = 0;
+            } else if (st->niter_max <= 0) {
+                st->done = 1;
+                st->niter_out = 1;
+            } else if (fused) {
+                st->rho = v[1];
+            }
+            set_cond(cond, st->done ? 0u : 1u);
+        } else {
+            st->need_true = 0;
+            finish_iteration(st, v[0], v[1], fused, cond);
+        }
+    }
+}
+
+// End of a binary32 iteration: either finish it on the recursive residual or
+// hand over to k_mx_true for a binary64 residual first.
+__device__ __forceinline__ void mx_end_iteration(DevState *st, double e2, double rz, bool fused)
+{
+    double est = sqrt(e2);
+    if (!(est <= DBL_MAX) || est < st->tol || est < st->delta * st->r_true ||
+        st->iter >= st->niter_max) {
+        st->need_true = 1;
+        st->error = est;
+    } else {
+        finish_iteration(st, e2, rz, fused, 0);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ double dd(T v) { return (double)v; }
+
+// rho = (r, z) / (z1, r2) after binary32 sweeps.
+template <int METHOD>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho(int n_chunks, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
+    }
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        acc = acc + (METHOD == 0 ? dd(F.r[i]) * dd(F.z[i]) : dd(F.z[i]) * dd(F.r2[i]));
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
+}
+
+// ---------------------------------------------------------------- CG
+
+template <bool FROMZ>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p(int n_chunks, Vec32 F, const DevState *st)
+{
+    if (st->done || st->need_true) return;
+    const int it = st->iter;
+    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        float z = FROMZ ? F.z[i] : F.r[i] / F.d[i];
+        F.p[i] = it == 1 ? z : z + beta * F.p[i];
+    }
+}
+
+// q = A p in binary32 with (p, q) in binary64 and alpha.
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__ p,
+             float *__restrict__ q, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        float s = row_accum<false, float, float, float>(0.f, A.col, val, p, g.off, 0, g.len);
+        q[i] = s;
+        acc = acc + dd(p[i]) * dd(s);
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    const double alfa = st->alpha;
+    const float alfa32 = (float)alfa;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
+        float r = F.r[i] - alfa32 * F.q[i];
+        F.r[i] = r;
+        e2 = e2 + dd(r) * dd(r);
+        if (FUSED) { float z = r / F.d[i]; rz = rz + dd(r) * dd(z); }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
+}
+
+// -------------------------------------------------------------- BiCG
+
+template <bool FROMZ>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_bicg_p(int n_chunks, Vec32 F, const DevState *st)
+{
+    if (st->done || st->need_true) return;
+    const int it = st->iter;
+    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        float z1, z2;
+        if (FROMZ) { z1 = F.z[i]; z2 = F.z2[i]; }
+        else { float di = F.d[i]; z1 = F.r[i] / di; z2 = F.r2[i] / di; }
+        if (it == 1) { F.p[i] = z1; F.p2[i] = z2; }
+        else { F.p[i] = z1 + beta * F.p[i]; F.p2[i] = z2 + beta * F.p2[i]; }
+    }
+}
+
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_spmv2_pq(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        float s1 = 0.f, s2 = 0.f;
+        row_accum2<false, float, float, float>(s1, s2, A.col, val, F.p, F.p2, g.off, 0, g.len);
+        F.q[i] = s1;
+        F.q2[i] = s2;
+        acc = acc + dd(F.p2[i]) * dd(s1);
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_bicg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    const double alfa = st->alpha;
+    const float alfa32 = (float)alfa;
+    double e2 = 0.0, rz = 0.0;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
+        float r1 = F.r[i] - alfa32 * F.q[i];
+        float r2 = F.r2[i] - alfa32 * F.q2[i];
+        F.r[i] = r1;
+        F.r2[i] = r2;
+        e2 = e2 + dd(r1) * dd(r1);
+        if (FUSED) { float z1 = r1 / F.d[i]; rz = rz + dd(z1) * dd(r2); }
+    }
+    double v[2] = {e2, rz};
+    if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
+}
+
+// --------------------------------------------------------------- CGS
+
+template <bool FUSEDP>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cgs_u(int n_chunks, Vec32 F, const DevState *st)
+{
+    if (st->done || st->need_true) return;
+    const int it = st->iter;
+    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        float u1, u2;
+        if (it == 1) { u1 = F.r[i]; u2 = u1; }
+        else {
+            float q1 = F.q[i];
+            u1 = F.r[i] + beta * q1;
+            u2 = u1 + beta * (q1 + beta * F.u2[i]);
+        }
+        F.u1[i] = u1;
+        F.u2[i] = u2;
+        if (FUSEDP) F.p2[i] = u2 / F.d[i];
+    }
+}
+
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_spmv_v(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    double acc = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        float s = row_accum<false, float, float, float>(0.f, A.col, val, F.p2, g.off, 0, g.len);
+        F.v2[i] = s;
+        acc = acc + dd(F.r2[i]) * dd(s);
+    }
+    double v[1] = {acc};
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->alpha = st->rho / v[0];
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+    }
+}
+
+template <bool FUSEDP>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cgs_q(int n_chunks, Vec32 F, const DevState *st)
+{
+    if (st->done || st->need_true) return;
+    const float alfa32 = (float)st->alpha;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        float u1 = F.u1[i];
+        float q1 = u1 - alfa32 * F.v2[i];
+        F.q[i] = q1;
+        float w = u1 + q1;
+        if (FUSEDP) F.p[i] = w / F.d[i];
+        else F.w[i] = w;
+    }
+}
+
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_cgs_spmv_r(SellDev A, const float *__restrict__ val, Vec64 V, Vec32 F, DevState *st,
+                double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    const double alfa = st->alpha;
+    const float alfa32 = (float)alfa;
+    double e2 = 0.0, rr = 0.0;
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
+        RowGeom g = row_geom(A, i);
+        float q2 = row_accum<false, float, float, float>(0.f, A.col, val, F.p, g.off, 0, g.len);
+        float r1 = F.r[i] - alfa32 * q2;
+        F.r[i] = r1;
+        e2 = e2 + dd(r1) * dd(r1);
+        rr = rr + dd(r1) * dd(F.r2[i]);
+    }
+    double v[2] = {e2, rr};
+    if (grid_reduce<2>(v, part, &st->counter)) {
+        st->spmv_ns += gtimer() - st->t_spmv0;
+        st->spmv_n += 1;
+        mx_end_iteration(st, v[0], v[1], true);
+    }
+}
+
+}  // namespace tfs

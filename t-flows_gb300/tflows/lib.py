@@ -1,0 +1,103 @@
+"""ctypes binding of libtfs_gb300.so (declarations in include/tfs_solver.h and
+include/tfs_synth.h).  The library is built in-tree by ``tflows.build``; a
+missing library raises instead of falling back to anything else."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+TFS_OK = 0
+TFS_ERR_ARG, TFS_ERR_MATRIX, TFS_ERR_CUDA, TFS_ERR_NONFINITE = 1, 2, 3, 4
+TFS_ERR_TOPOLOGY, TFS_ERR_TIMEOUT, TFS_ERR_BUDGET = 5, 6, 7
+TFS_CG, TFS_BICG, TFS_CGS = 0, 1, 2
+TFS_PREC_NONE, TFS_PREC_DIAG, TFS_PREC_DIC = 0, 1, 2
+TFS_FP64, TFS_MIXED = 0, 1
+TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF = 0, 1
+
+_PKG = Path(__file__).resolve().parent
+lib_path = _PKG / "lib" / "libtfs_gb300.so"
+
+i32, i64, u64, dbl = C.c_int32, C.c_int64, C.c_uint64, C.c_double
+P_i32, P_dbl, P_void = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p
+
+
+class tfs_stats(C.Structure):
+    _fields_ = [("iterations", i32), ("true_residuals", i32), ("n_levels", i32), ("status", i32),
+                ("solve_ms", dbl), ("spmv_ns_total", dbl), ("spmv_launches", i64),
+                ("sweep_ns_total", dbl), ("sweep_launches", i64), ("kernel_launches", i64),
+                ("device_bytes", i64)]
+
+
+class TfsError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: status {status} ({status_string(status)}) {detail}".rstrip())
+
+
+# (name, restype, argtypes) of every exported symbol of the C ABI.
+SIGNATURES = {
+    "tfs_topology_register": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, C.POINTER(P_void)]),
+    "tfs_release": (C.c_int, [P_void]),
+    "tfs_set_precision": (C.c_int, [P_void, C.c_int]),
+    "tfs_solve": (C.c_int, [C.c_int, P_void, i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl,
+                            i32, P_i32, dbl, P_dbl, P_dbl]),
+    "tfs_cg": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl, i32, P_i32, dbl, P_dbl, P_dbl]),
+    "tfs_bicg": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl, i32, P_i32, dbl, P_dbl, P_dbl]),
+    "tfs_cgs": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl, i32, P_i32, dbl, P_dbl, P_dbl]),
+    "tfs_solve_device": (C.c_int, [C.c_int, P_void, P_void, P_void, P_void, i32, P_i32, dbl, P_dbl, P_dbl]),
+    "tfs_spmv": (C.c_int, [P_void, P_dbl, P_dbl, P_dbl]),
+    "tfs_residual": (C.c_int, [P_void, P_dbl, P_dbl, P_dbl]),
+    "tfs_prec_form": (C.c_int, [P_void, P_dbl, i32, P_dbl]),
+    "tfs_prec_solve": (C.c_int, [P_void, P_dbl, i32, P_dbl, P_dbl]),
+    "tfs_get_stats": (C.c_int, [P_void, C.POINTER(tfs_stats)]),
+    "tfs_get_levels": (C.c_int, [P_void, P_i32]),
+    "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
+    "tfs_status_string": (C.c_char_p, [C.c_int]),
+    "tfs_last_error": (C.c_char_p, []),
+    "tfs_topology_count": (i32, [i32, i32, P_i32]),
+    "tfs_topology_build": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_i32, P_i32, P_i32]),
+    "tfs_synth_create": (C.c_int, [C.c_int, i32, i32, i32, dbl, u64, C.c_int, C.POINTER(P_void)]),
+    "tfs_synth_dims": (C.c_int, [P_void, P_i32, P_i32, P_i32]),
+    "tfs_synth_export": (C.c_int, [P_void, P_i32, P_i32, P_i32, P_i32, P_dbl, P_dbl]),
+    "tfs_synth_free": (None, [P_void]),
+    "tfs_synth_loguniform": (i64, [i64, i64, u64, u64]),
+    "tfs_synth_uniform": (dbl, [u64, u64, u64]),
+}
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load libtfs_gb300.so and declare its signatures (raises if absent)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else lib_path
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build it with `python -m tflows.build` "
+                                "(or __graft_entry__.build())")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load_library().tfs_status_string(status).decode()
+    except Exception:  # library not loadable: plain number
+        return str(status)
+
+
+def last_error() -> str:
+    return load_library().tfs_last_error().decode(errors="replace")
+
+
+def check(status: int, where: str) -> None:
+    if status != TFS_OK:
+        raise TfsError(status, where, last_error())

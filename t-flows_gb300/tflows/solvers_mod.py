@@ -1,0 +1,184 @@
+"""Solvers_Mod of T-FlowS (Sources/Process/Solvers_Mod.f90) on the GB300.
+
+``Cg``, ``Bicg`` and ``Cgs`` keep the argument meaning of the Fortran
+subroutines (Cg.f90:2-4): ``x`` and ``r1`` are updated in place (r1 enters as
+b and leaves as the final residual), ``tol`` is absolute, and the call returns
+what the Fortran writes back into ``niter``, ``ini_res`` and ``fin_res``.
+``ini_res`` is returned unchanged when ||b|| < tol, as in the reference.
+All work runs in libtfs_gb300.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import NamedTuple
+
+import numpy as np
+
+from .lib import (TFS_BICG, TFS_CG, TFS_CGS, TFS_ERR_NONFINITE, TFS_FP64, TFS_OK, TfsError,
+                  check, last_error, load_library, tfs_stats)
+from .matrix_mod import Matrix_Type, ptr
+
+_dbl, _i32 = C.c_double, C.c_int32
+
+
+class SolveResult(NamedTuple):
+    niter: int
+    ini_res: float
+    fin_res: float
+    status: int
+
+
+def _vec(a: np.ndarray, n: int, name: str) -> np.ndarray:
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous \
+            or a.shape != (n,):
+        raise ValueError(f"{name} must be a contiguous float64 array of length {n}")
+    return a
+
+
+class Solver:
+    """A registered topology (one tfs_handle): device layout, DIC level
+    schedule and work vectors stay resident between solves."""
+
+    def __init__(self, A: Matrix_Type, precision: int = TFS_FP64):
+        self.lib = load_library()
+        self.n, self.nnz = A.n_cells, A.nnz
+        self._row, self._col, self._dia = A.row, A.col, A.dia
+        h = C.c_void_p()
+        check(self.lib.tfs_topology_register(self.n, self.nnz, ptr(A.row, _i32), ptr(A.col, _i32),
+                                             ptr(A.dia, _i32), C.byref(h)), "tfs_topology_register")
+        self.h = h
+        self.set_precision(precision)
+
+    def set_precision(self, mode: int) -> None:
+        check(self.lib.tfs_set_precision(self.h, mode), "tfs_set_precision")
+        self.precision = mode
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.tfs_release(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, method: int, val: np.ndarray, x: np.ndarray, r1: np.ndarray, prec: int,
+              niter: int, tol: float, ini_res: float = 0.0) -> SolveResult:
+        val = _vec(val, self.nnz, "val")
+        x, r1 = _vec(x, self.n, "x"), _vec(r1, self.n, "r1")
+        it, ini, fin = _i32(niter), _dbl(ini_res), _dbl(0.0)
+        st = self.lib.tfs_solve(method, self.h, self.n, self.nnz, ptr(self._row, _i32),
+                                ptr(self._col, _i32), ptr(self._dia, _i32), ptr(val, _dbl),
+                                ptr(x, _dbl), ptr(r1, _dbl), prec, C.byref(it), tol,
+                                C.byref(ini), C.byref(fin))
+        if st not in (TFS_OK, TFS_ERR_NONFINITE):
+            raise TfsError(st, "tfs_solve", last_error())
+        return SolveResult(it.value, ini.value, fin.value, st)
+
+    def solve_device(self, method: int, d_val: int, d_x: int, d_r1: int, prec: int, niter: int,
+                     tol: float, ini_res: float = 0.0) -> SolveResult:
+        """Solve on device arrays given as raw CUDA pointers (natural order)."""
+        it, ini, fin = _i32(niter), _dbl(ini_res), _dbl(0.0)
+        st = self.lib.tfs_solve_device(method, self.h, C.c_void_p(d_val), C.c_void_p(d_x),
+                                       C.c_void_p(d_r1), prec, C.byref(it), tol, C.byref(ini),
+                                       C.byref(fin))
+        if st not in (TFS_OK, TFS_ERR_NONFINITE):
+            raise TfsError(st, "tfs_solve_device", last_error())
+        return SolveResult(it.value, ini.value, fin.value, st)
+
+    def spmv(self, val: np.ndarray, p: np.ndarray) -> np.ndarray:
+        q = np.empty(self.n)
+        check(self.lib.tfs_spmv(self.h, ptr(_vec(val, self.nnz, "val"), _dbl),
+                                ptr(_vec(p, self.n, "p"), _dbl), ptr(q, _dbl)), "tfs_spmv")
+        return q
+
+    def residual(self, val: np.ndarray, x: np.ndarray, r1: np.ndarray) -> None:
+        check(self.lib.tfs_residual(self.h, ptr(_vec(val, self.nnz, "val"), _dbl),
+                                    ptr(_vec(x, self.n, "x"), _dbl),
+                                    ptr(_vec(r1, self.n, "r1"), _dbl)), "tfs_residual")
+
+    def prec_form(self, val: np.ndarray, prec: int) -> np.ndarray:
+        d = np.empty(self.n)
+        check(self.lib.tfs_prec_form(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), prec,
+                                     ptr(d, _dbl)), "tfs_prec_form")
+        return d
+
+    def prec_solve(self, val: np.ndarray, prec: int, b: np.ndarray) -> np.ndarray:
+        x = np.empty(self.n)
+        check(self.lib.tfs_prec_solve(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), prec,
+                                      ptr(_vec(b, self.n, "b"), _dbl), ptr(x, _dbl)),
+              "tfs_prec_solve")
+        return x
+
+    def levels(self) -> np.ndarray:
+        lv = np.empty(self.n, np.int32)
+        check(self.lib.tfs_get_levels(self.h, ptr(lv, _i32)), "tfs_get_levels")
+        return lv
+
+    def stats(self) -> dict:
+        s = tfs_stats()
+        check(self.lib.tfs_get_stats(self.h, C.byref(s)), "tfs_get_stats")
+        return {k: getattr(s, k) for k, _ in tfs_stats._fields_}
+
+    def time_spmv(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
+        ms = _dbl(0.0)
+        check(self.lib.tfs_time_spmv(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), mode, reps,
+                                     C.byref(ms)), "tfs_time_spmv")
+        return ms.value
+
+
+def _solver_of(A: Matrix_Type) -> Solver:
+    if A._solver is None:
+        A._solver = Solver(A)
+    return A._solver
+
+
+def _call(method: int, A: Matrix_Type, x, r1, prec, niter, tol, ini_res):
+    res = _solver_of(A).solve(method, A.val, x, r1, prec, niter, tol, ini_res)
+    return res.niter, res.ini_res, res.fin_res
+
+
+def Cg(A: Matrix_Type, x: np.ndarray, r1: np.ndarray, prec: int, niter: int, tol: float,
+       ini_res: float = 0.0):
+    """Preconditioned CG (Cg.f90:2-183). Returns (niter, ini_res, fin_res)."""
+    return _call(TFS_CG, A, x, r1, prec, niter, tol, ini_res)
+
+
+def Bicg(A: Matrix_Type, x: np.ndarray, r1: np.ndarray, prec: int, niter: int, tol: float,
+         ini_res: float = 0.0):
+    """Preconditioned BiCG, A (not A^T) on the shadow system (Bicg.f90:2-196)."""
+    return _call(TFS_BICG, A, x, r1, prec, niter, tol, ini_res)
+
+
+def Cgs(A: Matrix_Type, x: np.ndarray, r1: np.ndarray, prec: int, niter: int, tol: float,
+        ini_res: float = 0.0):
+    """Preconditioned CGS (Cgs.f90:2-232)."""
+    return _call(TFS_CGS, A, x, r1, prec, niter, tol, ini_res)
+
+
+def Prec_Form(A: Matrix_Type, prec: int) -> np.ndarray:
+    """D % val(D % dia(i)) for i = 1..n (Prec_Form.f90:2-51)."""
+    return _solver_of(A).prec_form(A.val, prec)
+
+
+def Prec_Solve(A: Matrix_Type, b: np.ndarray, prec: int) -> np.ndarray:
+    """x = M^-1 b with M formed from A (Prec_Form.f90 then Prec_Solve.f90)."""
+    return _solver_of(A).prec_solve(A.val, prec, b)
+
+
+def Residual(A: Matrix_Type, x: np.ndarray, r1: np.ndarray) -> None:
+    """r1 <- r1 - A x in place (Residual.f90:2-40)."""
+    _solver_of(A).residual(A.val, x, r1)
+
+
+def spmv(A: Matrix_Type, p: np.ndarray) -> np.ndarray:
+    """q = A p (the product loop of Cg.f90:128-134)."""
+    return _solver_of(A).spmv(A.val, p)

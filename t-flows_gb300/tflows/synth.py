@@ -1,0 +1,55 @@
+"""Seeded synthetic systems (include/tfs_synth.h) for tests and benchmarks."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .lib import TFS_SYNTH_CONVDIFF, TFS_SYNTH_POISSON, check, load_library
+from .matrix_mod import Matrix_Type, ptr
+
+POISSON, CONVDIFF = TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF
+BASE_SEED = 20261203
+
+
+class SynthSystem:
+    """A jittered-hex finite-volume system: faces_c (1-based), CSR row/col/dia
+    (1-based), val and the right-hand side b."""
+
+    def __init__(self, kind: int, nx: int, ny: int | None = None, nz: int | None = None,
+                 jitter: float = 0.2, seed: int = BASE_SEED, permute: bool = True):
+        lib = load_library()
+        ny = nx if ny is None else ny
+        nz = nx if nz is None else nz
+        h = C.c_void_p()
+        check(lib.tfs_synth_create(kind, nx, ny, nz, float(jitter), seed & (2**64 - 1),
+                                   1 if permute else 0, C.byref(h)), "tfs_synth_create")
+        try:
+            n, nnz, nf = C.c_int32(), C.c_int32(), C.c_int32()
+            lib.tfs_synth_dims(h, C.byref(n), C.byref(nnz), C.byref(nf))
+            self.kind, self.dims, self.jitter, self.seed = kind, (nx, ny, nz), jitter, seed
+            self.n, self.nnz, self.n_faces = n.value, nnz.value, nf.value
+            self.faces_c = np.zeros((self.n_faces, 2), np.int32)
+            self.row = np.zeros(self.n + 1, np.int32)
+            self.col = np.zeros(self.nnz, np.int32)
+            self.dia = np.zeros(self.n, np.int32)
+            self.val = np.zeros(self.nnz)
+            self.b = np.zeros(self.n)
+            i32 = C.c_int32
+            check(lib.tfs_synth_export(h, ptr(self.faces_c, i32), ptr(self.row, i32),
+                                       ptr(self.col, i32), ptr(self.dia, i32),
+                                       ptr(self.val, C.c_double), ptr(self.b, C.c_double)),
+                  "tfs_synth_export")
+        finally:
+            lib.tfs_synth_free(h)
+
+    def matrix(self) -> Matrix_Type:
+        return Matrix_Type(self.n, self.row, self.col, self.dia, self.val)
+
+
+def loguniform(lo: int, hi: int, seed: int, index: int) -> int:
+    return int(load_library().tfs_synth_loguniform(lo, hi, seed & (2**64 - 1), index))
+
+
+def uniform(seed: int, stream: int, index: int) -> float:
+    return float(load_library().tfs_synth_uniform(seed & (2**64 - 1), stream, index))

@@ -1,0 +1,33 @@
+"""Shared helpers of the parity tests: seeded systems and oracle runs."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import tfs_oracle as O
+from tflows import SynthSystem
+from tflows.synth import CONVDIFF, POISSON
+
+# Iteration-count gate: +-2% of the oracle's count, never tighter than +-1.
+ITER_REL = 0.02
+# Solution gate: ||x_gpu - x_oracle||_2 / ||x_oracle||_2.
+SOL_REL = 1e-9
+
+
+def system(kind=POISSON, n=16, ny=None, nz=None, jitter=0.2, seed=20261203, permute=True):
+    return SynthSystem(kind, n, ny, nz, jitter=jitter, seed=seed, permute=permute)
+
+
+def oracle_solve(s, method, prec, niter=2000, rel=1e-8, x0=None):
+    x = np.zeros(s.n) if x0 is None else x0.copy()
+    r = s.b.copy()
+    tol = rel * float(np.sqrt(np.dot(s.b, s.b)))
+    it, ini, fin = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, niter, tol)
+    return dict(x=x, r=r, niter=it, ini=ini, fin=fin, tol=tol)
+
+
+def iter_ok(got: int, want: int) -> bool:
+    return abs(got - want) <= max(1, int(np.ceil(ITER_REL * want)))
+
+
+def rel_l2(a, b) -> float:
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

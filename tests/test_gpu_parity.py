@@ -1,0 +1,271 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle.
+
+Per-row routines (SpMV, Residual, Prec_Form, Prec_Solve) must be bitwise
+equal to the oracle: the kernels keep the reference's per-row arithmetic.
+Whole solves differ from the oracle only through the order of the dot
+product sums, so they are gated by the tolerances of the hot-path contract:
+iteration count within +-2% (never tighter than +-1) and solution relative L2
+difference <= 1e-9 at a 1e-8 relative stopping tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import SOL_REL, iter_ok, oracle_solve, rel_l2, system
+from oracle import tfs_oracle as O
+from tflows import (TFS_BICG, TFS_CG, TFS_CGS, TFS_FP64, TFS_MIXED, Matrix_Type, Solver)
+from tflows.lib import TFS_ERR_NONFINITE
+from tflows.synth import CONVDIFF, POISSON
+
+pytestmark = pytest.mark.gpu
+
+METHODS = [TFS_CG, TFS_BICG, TFS_CGS]
+PRECS = [0, 1, 2]
+
+
+@pytest.fixture(scope="module")
+def poisson16(gpu):
+    s = system(POISSON, 16)
+    return s, Solver(s.matrix())
+
+
+@pytest.fixture(scope="module")
+def convdiff12(gpu):
+    s = system(CONVDIFF, 12, 11, 10)
+    return s, Solver(s.matrix())
+
+
+# ------------------------------------------------------ per-row routines
+
+@pytest.mark.parametrize("which", ["poisson", "convdiff"])
+def test_spmv_bitwise(which, poisson16, convdiff12):
+    s, sol = poisson16 if which == "poisson" else convdiff12
+    p = np.random.default_rng(1).uniform(-1, 1, s.n)
+    q = sol.spmv(s.val, p)
+    assert np.array_equal(q, O.spmv(s.n, s.row, s.col, s.val, p))
+
+
+def test_residual_bitwise(poisson16):
+    s, sol = poisson16
+    x = np.random.default_rng(2).uniform(-1, 1, s.n)
+    r_gpu = s.b.copy()
+    sol.residual(s.val, x, r_gpu)
+    r_ref = s.b.copy()
+    O.residual(s.n, s.row, s.col, s.val, x, r_ref)
+    assert np.array_equal(r_gpu, r_ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("which", ["poisson", "convdiff"])
+def test_prec_form_bitwise(prec, which, poisson16, convdiff12):
+    s, sol = poisson16 if which == "poisson" else convdiff12
+    d = sol.prec_form(s.val, prec)
+    assert np.array_equal(d, O.prec_form(s.n, s.row, s.col, s.dia, s.val, prec))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("which", ["poisson", "convdiff"])
+def test_prec_solve_bitwise(prec, which, poisson16, convdiff12):
+    s, sol = poisson16 if which == "poisson" else convdiff12
+    b = np.random.default_rng(3).uniform(-1, 1, s.n)
+    x = sol.prec_solve(s.val, prec, b)
+    assert np.array_equal(x, O.prec_solve(s.n, s.row, s.col, s.dia, s.val, prec, b))
+
+
+def test_level_schedule_valid(poisson16):
+    """Every lower neighbour of a row sits on a strictly smaller level and the
+    levels are the longest-path depths (host recomputation)."""
+    s, sol = poisson16
+    lv = sol.levels()
+    want = np.zeros(s.n, np.int64)
+    for i in range(s.n):
+        lo = s.row[i] - 1
+        cols = s.col[lo:s.dia[i] - 1] - 1
+        want[i] = 0 if cols.size == 0 else 1 + want[cols].max()
+    assert np.array_equal(lv, want)
+
+
+def test_level_schedule_natural_order(gpu):
+    """Unpermuted cell numbering: the levels are the i+j+k hyperplanes."""
+    s = system(POISSON, 6, 5, 4, permute=False)
+    lv = Solver(s.matrix()).levels()
+    ijk = np.array([i + j + k for k in range(4) for j in range(5) for i in range(6)])
+    assert np.array_equal(lv, ijk)
+
+
+# ------------------------------------------------------ whole solves
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("method", METHODS)
+def test_solve_matches_oracle_poisson(method, prec, poisson16):
+    s, sol = poisson16
+    ref = oracle_solve(s, method, prec)
+    x = np.zeros(s.n)
+    r = s.b.copy()
+    res = sol.solve(method, s.val, x, r, prec, 2000, ref["tol"])
+    assert res.status == 0
+    assert iter_ok(res.niter, ref["niter"]), (res.niter, ref["niter"])
+    assert rel_l2(x, ref["x"]) <= SOL_REL
+    assert res.ini_res == pytest.approx(ref["ini"], rel=1e-13)
+    assert res.fin_res < ref["tol"]
+    # r1 returns the final recursive residual (Cg.f90:159-162)
+    assert rel_l2(r, ref["r"]) <= 1e-6
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("method", [TFS_BICG, TFS_CGS])
+def test_solve_matches_oracle_convdiff(method, prec, convdiff12):
+    s, sol = convdiff12
+    ref = oracle_solve(s, method, prec)
+    x = np.zeros(s.n)
+    r = s.b.copy()
+    res = sol.solve(method, s.val, x, r, prec, 2000, ref["tol"])
+    assert res.status == 0
+    assert iter_ok(res.niter, ref["niter"]), (res.niter, ref["niter"])
+    assert rel_l2(x, ref["x"]) <= SOL_REL
+
+
+def test_solve_32_cube_dic_cg(gpu):
+    s = system(POISSON, 32)
+    ref = oracle_solve(s, TFS_CG, 2)
+    x = np.zeros(s.n)
+    r = s.b.copy()
+    res = Solver(s.matrix()).solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
+    assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+
+
+def test_nonzero_initial_guess(poisson16):
+    s, sol = poisson16
+    x0 = np.random.default_rng(4).uniform(-1, 1, s.n)
+    ref = oracle_solve(s, TFS_CG, 1, x0=x0)
+    x, r = x0.copy(), s.b.copy()
+    res = sol.solve(TFS_CG, s.val, x, r, 1, 2000, ref["tol"])
+    assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+
+
+def test_reproducible_bitwise(poisson16):
+    s, sol = poisson16
+    outs = []
+    for _ in range(2):
+        x, r = np.zeros(s.n), s.b.copy()
+        res = sol.solve(TFS_BICG, s.val, x, r, 2, 500, 1e-10)
+        outs.append((x, r, res))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2] == outs[1][2]
+
+
+# ------------------------------------------------------ reference semantics
+
+@pytest.mark.parametrize("method", METHODS)
+def test_early_exit_small_b(method, poisson16):
+    """||b|| < tol: iter = 0, x and r1 untouched, ini_res untouched,
+    fin_res = ||b|| (Cg.f90:55-58)."""
+    s, sol = poisson16
+    b = s.b * 1e-12
+    x, r = np.ones(s.n), b.copy()
+    res = sol.solve(method, s.val, x, r, 1, 100, 1.0, ini_res=-7.0)
+    assert res.niter == 0 and res.ini_res == -7.0
+    assert res.fin_res == pytest.approx(np.linalg.norm(b), rel=1e-13)
+    assert np.array_equal(x, np.ones(s.n)) and np.array_equal(r, b)
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_early_exit_exact_guess(method, poisson16):
+    """||b - A x0|| < tol: iter = 0, ini_res = fin_res (Cg.f90:85-90)."""
+    s, sol = poisson16
+    xs = np.random.default_rng(5).uniform(-1, 1, s.n)
+    b = O.spmv(s.n, s.row, s.col, s.val, xs)
+    ref_x, ref_r = xs.copy(), b.copy()
+    it, ini, fin = O.solve(method, s.n, s.row, s.col, s.dia, s.val, ref_x, ref_r, 1, 100, 1e-6)
+    x, r = xs.copy(), b.copy()
+    res = sol.solve(method, s.val, x, r, 1, 100, 1e-6)
+    assert res.niter == it == 0
+    assert res.ini_res == res.fin_res and res.ini_res == pytest.approx(ini, rel=1e-12, abs=1e-15)
+    assert np.array_equal(r, ref_r)
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_not_converged_returns_limit_plus_one(method, poisson16):
+    s, sol = poisson16
+    ref = oracle_solve(s, method, 1, niter=7, rel=1e-14)
+    x, r = np.zeros(s.n), s.b.copy()
+    res = sol.solve(method, s.val, x, r, 1, 7, ref["tol"])
+    assert res.niter == ref["niter"] == 8
+    assert rel_l2(x, ref["x"]) <= 1e-12
+    assert res.fin_res == pytest.approx(ref["fin"], rel=1e-10)
+
+
+def test_zero_iteration_limit(poisson16):
+    s, sol = poisson16
+    ref = oracle_solve(s, TFS_CG, 1, niter=0)
+    x, r = np.zeros(s.n), s.b.copy()
+    res = sol.solve(TFS_CG, s.val, x, r, 1, 0, ref["tol"])
+    assert res.niter == ref["niter"] == 1
+    assert res.fin_res == pytest.approx(ref["fin"], rel=1e-13)
+
+
+def test_nan_rhs_reports_nonfinite(poisson16):
+    s, sol = poisson16
+    b = s.b.copy()
+    b[3] = np.nan
+    x, r = np.zeros(s.n), b.copy()
+    res = sol.solve(TFS_CG, s.val, x, r, 1, 50, 1e-8)
+    assert res.status == TFS_ERR_NONFINITE
+    assert np.isnan(res.fin_res) and res.niter == 51
+
+
+def test_tiny_systems(gpu):
+    """n = 1 (a single diagonal entry) and ragged n < 32."""
+    A = Matrix_Type(1, [1, 2], [1], [1], [4.0])
+    with Solver(A) as sol:
+        x, r = np.zeros(1), np.array([2.0])
+        res = sol.solve(TFS_CG, A.val, x, r, 1, 10, 1e-12)
+        assert res.niter == 1 and x[0] == 0.5
+    s = system(POISSON, 3, 2, 1)
+    ref = oracle_solve(s, TFS_CG, 2)
+    x, r = np.zeros(s.n), s.b.copy()
+    res = Solver(s.matrix()).solve(TFS_CG, s.val, x, r, 2, 100, ref["tol"])
+    assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+
+
+def test_fortran_shaped_entry_points(poisson16):
+    """tfs_cg/tfs_bicg/tfs_cgs with no handle (cached by array identity)."""
+    import ctypes as C
+    from tflows.matrix_mod import ptr
+    s, _ = poisson16
+    from tflows.lib import load_library
+    lib = load_library()
+    for fn, method in ((lib.tfs_cg, TFS_CG), (lib.tfs_bicg, TFS_BICG), (lib.tfs_cgs, TFS_CGS)):
+        ref = oracle_solve(s, method, 1)
+        x, r = np.zeros(s.n), s.b.copy()
+        it, ini, fin = C.c_int32(2000), C.c_double(0), C.c_double(0)
+        st = fn(s.n, s.nnz, ptr(s.row, C.c_int32), ptr(s.col, C.c_int32), ptr(s.dia, C.c_int32),
+                ptr(s.val, C.c_double), ptr(x, C.c_double), ptr(r, C.c_double), 1,
+                C.byref(it), ref["tol"], C.byref(ini), C.byref(fin))
+        assert st == 0 and iter_ok(it.value, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+
+
+# ------------------------------------------------------ mixed precision
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("method", METHODS)
+def test_mixed_precision_converges(method, prec, poisson16):
+    """Binary32 inner iterations with binary64 reliable updates reach the same
+    absolute tolerance on the binary64 true residual; error vs the FP64 oracle
+    is bounded by the conditioning at that tolerance."""
+    s, _ = poisson16
+    ref = oracle_solve(s, method, prec)
+    with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+        x, r = np.zeros(s.n), s.b.copy()
+        res = sol.solve(method, s.val, x, r, prec, 2000, ref["tol"])
+        st = sol.stats()
+    assert res.status == 0
+    assert res.fin_res < ref["tol"]
+    rt = s.b.copy()
+    O.residual(s.n, s.row, s.col, s.val, x, rt)
+    assert np.linalg.norm(rt) < ref["tol"]          # true residual, binary64
+    assert np.array_equal(r, rt) or rel_l2(r, rt) < 1e-12
+    assert rel_l2(x, ref["x"]) < 1e-6
+    assert res.niter <= 1.3 * ref["niter"] + 5
+    assert st["true_residuals"] >= 2

@@ -1,0 +1,159 @@
+"""CPU tests of the host side: the C ABI exports, the topology builder, the
+synthetic systems, input validation and the replica partition."""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import tfs_oracle as O
+from tflows import Matrix_Mod_Topology, SynthSystem
+from tflows.lib import (SIGNATURES, TFS_ERR_ARG, TFS_ERR_MATRIX, lib_path, load_library)
+from tflows.matrix_mod import ptr
+from tflows.synth import CONVDIFF, POISSON, loguniform
+
+REPO = Path(__file__).resolve().parents[1]
+GOLD = REPO / "tests" / "golden"
+
+
+def header_functions() -> set[str]:
+    names = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(tfs_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = load_library()
+    declared = header_functions()
+    assert len(declared) >= 25
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    # the ctypes table covers the same set
+    assert declared <= set(SIGNATURES), sorted(declared - set(SIGNATURES))
+
+
+def test_library_is_in_tree_and_built_for_sm103a():
+    from tflows import build
+    assert lib_path.is_relative_to(REPO)
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+@pytest.mark.parametrize("kind,dims,perm", [(POISSON, (6, 5, 4), True), (POISSON, (7, 7, 7), False),
+                                            (CONVDIFF, (5, 6, 7), True), (POISSON, (1, 1, 9), True)])
+def test_topology_matches_oracle(kind, dims, perm):
+    s = SynthSystem(kind, *dims, seed=3, permute=perm)
+    A = Matrix_Mod_Topology(s.n, s.faces_c)
+    row, col, dia, mir, pos = O.topology(s.n, s.faces_c)
+    for a, b in ((A.row, row), (A.col, col), (A.dia, dia), (A.mir, mir), (A.pos, pos)):
+        assert np.array_equal(a, b)
+    assert np.array_equal(A.row, s.row) and np.array_equal(A.col, s.col)
+
+
+def test_topology_boundary_faces_and_counts():
+    """Faces with c2 <= 0 are boundary faces: no entry, pos = 0."""
+    faces = np.array([[1, 2], [2, 3], [1, -1], [3, 0]], np.int32)
+    A = Matrix_Mod_Topology(3, faces)
+    assert A.row.tolist() == [1, 3, 6, 8]
+    assert A.col.tolist() == [1, 2, 1, 2, 3, 2, 3]
+    assert A.dia.tolist() == [1, 4, 7]
+    assert A.pos.tolist() == [[2, 3], [5, 6], [0, 0], [0, 0]]
+    assert A.mir.tolist() == [1, 3, 2, 4, 6, 5, 7]
+    assert A.nonzeros == A.nnz + 1
+
+
+def test_synth_sizes_match_hex_stencil():
+    for n in (8, 13):
+        s = SynthSystem(POISSON, n)
+        interior = 3 * n * n * (n - 1)
+        assert s.n == n ** 3 and s.n_faces == interior and s.nnz == n ** 3 + 2 * interior
+    s = SynthSystem(POISSON, 32)
+    assert s.nnz == 223232          # the 32^3 workload
+
+
+def test_synth_poisson_properties():
+    s = SynthSystem(POISSON, 9, 8, 7, jitter=0.25)
+    A = Matrix_Mod_Topology(s.n, s.faces_c)
+    assert np.array_equal(s.val, s.val[A.mir - 1])              # symmetric
+    off = np.ones(s.nnz, bool)
+    off[s.dia - 1] = False
+    assert (s.val[off] < 0).all() and (s.val[s.dia - 1] > 0).all()
+    rowsum = np.add.reduceat(s.val, s.row[:-1] - 1)
+    assert (rowsum > -1e-12).all() and (rowsum > 1e-6).sum() == 8 * 7  # x = 0 Dirichlet cells
+    assert (np.abs(s.b) <= 1).all()
+
+
+def test_synth_convdiff_properties():
+    s = SynthSystem(CONVDIFF, 10, jitter=0.2)
+    off = np.ones(s.nnz, bool)
+    off[s.dia - 1] = False
+    assert (s.val[off] <= 0).all()
+    rowsum = np.add.reduceat(s.val, s.row[:-1] - 1)
+    assert (rowsum > 0).all()                                  # V/dt: strictly dominant
+    A = Matrix_Mod_Topology(s.n, s.faces_c)
+    assert not np.array_equal(s.val, s.val[A.mir - 1])         # upwind: non-symmetric
+
+
+def test_synth_deterministic_and_golden():
+    import hashlib
+    expected = json.loads((GOLD / "synth_hashes.json").read_text())
+    from golden.make_golden import SYNTH_HASH_CASES, synth_hash
+    for name, (kind, nx, ny, nz, jit, seed, perm) in SYNTH_HASH_CASES.items():
+        s = SynthSystem(kind, nx, ny, nz, jitter=jit, seed=seed, permute=perm)
+        assert synth_hash(s) == expected[name], name
+    assert hashlib is not None
+
+
+def test_loguniform_range_and_determinism():
+    v = [loguniform(5000, 500000, 7, i) for i in range(2000)]
+    assert min(v) >= 5000 and max(v) <= 500000
+    assert v == [loguniform(5000, 500000, 7, i) for i in range(2000)]
+    logs = np.log(v)
+    assert abs(np.median(logs) - 0.5 * (np.log(5000) + np.log(500000))) < 0.2
+
+
+def _register(n, nnz, row, col, dia):
+    lib = load_library()
+    h = C.c_void_p()
+    st = lib.tfs_topology_register(n, nnz, ptr(np.asarray(row, np.int32), C.c_int32),
+                                   ptr(np.asarray(col, np.int32), C.c_int32),
+                                   ptr(np.asarray(dia, np.int32), C.c_int32), C.byref(h))
+    if st == 0:
+        lib.tfs_release(h)
+    return st
+
+
+@pytest.mark.parametrize("case,want", [
+    ("unsorted", TFS_ERR_MATRIX), ("col_range", TFS_ERR_MATRIX), ("bad_dia", TFS_ERR_MATRIX),
+    ("row_end", TFS_ERR_MATRIX), ("empty_row", TFS_ERR_MATRIX), ("n_zero", TFS_ERR_ARG)])
+def test_malformed_csr_rejected_before_device_work(case, want):
+    row = np.array([1, 3, 5, 7], np.int32)
+    col = np.array([1, 2, 1, 2, 2, 3], np.int32)
+    dia = np.array([1, 4, 6], np.int32)
+    n, nnz = 3, 6
+    if case == "unsorted":
+        col = np.array([2, 1, 1, 2, 2, 3], np.int32)
+    elif case == "col_range":
+        col = np.array([1, 4, 1, 2, 2, 3], np.int32)
+    elif case == "bad_dia":
+        dia = np.array([1, 3, 6], np.int32)
+    elif case == "row_end":
+        nnz = 7
+    elif case == "empty_row":
+        row = np.array([1, 3, 3, 7], np.int32)
+    elif case == "n_zero":
+        n = 0
+    assert _register(n, nnz, row, col, dia) == want
+
+
+def test_fortran_shim_binds_the_abi():
+    shim = (REPO / "t-flows_gb300" / "fortran" / "Solvers_Mod_Gpu.f90").read_text()
+    for name in ("tfs_cg", "tfs_bicg", "tfs_cgs"):
+        assert f'bind(C, name="{name}")' in shim
+    for sub in ("subroutine Cg(", "subroutine Bicg(", "subroutine Cgs("):
+        assert sub in shim

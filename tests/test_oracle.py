@@ -1,0 +1,222 @@
+"""CPU tests of the oracle: known answers, the reference's documented CSR
+example, the reference's output semantics, and the golden fixtures."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import tfs_oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+TINY = 1.e-30
+
+
+@pytest.fixture(scope="module")
+def kat():
+    return dict(np.load(GOLD / "matrix_mod_example.npz"))
+
+
+# -------------------------------------------- Matrix_Mod.f90:15-34 example
+
+def test_layout_example_dense(kat):
+    """val/col/row/dia of Matrix_Mod.f90:30-34 describe the matrix drawn at
+    Matrix_Mod.f90:23-26 (row gains its n+1 terminator 13)."""
+    n = 4
+    a = np.zeros((n, n))
+    for i in range(n):
+        for j in range(kat["row"][i] - 1, kat["row"][i + 1] - 1):
+            a[i, kat["col"][j] - 1] = kat["val"][j]
+    assert np.array_equal(a, kat["dense"])
+    for i in range(n):
+        assert kat["col"][kat["dia"][i] - 1] == i + 1
+    # the documented dia (Matrix_Mod.f90:34) points row 3 at column 4
+    doc = kat["dia_documented"]
+    assert [int(kat["col"][doc[i] - 1]) for i in range(n)] == [1, 2, 4, 4]
+
+
+def test_layout_example_spmv_residual(kat):
+    p = np.array([1.0, -2.0, 0.5, 3.0])
+    q = O.spmv(4, kat["row"], kat["col"], kat["val"], p)
+    assert np.array_equal(q, kat["dense"] @ p)        # small integers: exact
+    r = np.array([1.0, 2.0, 3.0, 4.0])
+    O.residual(4, kat["row"], kat["col"], kat["val"], p, r)
+    assert np.array_equal(r, np.array([1.0, 2.0, 3.0, 4.0]) - kat["dense"] @ p)
+
+
+def test_layout_example_prec_form(kat):
+    d1 = O.prec_form(4, kat["row"], kat["col"], kat["dia"], kat["val"], 1)
+    assert np.array_equal(d1, [10.0, 12.0, 99.0, 53.0])
+    d0 = O.prec_form(4, kat["row"], kat["col"], kat["dia"], kat["val"], 0)
+    assert np.array_equal(d0, np.ones(4))
+    # DIC recurrence D_i = 1/(a_ii - sum_{lower} D_k a_ik a_ik), Prec_Form.f90:32-40
+    D = [0.0] * 4
+    D[0] = 1.0 / 10.0
+    D[1] = 1.0 / (12.0 - D[0] * 2.0 * 2.0)
+    D[2] = 1.0 / (99.0 - D[1] * 1.0 * 1.0)
+    D[3] = 1.0 / ((53.0 - D[0] * -3.0 * -3.0) - D[1] * 11.0 * 11.0)
+    d2 = O.prec_form(4, kat["row"], kat["col"], kat["dia"], kat["val"], 2)
+    assert np.array_equal(d2, D)
+
+
+def test_layout_example_prec_solve(kat):
+    b = np.array([1.0, 2.0, 3.0, 4.0])
+    D = O.prec_form(4, kat["row"], kat["col"], kat["dia"], kat["val"], 2)
+    # forward (Prec_Solve.f90:46-53), scaling (:55-57), backward (:60-67)
+    y = [0.0] * 4
+    y[0] = b[0] * D[0]
+    y[1] = (b[1] - 2.0 * y[0]) * D[1]
+    y[2] = (b[2] - 1.0 * y[1]) * D[2]
+    y[3] = ((b[3] - -3.0 * y[0]) - 11.0 * y[1]) * D[3]
+    y = [y[i] / (D[i] + TINY) for i in range(4)]
+    x = [0.0] * 4
+    x[3] = y[3] * D[3]
+    x[2] = (y[2] - 7.0 * x[3]) * D[2]
+    x[1] = (y[1] - -1.0 * x[2]) * D[1]
+    x[0] = ((y[0] - 4.0 * x[2]) - 5.0 * x[3]) * D[0]
+    got = O.prec_solve(4, kat["row"], kat["col"], kat["dia"], kat["val"], 2, b)
+    assert np.array_equal(got, x)
+    got1 = O.prec_solve(4, kat["row"], kat["col"], kat["dia"], kat["val"], 1, b)
+    assert np.array_equal(got1, b / np.array([10.0, 12.0, 99.0, 53.0]))
+
+
+# ------------------------------------------------------ known answers
+
+def csr_from_dense(a):
+    n = a.shape[0]
+    row, col, val, dia = [1], [], [], []
+    for i in range(n):
+        for j in range(n):
+            if a[i, j] != 0 or i == j:
+                if i == j:
+                    dia.append(len(col) + 1)
+                col.append(j + 1)
+                val.append(a[i, j])
+        row.append(len(col) + 1)
+    return (np.array(row, np.int32), np.array(col, np.int32), np.array(dia, np.int32),
+            np.array(val, np.float64))
+
+
+def test_cg_2x2_two_iterations():
+    """CG on an SPD 2x2 system terminates in n = 2 iterations."""
+    row, col, dia, val = csr_from_dense(np.array([[4.0, 1.0], [1.0, 3.0]]))
+    x, r = np.zeros(2), np.array([1.0, 2.0])
+    it, ini, fin = O.solve(0, 2, row, col, dia, val, x, r, 0, 10, 1e-12)
+    assert it == 2
+    assert np.allclose(x, [1 / 11, 7 / 11], rtol=0, atol=1e-15)
+    assert ini == pytest.approx(np.sqrt(5.0), rel=1e-15)
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_diagonal_system_one_iteration(method):
+    d = np.array([2.0, 5.0, 0.25, 8.0, 3.0])
+    row, col, dia, val = csr_from_dense(np.diag(d))
+    b = np.array([1.0, -2.0, 3.0, 0.5, -1.5])
+    x, r = np.zeros(5), b.copy()
+    it, _, fin = O.solve(method, 5, row, col, dia, val, x, r, 1, 10, 1e-10)
+    assert it == 1 and fin < 1e-10
+    assert np.allclose(x, b / d, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("method,prec", [(0, 0), (0, 1), (0, 2), (1, 1), (2, 1), (2, 2)])
+def test_1d_poisson_manufactured(method, prec):
+    """Tridiagonal (-1, 2, -1) system with a manufactured x* (b = A x*): the
+    solvers reach x* to the accuracy the conditioning allows."""
+    n = 60
+    a = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+    t = np.arange(1, n + 1) / (n + 1)
+    xs = t * (1 - t) * np.exp(t) + 0.1 * np.cos(7 * t)
+    b = a @ xs
+    row, col, dia, val = csr_from_dense(a)
+    x, r = np.zeros(n), b.copy()
+    it, ini, fin = O.solve(method, n, row, col, dia, val, x, r, prec, 500, 1e-12 * np.linalg.norm(b))
+    assert fin < 1e-12 * np.linalg.norm(b)
+    assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-9
+    if method == 0 and prec == 0:
+        assert it <= n + 5          # CG terminates in <= n steps, up to rounding
+
+
+def test_scipy_jacobi_cg_cross_check():
+    """Independent sanity check: scipy's Jacobi-preconditioned CG (relative
+    tolerance, different update order) lands near the oracle's solution."""
+    sp = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    from tflows import SynthSystem
+    s = SynthSystem(0, 12, 11, 10)
+    A = sp.csr_matrix((s.val, s.col - 1, s.row - 1), shape=(s.n, s.n))
+    x, r = np.zeros(s.n), s.b.copy()
+    tol = 1e-10 * np.linalg.norm(s.b)
+    O.solve(0, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 5000, tol)
+    M = sp.diags(1.0 / A.diagonal())
+    xs, info = spla.cg(A, s.b, rtol=1e-12, M=M, maxiter=5000)
+    assert info == 0
+    assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-7
+
+
+# ------------------------------------------------------ semantics
+
+def _poisson(n=8):
+    from tflows import SynthSystem
+    return SynthSystem(0, n)
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_semantics_small_b(method):
+    s = _poisson()
+    b = s.b * 1e-9
+    x, r = np.ones(s.n), b.copy()
+    it, ini, fin = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 10, 1.0, ini_res=-3.0)
+    assert it == 0 and ini == -3.0 and fin == pytest.approx(np.linalg.norm(b))
+    assert np.array_equal(x, np.ones(s.n)) and np.array_equal(r, b)
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_semantics_limit_plus_one(method):
+    s = _poisson()
+    x, r = np.zeros(s.n), s.b.copy()
+    it, ini, fin = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 5, 1e-30)
+    assert it == 6 and fin > 1e-30
+    x, r = np.zeros(s.n), s.b.copy()
+    it, ini, fin = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 0, 1e-30)
+    assert it == 1 and fin == ini
+
+
+def test_semantics_r1_is_recursive_residual():
+    """r1 leaves as the recursive residual, close to (not equal to) b - A x."""
+    s = _poisson()
+    x, r = np.zeros(s.n), s.b.copy()
+    O.solve(0, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 1000, 1e-8 * np.linalg.norm(s.b))
+    rt = s.b.copy()
+    O.residual(s.n, s.row, s.col, s.val, x, rt)
+    assert np.linalg.norm(r - rt) < 1e-12 * np.linalg.norm(s.b)
+
+
+# ------------------------------------------------------ golden fixtures
+
+@pytest.mark.parametrize("path", sorted(GOLD.glob("solve_*.npz")), ids=lambda p: p.stem)
+def test_golden_solves(path):
+    g = np.load(path)
+    n = g["dia"].size
+    for method in (0, 1, 2):
+        for prec in (0, 1, 2):
+            key = f"m{method}p{prec}"
+            x, r = np.zeros(n), g["b"].copy()
+            it, ini, fin = O.solve(method, n, g["row"], g["col"], g["dia"], g["val"], x, r, prec,
+                                   1000, float(g["tol"]))
+            assert np.array_equal(x, g[key + "_x"]) and np.array_equal(r, g[key + "_r"]), key
+            assert [it, ini, fin] == list(g[key + "_scal"]), key
+
+
+def test_golden_topology():
+    """The oracle's Topology.f90 restatement reproduces the fixtures' CSR."""
+    for path in sorted(GOLD.glob("solve_*.npz")):
+        g = np.load(path)
+        row, col, dia, mir, pos = O.topology(g["dia"].size, g["faces_c"])
+        assert np.array_equal(row, g["row"]) and np.array_equal(col, g["col"])
+        assert np.array_equal(dia, g["dia"])
+        # mirror of a mirror is the entry itself; pos points at (c1,c2),(c2,c1)
+        assert np.array_equal(mir[mir - 1] , np.arange(1, col.size + 1))
+        f = g["faces_c"]
+        assert np.array_equal(col[pos[:, 0] - 1], f[:, 1]) and np.array_equal(col[pos[:, 1] - 1], f[:, 0])
