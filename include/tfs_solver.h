@@ -41,6 +41,7 @@
 #ifndef TFS_SOLVER_H
 #define TFS_SOLVER_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -174,6 +175,33 @@ const char *tfs_status_string(int status);
 
 /* Text of the last error recorded by this thread (CUDA error names etc.). */
 const char *tfs_last_error(void);
+
+/* ---- device and timing helpers ------------------------------------------
+ * For callers without a CUDA runtime of their own (the benchmark harness, a
+ * Fortran driver).  None of these replaces a reference interface. */
+
+/* Make `device` current for the calling host thread (handles created later
+ * live on it). */
+int tfs_use_device(int device);
+
+/* Device memory (cudaMalloc / cudaFree) and page-locked host memory
+ * (cudaMallocHost / cudaFreeHost). */
+int tfs_device_alloc(size_t bytes, void **ptr);
+int tfs_device_free(void *ptr);
+int tfs_host_alloc(size_t bytes, void **ptr);
+int tfs_host_free(void *ptr);
+
+/* Copy `bytes` between any two of host/device memory, ordered on the
+ * handle's stream (asynchronous for device and page-locked memory). */
+int tfs_copy(tfs_handle *h, void *dst, const void *src, size_t bytes);
+
+/* Wait for all work queued on the handle's stream. */
+int tfs_sync(tfs_handle *h);
+
+/* CUDA events on the handle's stream around a region of calls:
+ * tfs_timer_stop waits for the region and returns its device time. */
+int tfs_timer_start(tfs_handle *h);
+int tfs_timer_stop(tfs_handle *h, double *ms);
 
 /* ---- host-side mesh utilities ------------------------------------------ */
 

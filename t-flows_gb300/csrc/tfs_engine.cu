@@ -317,6 +317,8 @@ static void free_handle(tfs_handle *h)
     if (h->h_state) cudaFreeHost(h->h_state);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->tev0) cudaEventDestroy(h->tev0);
+    if (h->tev1) cudaEventDestroy(h->tev1);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->stream2) cudaStreamDestroy(h->stream2);
     delete h;
@@ -932,5 +934,76 @@ extern "C" int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int rep
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
     *ms = (double)t / reps;
+    return TFS_OK;
+}
+
+// ------------------------------------------------------ device helpers
+
+extern "C" int tfs_use_device(int device)
+{
+    CK(cudaSetDevice(device));
+    return TFS_OK;
+}
+
+extern "C" int tfs_device_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr) return TFS_ERR_ARG;
+    CK(cudaMalloc(ptr, bytes ? bytes : 1));
+    return TFS_OK;
+}
+
+extern "C" int tfs_device_free(void *ptr)
+{
+    CK(cudaFree(ptr));
+    return TFS_OK;
+}
+
+extern "C" int tfs_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr) return TFS_ERR_ARG;
+    CK(cudaMallocHost(ptr, bytes ? bytes : 1));
+    return TFS_OK;
+}
+
+extern "C" int tfs_host_free(void *ptr)
+{
+    CK(cudaFreeHost(ptr));
+    return TFS_OK;
+}
+
+extern "C" int tfs_copy(tfs_handle *h, void *dst, const void *src, size_t bytes)
+{
+    if (!h || (!dst && bytes) || (!src && bytes)) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, h->stream));
+    return TFS_OK;
+}
+
+extern "C" int tfs_sync(tfs_handle *h)
+{
+    if (!h) return TFS_ERR_ARG;
+    CK(cudaStreamSynchronize(h->stream));
+    return TFS_OK;
+}
+
+extern "C" int tfs_timer_start(tfs_handle *h)
+{
+    if (!h) return TFS_ERR_ARG;
+    if (!h->tev0) {
+        CK(cudaEventCreate(&h->tev0));
+        CK(cudaEventCreate(&h->tev1));
+    }
+    CK(cudaEventRecord(h->tev0, h->stream));
+    return TFS_OK;
+}
+
+extern "C" int tfs_timer_stop(tfs_handle *h, double *ms)
+{
+    if (!h || !ms || !h->tev0) return TFS_ERR_ARG;
+    CK(cudaEventRecord(h->tev1, h->stream));
+    CK(cudaEventSynchronize(h->tev1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, h->tev0, h->tev1));
+    *ms = (double)t;
     return TFS_OK;
 }

@@ -85,7 +85,7 @@ struct tfs_handle {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int grid = 0;                      // blocks of the chunk kernels

@@ -55,6 +55,15 @@ SIGNATURES = {
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_status_string": (C.c_char_p, [C.c_int]),
     "tfs_last_error": (C.c_char_p, []),
+    "tfs_use_device": (C.c_int, [C.c_int]),
+    "tfs_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),
+    "tfs_device_free": (C.c_int, [P_void]),
+    "tfs_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),
+    "tfs_host_free": (C.c_int, [P_void]),
+    "tfs_copy": (C.c_int, [P_void, P_void, P_void, C.c_size_t]),
+    "tfs_sync": (C.c_int, [P_void]),
+    "tfs_timer_start": (C.c_int, [P_void]),
+    "tfs_timer_stop": (C.c_int, [P_void, P_dbl]),
     "tfs_topology_count": (i32, [i32, i32, P_i32]),
     "tfs_topology_build": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_i32, P_i32, P_i32]),
     "tfs_synth_create": (C.c_int, [C.c_int, i32, i32, i32, dbl, u64, C.c_int, C.POINTER(P_void)]),

@@ -109,8 +109,9 @@ def test_solve_matches_oracle_poisson(method, prec, poisson16):
     assert rel_l2(x, ref["x"]) <= SOL_REL
     assert res.ini_res == pytest.approx(ref["ini"], rel=1e-13)
     assert res.fin_res < ref["tol"]
-    # r1 returns the final recursive residual (Cg.f90:159-162)
-    assert rel_l2(r, ref["r"]) <= 1e-6
+    # r1 returns the final recursive residual (Cg.f90:159-162); it is ~tol in
+    # size, so its difference is gated relative to ||b|| like the solution.
+    assert np.linalg.norm(r - ref["r"]) <= SOL_REL * np.linalg.norm(s.b)
 
 
 @pytest.mark.parametrize("prec", [1, 2])
