@@ -231,7 +231,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     results = {}
     timed_launches = 0
     clock_info = None
-    for mode, name in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
+    modes = [m for m in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")) if m[1] in args.modes.split(",")]
+    for mode, name in modes:
         sol.set_precision(mode)
         for _ in range(args.warmup):
             res = step_resident()
@@ -275,27 +276,29 @@ def run_ours(args, dist: Dist) -> dict | None:
     bytes64 = 12 * nnz + 20 * n + 4
     bytes32 = 8 * nnz + 12 * n + 4
 
-    # End to end through tfs_solve with page-locked host arrays (mixed).
-    sol.set_precision(TFS_MIXED)
-    p_val, h_val = halloc(8 * nnz, np.float64, nnz)
-    p_x, h_x = halloc(8 * n, np.float64, n)
-    p_r, h_r = halloc(8 * n, np.float64, n)
-    h_val[:] = s.val
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        h_x[:] = 0.0
-        h_r[:] = s.b
-        t = time.perf_counter()
-        res = sol.solve(method, h_val, h_x, h_r, prec, args.niter, tol)
-        if i >= args.warmup:
-            e2e_ms.append((time.perf_counter() - t) * 1e3)
-    e2e_total = dist.max(sum(e2e_ms))
-    e2e = {"value": dist.sum(args.steps) / (e2e_total / 1e3), "unit": UNIT,
-           "h2d_bytes_per_step": 8 * nnz + 16 * n, "d2h_bytes_per_step": 16 * n,
-           "p50_ms": pct(e2e_ms, 50), "p99_ms": pct(e2e_ms, 99),
-           "timing": "host wall clock around each tfs_solve call (copies included)"}
-    for p in (p_val, p_x, p_r):
-        lib.tfs_host_free(C.c_void_p(p))
+    # End to end through tfs_solve with page-locked host arrays (headline arithmetic).
+    e2e = None
+    if not args.no_e2e:
+        sol.set_precision(modes[-1][0])
+        p_val, h_val = halloc(8 * nnz, np.float64, nnz)
+        p_x, h_x = halloc(8 * n, np.float64, n)
+        p_r, h_r = halloc(8 * n, np.float64, n)
+        h_val[:] = s.val
+        e2e_ms = []
+        for i in range(args.warmup + args.steps):
+            h_x[:] = 0.0
+            h_r[:] = s.b
+            t = time.perf_counter()
+            res = sol.solve(method, h_val, h_x, h_r, prec, args.niter, tol)
+            if i >= args.warmup:
+                e2e_ms.append((time.perf_counter() - t) * 1e3)
+        e2e_total = dist.max(sum(e2e_ms))
+        e2e = {"value": dist.sum(args.steps) / (e2e_total / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": 8 * nnz + 16 * n, "d2h_bytes_per_step": 16 * n,
+               "p50_ms": pct(e2e_ms, 50), "p99_ms": pct(e2e_ms, 99),
+               "timing": "host wall clock around each tfs_solve call (copies included)"}
+        for p in (p_val, p_x, p_r):
+            lib.tfs_host_free(C.c_void_p(p))
     for p in (d_val, d_b, d_x, d_r, d_zero):
         lib.tfs_device_free(C.c_void_p(p))
 
@@ -311,11 +314,11 @@ def run_ours(args, dist: Dist) -> dict | None:
                "sample": f"one full binary64 solve ({it} iterations, {cpu_s:.1f} s) of the same "
                          f"system on 1 host core; {os.cpu_count()} cores present",
                "oracle_iterations": it}
-        for name in ("fp64", "mixed"):
+        for name in results:
             x = results[name]["_x"]
             results[name]["rel_err_vs_oracle"] = float(np.linalg.norm(x - xo) / np.linalg.norm(xo))
-        results["fp64"]["iterations_vs_oracle"] = f"{results['fp64']['iterations']} vs {it}"
-    for name in ("fp64", "mixed"):
+            results[name]["iterations_vs_oracle"] = f"{results[name]['iterations']} vs {it}"
+    for name in results:
         results[name].pop("_x", None)
 
     peak, peak_src = measured_peak_gbs()
@@ -325,7 +328,8 @@ def run_ours(args, dist: Dist) -> dict | None:
             "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
             "algorithmic_bytes_per_launch": bytes32,
             "traffic": ncu_traffic(args.workload, "k_mx_spmv_pq")}
-    mixed = results["mixed"]
+    mixed = results.get("mixed") or results["fp64"]
+    fp64 = results.get("fp64") or mixed
     line = {
         "metric": METRIC, "value": round(mixed["solves_per_s"], 4), "unit": UNIT,
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
@@ -338,8 +342,8 @@ def run_ours(args, dist: Dist) -> dict | None:
                    "l2": "inputs larger than L2 (matrix + vectors > 129 MB)",
                    "parallelism": f"replicas x{dist.world}"},
         "p50_ms": round(mixed["p50_ms"], 4), "p99_ms": round(mixed["p99_ms"], 4),
-        "fp64": results["fp64"], "mixed": mixed,
-        "mixed_over_fp64": round(mixed["solves_per_s"] / results["fp64"]["solves_per_s"], 4),
+        "fp64": results.get("fp64"), "mixed": results.get("mixed"),
+        "mixed_over_fp64": round(mixed["solves_per_s"] / fp64["solves_per_s"], 4),
         "spmv": {"fp64_us": round(spmv64_ms * 1e3, 2), "fp32_us": round(spmv32_ms * 1e3, 2),
                  "fp64_gbs": round(bytes64 / (spmv64_ms * 1e-3) / 1e9, 1),
                  "fp32_gbs": round(achieved, 1), "timing": "CUDA events, back-to-back launches"},
@@ -432,6 +436,9 @@ def main(argv=None) -> int:
     ap.add_argument("--spmv-reps", type=int, default=50)
     ap.add_argument("--ref-sample-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--modes", default="fp64,mixed",
+                    help="arithmetic legs to run (profiling runs may pick one)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

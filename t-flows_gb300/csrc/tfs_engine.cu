@@ -266,8 +266,21 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
         (rc = dalloc(h, &h->val, nnz_pad)) || (rc = dalloc(h, &h->val32, nnz_pad)) ||
         (rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
         (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)) ||
-        (rc = dalloc(h, &h->st, 1)) || (rc = dalloc(h, &h->params, 1)))
+        (rc = dalloc(h, &h->st, 1)) || (rc = dalloc(h, &h->params, 1)) ||
+        (rc = dalloc(h, &h->flags, n_int)) || (rc = dalloc(h, &h->ctl, 1)))
         return rc;
+    CK(cudaMemsetAsync(h->flags, 0, sizeof(unsigned) * (size_t)n_int, h->stream));
+    CK(cudaMemsetAsync(h->ctl, 0, sizeof(SweepCtl), h->stream));
+    {
+        int occ = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_df<double, 2, 0>, TFS_TPB, 0));
+        if (occ < 1) occ = 1;
+        int gs = h->sm_count * occ;
+        h->sweep_grid = h->n_chunks < gs ? h->n_chunks : gs;
+        if (h->sweep_grid < 1) h->sweep_grid = 1;
+        const char *env = getenv("TFS_SWEEP");
+        if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
+    }
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->rowinfo, rowinfo.data(), sizeof(uint32_t) * n_int, cudaMemcpyHostToDevice, h->stream));
@@ -309,7 +322,7 @@ static void free_handle(tfs_handle *h)
         if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
     }
     void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
-                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params,
+                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params, h->flags, h->ctl,
                     h->vec_pool, h->vec32_pool};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -375,6 +388,24 @@ extern "C" int tfs_set_precision(tfs_handle *h, int mode)
 
 // ------------------------------------------------------ graph capture
 
+// DIC recurrence (Prec_Form.f90:32-40): one dataflow launch or one launch per
+// level.  Returns the number of kernels launched.
+static int launch_dic_form(tfs_handle *h, cudaStream_t s)
+{
+    SellDev A = sell_of(h);
+    const int T = TFS_TPB;
+    if (h->sweep_mode == 1) {
+        k_sweep_df<double, 1, 2><<<h->sweep_grid, T, 0, s>>>(A, h->val, h->v.d, nullptr, nullptr, nullptr,
+                                                             nullptr, nullptr, nullptr, h->flags, h->ctl, h->st);
+        return 1;
+    }
+    for (int l = 0; l < h->n_levels; l++) {
+        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+        k_dic_form<<<(r1 - r0 + T - 1) / T, T, 0, s>>>(A, h->val, h->v.d, r0, r1, h->st);
+    }
+    return h->n_levels;
+}
+
 static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond);
 static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count);
 static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst);
@@ -392,13 +423,7 @@ static int launch_prologue(tfs_handle *h, int method, int prec, cudaGraphConditi
                                   h->precision == TFS_MIXED ? h->val32 : nullptr, h->nnz_pad);
     k_load<<<G, T, 0, s>>>(A, h->val, h->perm, h->params, h->v, h->st, h->part, prec);
     *count = 3;
-    if (prec == 2) {
-        for (int l = 0; l < h->n_levels; l++) {
-            int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-            k_dic_form<<<(r1 - r0 + T - 1) / T, T, 0, s>>>(A, h->val, h->v.d, r0, r1, h->st);
-        }
-        *count += h->n_levels;
-    }
+    if (prec == 2) *count += launch_dic_form(h, s);
     if (h->precision == TFS_MIXED) {
         tfs_mixed_prologue(h, method, prec, cond);
         *count += 2;
@@ -420,9 +445,23 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 {
     SellDev A = sell_of(h);
     const int T_ = TFS_TPB;
-    const T *val, *d;
-    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
-    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
+    const T *val;
+    T *d;
+    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (T *)h->v.d; }
+    else { val = (const T *)h->val32; d = (T *)h->f.d; }
+    if (h->sweep_mode == 1) {
+        const int G = h->sweep_grid;
+        if (nr == 1) {
+            k_sweep_df<T, 1, 0><<<G, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, h->flags, h->ctl, h->st);
+            k_sweep_df<T, 1, 1><<<G, T_, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, h->flags, h->ctl, h->st);
+        } else {
+            k_sweep_df<T, 2, 0><<<G, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, h->flags, h->ctl, h->st);
+            k_sweep_df<T, 2, 1><<<G, T_, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, h->flags, h->ctl, h->st);
+        }
+        *count += 2;
+        CKL("sweep launch");
+        return TFS_OK;
+    }
     for (int l = 0; l < h->n_levels; l++) {
         int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
         int g = (r1 - r0 + T_ - 1) / T_;
@@ -837,12 +876,7 @@ static int form_prec(tfs_handle *h, int prec)
 {
     SellDev A = sell_of(h);
     k_diag_form<<<(h->n_int + 255) / 256, 256, 0, h->stream>>>(A, h->val, h->v.d, prec == 1 ? 1 : 0);
-    if (prec == 2) {
-        for (int l = 0; l < h->n_levels; l++) {
-            int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-            k_dic_form<<<(r1 - r0 + 255) / 256, 256, 0, h->stream>>>(A, h->val, h->v.d, r0, r1, h->st);
-        }
-    }
+    if (prec == 2) launch_dic_form(h, h->stream);
     CKL("prec form");
     return TFS_OK;
 }

@@ -47,6 +47,12 @@ struct DevState {
     int pad1;
 };
 
+// Control words of the single-launch dataflow sweeps; they persist across
+// solves (the epoch numbers the readiness flags, which are never cleared).
+struct SweepCtl {
+    unsigned int ticket, done, epoch, abort;
+};
+
 // Per-call arguments, written by the host before every graph launch.
 struct DevParams {
     double tol;
@@ -89,6 +95,8 @@ struct tfs_handle {
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int grid = 0;                      // blocks of the chunk kernels
+    int sweep_grid = 0;                // blocks of the dataflow sweeps
+    int sweep_mode = 1;                // 1: dataflow single launch, 0: one launch per level
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row
@@ -100,6 +108,8 @@ struct tfs_handle {
     float *val32 = nullptr;
     double *stage_val = nullptr, *stage_b = nullptr, *stage_x = nullptr;
     double *part = nullptr;
+    unsigned int *flags = nullptr;     // readiness flag per internal row
+    SweepCtl *ctl = nullptr;
     DevState *st = nullptr;
     DevParams *params = nullptr;
     void *vec_pool = nullptr, *vec32_pool = nullptr;

@@ -380,6 +380,120 @@ k_bwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
     }
 }
 
+// ---------------------------------------------- dataflow (single-launch) sweeps
+//
+// One launch runs a whole triangular sweep.  Blocks take 256-row tiles from a
+// ticket counter in level order (descending for the backward sweep); a row
+// waits for the readiness flags of the rows it reads, then does the
+// reference's per-row arithmetic.  No deadlock is possible: a row only waits
+// for rows of strictly earlier levels, which sit in earlier tickets, and a
+// ticket is taken only by a block that is already running.  Rows of one
+// 32-row slice share a level (levels are padded to 32), so no thread ever
+// waits on another lane of its own warp.  Every wait is bounded: after
+// TFS_MAX_POLLS polls the kernel raises ctl->abort, every other waiter gives
+// up within 64 polls, and the solve ends with TFS_ERR_TIMEOUT.
+// Flags carry the epoch of the sweep that wrote them; the last block of a
+// sweep publishes the epoch and re-arms the ticket counter.
+
+#define TFS_MAX_POLLS (1 << 20)
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __noinline__ bool wait_flag_slow(const unsigned *f, unsigned e, SweepCtl *ctl)
+{
+    for (int it = 0; it < TFS_MAX_POLLS; it++) {
+        if (it >= 32) __nanosleep(64);
+        if (ld_acquire(f) == e) return true;
+        if ((it & 63) == 63 && *(volatile unsigned *)&ctl->abort) return false;
+    }
+    atomicExch(&ctl->abort, 1u);
+    return false;
+}
+__device__ __forceinline__ void wait_flag(const unsigned *f, unsigned e, SweepCtl *ctl)
+{
+    if (ld_acquire(f) != e) wait_flag_slow(f, e, ctl);
+}
+
+// MODE 0: forward sweep y = (b - L y) * D; MODE 1: backward sweep
+// z = (y/(D+TINY) - U z) * D; MODE 2: DIC form D_i = 1/(a_ii - sum D_k a^2).
+template <typename T, int NR, int MODE>
+__global__ void __launch_bounds__(TFS_TPB)
+k_sweep_df(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
+           T *o1, T *o2, const T *y1, const T *y2, unsigned *flag, SweepCtl *ctl, DevState *st)
+{
+    if (st->done) return;
+    __shared__ int s_tile;
+    const unsigned e = *(volatile unsigned *)&ctl->epoch + 1u;
+    const int n_tiles = A.n_chunks;
+    if (MODE != 1 && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl->ticket, 1u);
+        __syncthreads();
+        const int t = s_tile;
+        __syncthreads();
+        if (t >= n_tiles) break;
+        const int tile = MODE == 1 ? n_tiles - 1 - t : t;
+        const int i = tile * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        if (g.len == 0) {
+            if (MODE == 2) d[i] = (T)1;
+            else { o1[i] = (T)0; if (NR == 2) o2[i] = (T)0; }
+            continue;
+        }
+        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+        for (int j = j0; j < j1; j++) wait_flag(flag + __ldg(A.col + g.off + (j << 5)), e, ctl);
+        if (MODE == 2) {
+            T sum1 = __ldg(val + g.off + (g.dpos << 5));
+            for (int j = 0; j < g.dpos; j++) {
+                int ee = g.off + (j << 5);
+                T a = __ldg(val + ee);
+                sum1 = sum1 - __ldcg(d + __ldg(A.col + ee)) * a * a;
+            }
+            d[i] = (T)1 / sum1;
+        } else {
+            const T di = d[i];
+            T s1, s2 = (T)0;
+            if (MODE == 0) { s1 = b1[i]; if (NR == 2) s2 = b2[i]; }
+            else { s1 = y1[i] / (di + (T)TINY); if (NR == 2) s2 = y2[i] / (di + (T)TINY); }
+            for (int j = j0; j < j1; j++) {
+                int ee = g.off + (j << 5);
+                int k = __ldg(A.col + ee);
+                T a = __ldg(val + ee);
+                s1 = s1 - a * __ldcg(o1 + k);
+                if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
+            }
+            o1[i] = s1 * di;
+            if (NR == 2) o2[i] = s2 * di;
+        }
+        __threadfence();
+        st_release(flag + i, e);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl->done, 1u) == gridDim.x - 1) {
+            ctl->ticket = 0u;
+            ctl->done = 0u;
+            ctl->epoch = e;
+            if (ctl->abort) {
+                ctl->abort = 0u;
+                st->status = TFS_ERR_TIMEOUT;
+                st->done = 1;
+                st->niter_out = st->iter + 1;
+            }
+            __threadfence();
+        }
+    }
+}
+
 // rho after the sweeps: CG (r, z) (Cg.f90:108-112); BiCG (z1, r2) (Bicg.f90:113-117).
 template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)
