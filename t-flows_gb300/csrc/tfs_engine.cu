@@ -10,6 +10,7 @@
 // The graph of each (method, prec, arithmetic) is built once per handle and
 // reused; per-call arguments go through a small DevParams block copied in
 // before the launch.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -143,15 +144,61 @@ static int validate_csr(int32_t n, int32_t nnz, const int32_t *row1, const int32
 
 // ------------------------------------------------------- registration
 
-static int compute_levels(tfs_handle *h, const std::vector<int> &row0, const std::vector<int> &col0,
-                          const std::vector<int> &dia0, std::vector<int32_t> &level)
+// Dependency lists of the level analysis: for row i every k < i that the
+// forward sweep reads (a_ik != 0) and, when the pattern is not structurally
+// symmetric, every k < i whose row reads i in the backward sweep (a_ki != 0),
+// so that descending levels are a valid backward schedule too.
+static void dependency_lists(int n, const std::vector<int> &row0, const std::vector<int> &col0,
+                             const std::vector<int> &dia0, std::vector<int> &lrow,
+                             std::vector<int> &lcol)
+{
+    auto has = [&](int r, int c) {
+        int lo = row0[r], hi = row0[r + 1] - 1;
+        while (lo <= hi) {
+            int mid = lo + (hi - lo) / 2;
+            if (col0[mid] == c) return true;
+            if (col0[mid] < c) lo = mid + 1; else hi = mid - 1;
+        }
+        return false;
+    };
+    bool sym = true;
+    for (int i = 0; i < n && sym; i++)
+        for (int j = row0[i]; j < row0[i + 1]; j++)
+            if (col0[j] != i && !has(col0[j], i)) { sym = false; break; }
+    lrow.assign(n + 1, 0);
+    if (sym) {
+        for (int i = 0; i < n; i++) lrow[i + 1] = lrow[i] + (dia0[i] - row0[i]);
+        lcol.resize(lrow[n]);
+        for (int i = 0; i < n; i++)
+            for (int j = row0[i]; j < dia0[i]; j++) lcol[lrow[i] + (j - row0[i])] = col0[j];
+        return;
+    }
+    std::vector<std::vector<int>> dep(n);
+    for (int i = 0; i < n; i++)
+        for (int j = row0[i]; j < row0[i + 1]; j++) {
+            int k = col0[j];
+            if (k < i) dep[i].push_back(k);
+            else if (k > i) dep[k].push_back(i);
+        }
+    for (int i = 0; i < n; i++) {
+        std::sort(dep[i].begin(), dep[i].end());
+        dep[i].erase(std::unique(dep[i].begin(), dep[i].end()), dep[i].end());
+        lrow[i + 1] = lrow[i] + (int)dep[i].size();
+    }
+    lcol.resize(lrow[n]);
+    for (int i = 0; i < n; i++) std::copy(dep[i].begin(), dep[i].end(), lcol.begin() + lrow[i]);
+}
+
+static int compute_levels(tfs_handle *h, const std::vector<int> &lrow, const std::vector<int> &lcol,
+                          std::vector<int32_t> &level)
 {
     const int n = h->n;
-    int *d_row = nullptr, *d_col = nullptr, *d_dia = nullptr, *d_lvl = nullptr, *d_chg = nullptr;
+    const size_t ndep = lcol.size();
+    int *d_row = nullptr, *d_col = nullptr, *d_lvl = nullptr, *d_chg = nullptr;
     int rc = TFS_OK;
     const int PASSES = 8;
     auto cleanup = [&]() {
-        cudaFree(d_row); cudaFree(d_col); cudaFree(d_dia); cudaFree(d_lvl); cudaFree(d_chg);
+        cudaFree(d_row); cudaFree(d_col); cudaFree(d_lvl); cudaFree(d_chg);
     };
 #define CKC(call)                                                       \
     do {                                                                \
@@ -159,13 +206,11 @@ static int compute_levels(tfs_handle *h, const std::vector<int> &row0, const std
         if (_e != cudaSuccess) { rc = tfs_engine_error(_e, #call); cleanup(); return rc; } \
     } while (0)
     CKC(cudaMalloc(&d_row, sizeof(int) * (n + 1)));
-    CKC(cudaMalloc(&d_col, sizeof(int) * (size_t)h->nnz));
-    CKC(cudaMalloc(&d_dia, sizeof(int) * n));
+    CKC(cudaMalloc(&d_col, sizeof(int) * (ndep ? ndep : 1)));
     CKC(cudaMalloc(&d_lvl, sizeof(int) * n));
     CKC(cudaMalloc(&d_chg, sizeof(int) * PASSES));
-    CKC(cudaMemcpyAsync(d_row, row0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
-    CKC(cudaMemcpyAsync(d_col, col0.data(), sizeof(int) * (size_t)h->nnz, cudaMemcpyHostToDevice, h->stream));
-    CKC(cudaMemcpyAsync(d_dia, dia0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+    CKC(cudaMemcpyAsync(d_row, lrow.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
+    if (ndep) CKC(cudaMemcpyAsync(d_col, lcol.data(), sizeof(int) * ndep, cudaMemcpyHostToDevice, h->stream));
     CKC(cudaMemsetAsync(d_lvl, 0, sizeof(int) * n, h->stream));
     int grid = (n + 255) / 256;
     if (grid > h->sm_count * 8) grid = h->sm_count * 8;
@@ -173,7 +218,7 @@ static int compute_levels(tfs_handle *h, const std::vector<int> &row0, const std
     for (int64_t done_passes = 0; done_passes <= (int64_t)n + PASSES; done_passes += PASSES) {
         CKC(cudaMemsetAsync(d_chg, 0, sizeof(int) * PASSES, h->stream));
         for (int p = 0; p < PASSES; p++)
-            k_level_pass<<<grid, 256, 0, h->stream>>>(n, d_row, d_col, d_dia, d_lvl, d_chg + p);
+            k_level_pass<<<grid, 256, 0, h->stream>>>(n, d_row, d_col, d_lvl, d_chg + p);
         CKC(cudaGetLastError());
         int chg[PASSES];
         CKC(cudaMemcpyAsync(chg, d_chg, sizeof chg, cudaMemcpyDeviceToHost, h->stream));
@@ -197,7 +242,9 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     for (int i = 0; i < n; i++) dia0[i] = dia1[i] - 1;
 
     std::vector<int32_t> level;
-    int rc = compute_levels(h, row0, col0, dia0, level);
+    std::vector<int> lrow, lcol;
+    dependency_lists(n, row0, col0, dia0, lrow, lcol);
+    int rc = compute_levels(h, lrow, lcol, level);
     if (rc) return rc;
     int nl = 0;
     for (int i = 0; i < n; i++) {

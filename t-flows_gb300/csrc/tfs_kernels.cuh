@@ -796,16 +796,17 @@ __global__ void k_diag_apply(int n_int, const double *__restrict__ d, const doub
 
 // ------------------------------------------------- dependency analysis
 
-// One relaxation pass of level(i) = max(0, 1 + max_{lower j} level(col j)).
-// Levels only grow and never exceed their fixed point, so passes run in
-// place until one changes nothing.
-__global__ void k_level_pass(int n, const int *__restrict__ row0, const int *__restrict__ col0,
-                             const int *__restrict__ dia0, int *level, int *changed)
+// One relaxation pass of level(i) = max(0, 1 + max_{k in dep(i)} level(k)),
+// dep(i) = the rows i must wait for (lrow/lcol, all k < i).  Levels only grow
+// and never exceed their fixed point, so passes run in place until one
+// changes nothing.
+__global__ void k_level_pass(int n, const int *__restrict__ lrow, const int *__restrict__ lcol,
+                             int *level, int *changed)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int l = 0;
-        for (int j = __ldg(row0 + i); j < __ldg(dia0 + i); j++) {
-            int lk = ((volatile int *)level)[__ldg(col0 + j)] + 1;
+        for (int j = __ldg(lrow + i); j < __ldg(lrow + i + 1); j++) {
+            int lk = ((volatile int *)level)[__ldg(lcol + j)] + 1;
             l = lk > l ? lk : l;
         }
         if (l > level[i]) {
