@@ -81,6 +81,18 @@ static SellDev sell_of(const tfs_handle *h)
     return A;
 }
 
+static TileTable tile_table(const tfs_handle *h)
+{
+    TileTable t;
+    t.n_tiles = h->n_tiles;
+    t.n_levels = h->n_levels;
+    t.tail_level = h->tail_level;
+    t.tile = h->tiles;
+    t.lvl_begin = h->d_lvl_begin;
+    t.lvl_tiles = h->d_lvl_tiles;
+    return t;
+}
+
 template <typename T>
 static int dalloc(tfs_handle *h, T **p, size_t count)
 {
@@ -314,19 +326,46 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
         (rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
         (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)) ||
         (rc = dalloc(h, &h->st, 1)) || (rc = dalloc(h, &h->params, 1)) ||
-        (rc = dalloc(h, &h->flags, n_int)) || (rc = dalloc(h, &h->ctl, 1)))
+        (rc = dalloc(h, &h->ctl, 1)))
         return rc;
-    CK(cudaMemsetAsync(h->flags, 0, sizeof(unsigned) * (size_t)n_int, h->stream));
     CK(cudaMemsetAsync(h->ctl, 0, sizeof(SweepCtl), h->stream));
     {
+        // Sweep work items: tiles of at most TFS_SWEEP_TPB rows inside one
+        // level, then one item for the tail (the levels after the last level
+        // with more than TFS_TAIL_ROWS rows).
+        int tail = nl;
+        while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= TFS_TAIL_ROWS) tail--;
+        if (tail == 0) tail = nl > 1 ? 1 : nl;   // level 0 always runs as tiles
+        h->tail_level = tail;
+        std::vector<int2> tiles;
+        std::vector<int> lvl_tiles(nl, 0);
+        for (int l = 0; l < tail; l++)
+            for (int r = h->lvl_begin[l]; r < h->lvl_begin[l + 1]; r += TFS_SWEEP_TPB) {
+                tiles.push_back(make_int2(r, l));
+                lvl_tiles[l]++;
+            }
+        if (tail < nl) {
+            tiles.push_back(make_int2(h->lvl_begin[tail], tail));
+            for (int l = tail; l < nl; l++) lvl_tiles[l] = 1;
+        }
+        h->n_tiles = (int)tiles.size();
+        if ((rc = dalloc(h, &h->tiles, tiles.size())) || (rc = dalloc(h, &h->d_lvl_begin, nl + 1)) ||
+            (rc = dalloc(h, &h->d_lvl_tiles, nl)) || (rc = dalloc(h, &h->lvl_cnt, 3 * (size_t)nl)))
+            return rc;
+        CK(cudaMemcpyAsync(h->tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_begin.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_lvl_tiles, lvl_tiles.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemsetAsync(h->lvl_cnt, 0, sizeof(unsigned long long) * 3 * (size_t)nl, h->stream));
         int occ = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_df<double, 2, 0>, TFS_TPB, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_lv<double, 2, 0>, TFS_SWEEP_TPB, 0));
         if (occ < 1) occ = 1;
         int gs = h->sm_count * occ;
-        h->sweep_grid = h->n_chunks < gs ? h->n_chunks : gs;
+        h->sweep_grid = h->n_tiles < gs ? h->n_tiles : gs;
         if (h->sweep_grid < 1) h->sweep_grid = 1;
         const char *env = getenv("TFS_SWEEP");
         if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
+        env = getenv("TFS_GRAPH");
+        if (env && strcmp(env, "0") == 0) h->eager = 1;
     }
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
@@ -339,8 +378,8 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     CK(cudaMemsetAsync(h->part, 0, sizeof(double) * (TFS_NPART * (size_t)h->grid + 64), h->stream));
     CK(cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream));
 
-    // Work vectors: 16 binary64 + 15 binary32, zero so padding rows stay zero.
-    const size_t nv64 = 16, nv32 = 15;
+    // Work vectors: 16 binary64 + 16 binary32, zero so padding rows stay zero.
+    const size_t nv64 = 16, nv32 = 16;
     double *pool = nullptr;
     float *pool32 = nullptr;
     if ((rc = dalloc(h, &pool, nv64 * (size_t)n_int)) || (rc = dalloc(h, &pool32, nv32 * (size_t)n_int)))
@@ -352,9 +391,9 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     double *v[16];
     for (size_t k = 0; k < nv64; k++) v[k] = pool + k * (size_t)n_int;
     h->v = Vec64{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12], v[13], v[14], v[15]};
-    float *f[15];
+    float *f[16];
     for (size_t k = 0; k < nv32; k++) f[k] = pool32 + k * (size_t)n_int;
-    h->f = Vec32{f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10], f[11], f[12], f[13], f[14]};
+    h->f = Vec32{f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10], f[11], f[12], f[13], f[14], f[15]};
     CK(cudaStreamSynchronize(h->stream));
     return TFS_OK;
 }
@@ -369,7 +408,8 @@ static void free_handle(tfs_handle *h)
         if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
     }
     void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
-                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params, h->flags, h->ctl,
+                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params, h->ctl,
+                    h->lvl_cnt, h->tiles, h->d_lvl_begin, h->d_lvl_tiles,
                     h->vec_pool, h->vec32_pool};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -442,8 +482,9 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
     SellDev A = sell_of(h);
     const int T = TFS_TPB;
     if (h->sweep_mode == 1) {
-        k_sweep_df<double, 1, 2><<<h->sweep_grid, T, 0, s>>>(A, h->val, h->v.d, nullptr, nullptr, nullptr,
-                                                             nullptr, nullptr, nullptr, h->flags, h->ctl, h->st);
+        k_sweep_lv<double, 1, 2><<<h->sweep_grid, TFS_SWEEP_TPB, 0, s>>>(A, h->val, h->v.d, nullptr, nullptr, nullptr,
+                                                             nullptr, nullptr, nullptr, tile_table(h), h->ctl,
+                                                             h->lvl_cnt, h->st);
         return 1;
     }
     for (int l = 0; l < h->n_levels; l++) {
@@ -453,14 +494,14 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
     return h->n_levels;
 }
 
-static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond);
-static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count);
+static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int prec, cudaGraphConditionalHandle cond);
+static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec, cudaGraphConditionalHandle cond, int *count);
 static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst);
 static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s);
 
-static int launch_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+static int launch_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
+                           cudaGraphConditionalHandle cond, int *count)
 {
-    cudaStream_t s = h->stream;
     SellDev A = sell_of(h);
     const int G = h->grid, T = TFS_TPB;
     int gv = (h->nnz_pad + T - 1) / T;
@@ -472,7 +513,7 @@ static int launch_prologue(tfs_handle *h, int method, int prec, cudaGraphConditi
     *count = 3;
     if (prec == 2) *count += launch_dic_form(h, s);
     if (h->precision == TFS_MIXED) {
-        tfs_mixed_prologue(h, method, prec, cond);
+        tfs_mixed_prologue(h, s, method, prec, cond);
         *count += 2;
     } else {
         if (method == TFS_CG) k_residual<0><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
@@ -498,12 +539,13 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     else { val = (const T *)h->val32; d = (T *)h->f.d; }
     if (h->sweep_mode == 1) {
         const int G = h->sweep_grid;
+        TileTable tt = tile_table(h);
         if (nr == 1) {
-            k_sweep_df<T, 1, 0><<<G, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, h->flags, h->ctl, h->st);
-            k_sweep_df<T, 1, 1><<<G, T_, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, h->flags, h->ctl, h->st);
+            k_sweep_lv<T, 1, 0><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, tt, h->ctl, h->lvl_cnt, h->st);
+            k_sweep_lv<T, 1, 1><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, tt, h->ctl, h->lvl_cnt, h->st);
         } else {
-            k_sweep_df<T, 2, 0><<<G, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, h->flags, h->ctl, h->st);
-            k_sweep_df<T, 2, 1><<<G, T_, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, h->flags, h->ctl, h->st);
+            k_sweep_lv<T, 2, 0><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, tt, h->ctl, h->lvl_cnt, h->st);
+            k_sweep_lv<T, 2, 1><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, tt, h->ctl, h->lvl_cnt, h->st);
         }
         *count += 2;
         CKL("sweep launch");
@@ -530,9 +572,9 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 
 // After the binary64 preconditioner is formed: d32 = (float) d, then the
 // binary64 initial residual (k_mx_true<INIT>).
-static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond)
+static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
+                              cudaGraphConditionalHandle cond)
 {
-    cudaStream_t s = h->stream;
     SellDev A = sell_of(h);
     const int G = h->grid, T = TFS_TPB;
     k_mx_cast<<<G, T, 0, s>>>(h->n_int, h->v.d, h->f.d);
@@ -543,9 +585,9 @@ static int tfs_mixed_prologue(tfs_handle *h, int method, int prec, cudaGraphCond
     return TFS_OK;
 }
 
-static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
+                          cudaGraphConditionalHandle cond, int *count)
 {
-    cudaStream_t s = h->stream2;
     SellDev A = sell_of(h);
     const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
     Vec64 &V = h->v;
@@ -560,12 +602,14 @@ static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditio
             k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
             k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
             k_mx_cg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
         } else {
-            k_mx_cg_p<false><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
             k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
             k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 4;
         }
@@ -576,12 +620,14 @@ static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditio
             k_mx_bicg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
             k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_bicg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
         } else {
-            k_mx_bicg_p<false><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_bicg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
             k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_bicg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 4;
         }
@@ -593,6 +639,7 @@ static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditio
             k_mx_cgs_q<false><<<G, T, 0, s>>>(nc, F, h->st);
             if ((rc = launch_sweeps<float>(h, s, 1, F.w, nullptr, F.y, nullptr, F.p, nullptr, count))) return rc;
             k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
         } else {
@@ -600,6 +647,7 @@ static int tfs_mixed_body(tfs_handle *h, int method, int prec, cudaGraphConditio
             k_mx_spmv_v<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_cgs_q<true><<<G, T, 0, s>>>(nc, F, h->st);
             k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
         }
@@ -618,9 +666,9 @@ static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s)
     k_mx_spmv_pq<<<h->grid, TFS_TPB, 0, s>>>(sell_of(h), h->val32, h->f.p, h->f.q, h->st, h->part);
 }
 
-static int launch_body(tfs_handle *h, int method, int prec, cudaGraphConditionalHandle cond, int *count)
+static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
+                       cudaGraphConditionalHandle cond, int *count)
 {
-    cudaStream_t s = h->stream2;
     SellDev A = sell_of(h);
     const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
     Vec64 &V = h->v;
@@ -635,7 +683,7 @@ static int launch_body(tfs_handle *h, int method, int prec, cudaGraphConditional
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 4;
         } else {
-            k_cg_p<false><<<G, T, 0, s>>>(nc, V, h->st);
+            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
             k_spmv_pq<<<G, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
             k_cg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 3;
@@ -649,7 +697,7 @@ static int launch_body(tfs_handle *h, int method, int prec, cudaGraphConditional
             k_bicg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 4;
         } else {
-            k_bicg_p<false><<<G, T, 0, s>>>(nc, V, h->st);
+            k_bicg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
             k_spmv2_pq<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
             k_bicg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 3;
@@ -703,7 +751,7 @@ static int build_graph(tfs_handle *h, int method, int prec, GraphEntry &ge)
     };
     e = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return fail(e, "begin capture");
-    if ((rc = launch_prologue(h, method, prec, cond, &ge.prologue_kernels))) { fail(cudaErrorUnknown, "prologue"); return rc; }
+    if ((rc = launch_prologue(h, h->stream, method, prec, cond, &ge.prologue_kernels))) { fail(cudaErrorUnknown, "prologue"); return rc; }
     cudaStreamCaptureStatus cs;
     const cudaGraphNode_t *deps = nullptr;
     size_t ndeps = 0;
@@ -723,8 +771,8 @@ static int build_graph(tfs_handle *h, int method, int prec, GraphEntry &ge)
     // Body, captured on the second stream into the conditional node's graph.
     e = cudaStreamBeginCaptureToGraph(h->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return fail(e, "begin body capture");
-    if (h->precision == TFS_MIXED) rc = tfs_mixed_body(h, method, prec, cond, &ge.body_kernels);
-    else rc = launch_body(h, method, prec, cond, &ge.body_kernels);
+    if (h->precision == TFS_MIXED) rc = tfs_mixed_body(h, h->stream2, method, prec, cond, &ge.body_kernels);
+    else rc = launch_body(h, h->stream2, method, prec, cond, &ge.body_kernels);
     if (rc) { fail(cudaErrorUnknown, "body"); return rc; }
     cudaGraph_t btmp;
     e = cudaStreamEndCapture(h->stream2, &btmp);
@@ -739,8 +787,41 @@ static int build_graph(tfs_handle *h, int method, int prec, GraphEntry &ge)
     return TFS_OK;
 }
 
+// The same kernels without a graph: the host drives the loop, reading the
+// device's done flag after every TFS_EAGER_BATCH iterations (kernels of a
+// finished solve return at once).  Used for kernel-level profiling, which
+// cannot look inside graphs with conditional nodes.
+#define TFS_EAGER_BATCH 8
+static int run_eager(tfs_handle *h, int method, int prec, GraphEntry *ge)
+{
+    cudaStream_t s = h->stream;
+    int rc, cnt = 0;
+    if ((rc = launch_prologue(h, s, method, prec, 0, &cnt))) return rc;
+    ge->prologue_kernels = cnt;
+    const int limit = (h->h_params->niter_max > 0 ? h->h_params->niter_max : 0) + 8;
+    for (int it = 0; it < limit; it += TFS_EAGER_BATCH) {
+        CK(cudaMemcpyAsync(h->h_state, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h->h_state->done) break;
+        for (int b = 0; b < TFS_EAGER_BATCH; b++) {
+            if (h->precision == TFS_MIXED) rc = tfs_mixed_body(h, s, method, prec, 0, &cnt);
+            else rc = launch_body(h, s, method, prec, 0, &cnt);
+            if (rc) return rc;
+        }
+        ge->body_kernels = cnt;
+    }
+    if ((rc = launch_epilogue(h, &cnt))) return rc;
+    ge->epilogue_kernels = cnt;
+    return TFS_OK;
+}
+
 static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
 {
+    if (h->eager) {
+        static thread_local GraphEntry eager_entry;
+        *out = &eager_entry;
+        return TFS_OK;
+    }
     int key = method | (prec << 4) | (h->precision << 8);
     auto it = h->graphs.find(key);
     if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
@@ -779,7 +860,11 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
         CK(cudaMemcpyAsync(h->stage_x, x, sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, s));
     }
     CK(cudaEventRecord(h->ev0, s));
-    CK(cudaGraphLaunch(ge->exec, s));
+    if (h->eager) {
+        if ((rc = run_eager(h, method, prec, ge))) return rc;
+    } else {
+        CK(cudaGraphLaunch(ge->exec, s));
+    }
     CK(cudaEventRecord(h->ev1, s));
     if (!device_ptrs) {
         CK(cudaMemcpyAsync(x, h->stage_x, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, s));

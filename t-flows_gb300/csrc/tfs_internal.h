@@ -24,6 +24,8 @@
 #include "../../include/tfs_solver.h"
 
 #define TFS_TPB 256           // threads per block = rows per chunk
+#define TFS_SWEEP_TPB 1024    // threads per block = rows per tile of the level sweeps
+#define TFS_TAIL_ROWS 4096    // levels after the last one above this size form the tail
 #define TFS_NPART 4           // values reduced at once, at most
 
 // Device-resident state of one solve.  Written by k_init from DevParams and
@@ -47,10 +49,14 @@ struct DevState {
     int pad1;
 };
 
-// Control words of the single-launch dataflow sweeps; they persist across
-// solves (the epoch numbers the readiness flags, which are never cleared).
+// Control words of the single-launch level sweeps, one set per sweep kind
+// (0 DIC form, 1 forward, 2 backward).  They persist across solves: the
+// epoch of a kind counts its completed sweeps, and the per-level tile
+// counters are compared against epoch * tiles(level), so nothing is cleared.
 struct SweepCtl {
-    unsigned int ticket, done, epoch, abort;
+    unsigned int ticket[3], done[3];
+    unsigned int abort, pad;
+    unsigned long long epoch[3];
 };
 
 // Per-call arguments, written by the host before every graph launch.
@@ -79,6 +85,7 @@ struct Vec64 {
 // Work vectors (binary32) of the mixed-precision inner iteration.
 struct Vec32 {
     float *r, *r2, *p, *p2, *q, *q2, *u1, *u2, *v2, *w, *d, *y, *y2, *z, *z2;
+    float *e;   // solution correction since the last binary64 true residual
 };
 
 struct GraphEntry {
@@ -97,6 +104,7 @@ struct tfs_handle {
     int grid = 0;                      // blocks of the chunk kernels
     int sweep_grid = 0;                // blocks of the dataflow sweeps
     int sweep_mode = 1;                // 1: dataflow single launch, 0: one launch per level
+    int eager = 0;                     // 1: launch kernels directly, no CUDA graph
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row
@@ -108,7 +116,10 @@ struct tfs_handle {
     float *val32 = nullptr;
     double *stage_val = nullptr, *stage_b = nullptr, *stage_x = nullptr;
     double *part = nullptr;
-    unsigned int *flags = nullptr;     // readiness flag per internal row
+    unsigned long long *lvl_cnt = nullptr;  // finished tiles per level, 3 sets
+    int2 *tiles = nullptr;             // (first row, level) per sweep tile
+    int *d_lvl_begin = nullptr, *d_lvl_tiles = nullptr;
+    int n_tiles = 0, tail_level = 0;
     SweepCtl *ctl = nullptr;
     DevState *st = nullptr;
     DevParams *params = nullptr;

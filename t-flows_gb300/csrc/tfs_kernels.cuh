@@ -42,6 +42,9 @@ __device__ __forceinline__ RowGeom row_geom(const SellDev &A, int i)
 
 // Sequential sum s - sum_{j0<=j<j1} a_j x_col(j) (SUB) or s + ... (ADD),
 // loads of four entries issued before their products are summed in order.
+// The gathers of x bypass L1 (ld.global.cg): with the random cell numbering
+// of the workloads they almost never hit there, and allocating them in L1
+// made L1 throughput the limiter of the SpMV.
 template <bool SUB, typename VT, typename XT, typename AT>
 __device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
                                         const VT *__restrict__ val,
@@ -52,13 +55,13 @@ __device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
         int e0 = off + (j << 5), e1 = e0 + 32, e2 = e0 + 64, e3 = e0 + 96;
         int k0 = __ldg(col + e0), k1 = __ldg(col + e1), k2 = __ldg(col + e2), k3 = __ldg(col + e3);
         AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1), a2 = (AT)__ldg(val + e2), a3 = (AT)__ldg(val + e3);
-        AT x0 = (AT)x[k0], x1 = (AT)x[k1], x2 = (AT)x[k2], x3 = (AT)x[k3];
+        AT x0 = (AT)__ldcg(x + k0), x1 = (AT)__ldcg(x + k1), x2 = (AT)__ldcg(x + k2), x3 = (AT)__ldcg(x + k3);
         if (SUB) { s = s - a0 * x0; s = s - a1 * x1; s = s - a2 * x2; s = s - a3 * x3; }
         else     { s = s + a0 * x0; s = s + a1 * x1; s = s + a2 * x2; s = s + a3 * x3; }
     }
     for (; j < j1; j++) {
         int e = off + (j << 5);
-        AT a = (AT)__ldg(val + e), xv = (AT)x[__ldg(col + e)];
+        AT a = (AT)__ldg(val + e), xv = (AT)__ldcg(x + __ldg(col + e));
         if (SUB) s = s - a * xv; else s = s + a * xv;
     }
     return s;
@@ -75,7 +78,7 @@ __device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict
         int e0 = off + (j << 5), e1 = e0 + 32;
         int k0 = __ldg(col + e0), k1 = __ldg(col + e1);
         AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1);
-        AT p0 = (AT)x1[k0], p1 = (AT)x1[k1], q0 = (AT)x2[k0], q1 = (AT)x2[k1];
+        AT p0 = (AT)__ldcg(x1 + k0), p1 = (AT)__ldcg(x1 + k1), q0 = (AT)__ldcg(x2 + k0), q1 = (AT)__ldcg(x2 + k1);
         if (SUB) { s1 = s1 - a0 * p0; s2 = s2 - a0 * q0; s1 = s1 - a1 * p1; s2 = s2 - a1 * q1; }
         else     { s1 = s1 + a0 * p0; s2 = s2 + a0 * q0; s1 = s1 + a1 * p1; s2 = s2 + a1 * q1; }
     }
@@ -83,8 +86,9 @@ __device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict
         int e = off + (j << 5);
         int k = __ldg(col + e);
         AT a = (AT)__ldg(val + e);
-        if (SUB) { s1 = s1 - a * (AT)x1[k]; s2 = s2 - a * (AT)x2[k]; }
-        else     { s1 = s1 + a * (AT)x1[k]; s2 = s2 + a * (AT)x2[k]; }
+        AT p = (AT)__ldcg(x1 + k), q = (AT)__ldcg(x2 + k);
+        if (SUB) { s1 = s1 - a * p; s2 = s2 - a * q; }
+        else     { s1 = s1 + a * p; s2 = s2 + a * q; }
     }
 }
 
@@ -228,7 +232,7 @@ k_load(SellDev A, const double *__restrict__ val, const int *__restrict__ perm,
         if (o >= 0) { bi = b[o]; xi = x0[o]; }
         V.r[i] = bi;
         V.x[i] = xi;
-        acc = acc + bi * bi;
+        acc = fma(bi, bi, acc);
         RowGeom g = row_geom(A, i);
         V.d[i] = (prec == 1 && g.len > 0) ? val[g.off + (g.dpos << 5)] : 1.0;
     }
@@ -288,9 +292,14 @@ k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
         double r = row_accum<true, double, double, double>(V.r[i], A.col, val, V.x, g.off, 0, g.len);
         V.r[i] = r;
         if (METHOD != 0) V.r2[i] = r;
-        e2 = e2 + r * r;
-        if (METHOD == 2) rz = rz + r * r;               // Cgs.f90:105-109, r2 = r1
-        else if (fused) { double z = r / V.d[i]; rz = rz + (METHOD == 0 ? r * z : z * r); }
+        e2 = fma(r, r, e2);
+        if (METHOD == 2) rz = fma(r, r, rz);            // Cgs.f90:105-109, r2 = r1
+        else if (fused) {                               // z = M^-1 r, kept for the p update
+            double z = r / V.d[i];
+            V.z[i] = z;
+            if (METHOD == 1) V.z2[i] = z;
+            rz = fma(r, z, rz);
+        }
     }
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) {
@@ -380,109 +389,179 @@ k_bwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
     }
 }
 
-// ---------------------------------------------- dataflow (single-launch) sweeps
+// ---------------------------------------------- single-launch level sweeps
 //
-// One launch runs a whole triangular sweep.  Blocks take 256-row tiles from a
-// ticket counter in level order (descending for the backward sweep); a row
-// waits for the readiness flags of the rows it reads, then does the
-// reference's per-row arithmetic.  No deadlock is possible: a row only waits
-// for rows of strictly earlier levels, which sit in earlier tickets, and a
-// ticket is taken only by a block that is already running.  Rows of one
-// 32-row slice share a level (levels are padded to 32), so no thread ever
-// waits on another lane of its own warp.  Every wait is bounded: after
-// TFS_MAX_POLLS polls the kernel raises ctl->abort, every other waiter gives
-// up within 64 polls, and the solve ends with TFS_ERR_TIMEOUT.
-// Flags carry the epoch of the sweep that wrote them; the last block of a
-// sweep publishes the epoch and re-arms the ticket counter.
+// One launch runs a whole triangular sweep (or the DIC form) with blocks of
+// TFS_SWEEP_TPB threads.  Rows of the large levels are cut into tiles of at
+// most TFS_SWEEP_TPB rows that never straddle a level; the small trailing
+// levels (each at most TFS_TAIL_ROWS rows, the "tail") form one extra work
+// item that a single block runs level after level with __syncthreads()
+// between levels, so the deep, narrow end of the dependency chain costs no
+// grid-wide signalling.  Blocks take work items from a ticket counter in
+// level order (forward: large tiles then the tail; backward: the tail first,
+// then large tiles in descending order).  Before touching its dependencies a
+// large tile waits until every tile of the neighbouring level (l-1 forward,
+// l+1 backward) has finished in this sweep: each finished tile (and the tail
+// block, once per tail level) adds one to a 64-bit per-level counter, and
+// sweep number e is complete on level l when the counter reaches
+// e * tiles(l).  Rows keep the reference's per-row arithmetic.
+//
+// No deadlock is possible: a work item only waits for items with smaller
+// tickets, and a ticket is taken only by a block that is already running.
+// Every wait is bounded: after TFS_MAX_POLLS polls the kernel raises
+// ctl->abort, the other waiters give up within 64 polls, and the solve ends
+// with TFS_ERR_TIMEOUT.  The last block to finish publishes the sweep's epoch
+// and re-arms the ticket counter.
 
 #define TFS_MAX_POLLS (1 << 20)
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
+struct TileTable {
+    int n_tiles, n_levels, tail_level;   // tail_level == n_levels: no tail
+    const int2 *tile;          // (first internal row, level); the tail item is last
+    const int *lvl_begin;      // internal row offset of every level, n_levels + 1
+    const int *lvl_tiles;      // work items per level (1 for every tail level)
+};
 
-__device__ __noinline__ bool wait_flag_slow(const unsigned *f, unsigned e, SweepCtl *ctl)
+// Thread 0 of the block: wait until *cnt >= target (bounded).
+__device__ __noinline__ void wait_count(const unsigned long long *cnt, unsigned long long target,
+                                        SweepCtl *ctl)
 {
     for (int it = 0; it < TFS_MAX_POLLS; it++) {
-        if (it >= 32) __nanosleep(64);
-        if (ld_acquire(f) == e) return true;
-        if ((it & 63) == 63 && *(volatile unsigned *)&ctl->abort) return false;
+        if (*(volatile const unsigned long long *)cnt >= target) return;
+        if (it >= 16) __nanosleep(64);
+        if ((it & 63) == 63 && *(volatile unsigned *)&ctl->abort) return;
     }
     atomicExch(&ctl->abort, 1u);
-    return false;
-}
-__device__ __forceinline__ void wait_flag(const unsigned *f, unsigned e, SweepCtl *ctl)
-{
-    if (ld_acquire(f) != e) wait_flag_slow(f, e, ctl);
 }
 
-// MODE 0: forward sweep y = (b - L y) * D; MODE 1: backward sweep
+// One row of a sweep.  MODE 0: forward y = (b - L y) * D; MODE 1: backward
 // z = (y/(D+TINY) - U z) * D; MODE 2: DIC form D_i = 1/(a_ii - sum D_k a^2).
-template <typename T, int NR, int MODE>
-__global__ void __launch_bounds__(TFS_TPB)
-k_sweep_df(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
-           T *o1, T *o2, const T *y1, const T *y2, unsigned *flag, SweepCtl *ctl, DevState *st)
+// The first NP entries may come prefetched in kk/aa.
+template <typename T, int NR, int MODE, int NP>
+__device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict__ val, T *d,
+                                          const T *b1, const T *b2, T *o1, T *o2, const T *y1,
+                                          const T *y2, int i, const RowGeom &g, const int *kk,
+                                          const T *aa)
 {
-    if (st->done) return;
-    __shared__ int s_tile;
-    const unsigned e = *(volatile unsigned *)&ctl->epoch + 1u;
-    const int n_tiles = A.n_chunks;
-    if (MODE != 1 && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl->ticket, 1u);
-        __syncthreads();
-        const int t = s_tile;
-        __syncthreads();
-        if (t >= n_tiles) break;
-        const int tile = MODE == 1 ? n_tiles - 1 - t : t;
-        const int i = tile * TFS_TPB + threadIdx.x;
-        RowGeom g = row_geom(A, i);
-        if (g.len == 0) {
-            if (MODE == 2) d[i] = (T)1;
-            else { o1[i] = (T)0; if (NR == 2) o2[i] = (T)0; }
-            continue;
-        }
-        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
-        for (int j = j0; j < j1; j++) wait_flag(flag + __ldg(A.col + g.off + (j << 5)), e, ctl);
-        if (MODE == 2) {
-            T sum1 = __ldg(val + g.off + (g.dpos << 5));
-            for (int j = 0; j < g.dpos; j++) {
-                int ee = g.off + (j << 5);
-                T a = __ldg(val + ee);
-                sum1 = sum1 - __ldcg(d + __ldg(A.col + ee)) * a * a;
-            }
-            d[i] = (T)1 / sum1;
-        } else {
-            const T di = d[i];
-            T s1, s2 = (T)0;
-            if (MODE == 0) { s1 = b1[i]; if (NR == 2) s2 = b2[i]; }
-            else { s1 = y1[i] / (di + (T)TINY); if (NR == 2) s2 = y2[i] / (di + (T)TINY); }
-            for (int j = j0; j < j1; j++) {
-                int ee = g.off + (j << 5);
-                int k = __ldg(A.col + ee);
-                T a = __ldg(val + ee);
+    const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+    if (g.len == 0) {
+        if (MODE == 2) d[i] = (T)1;
+        else { o1[i] = (T)0; if (NR == 2) o2[i] = (T)0; }
+        return;
+    }
+    T s1, s2 = (T)0, di = (T)0;
+    if (MODE == 2) {
+        s1 = __ldg(val + g.off + (g.dpos << 5));
+    } else {
+        di = d[i];
+        if (MODE == 0) { s1 = b1[i]; if (NR == 2) s2 = b2[i]; }
+        else { s1 = y1[i] / (di + (T)TINY); if (NR == 2) s2 = y2[i] / (di + (T)TINY); }
+    }
+    // Entries in ascending column order: the prefetched ones first.
+    int j = j0;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        if (j < j1) {
+            const int k = kk[q];
+            const T a = aa[q];
+            if (MODE == 2) s1 = s1 - __ldcg(d + k) * a * a;
+            else {
                 s1 = s1 - a * __ldcg(o1 + k);
                 if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
             }
-            o1[i] = s1 * di;
-            if (NR == 2) o2[i] = s2 * di;
+            j++;
         }
+    }
+    for (; j < j1; j++) {
+        const int ee = g.off + (j << 5);
+        const int k = __ldg(A.col + ee);
+        const T a = __ldg(val + ee);
+        if (MODE == 2) s1 = s1 - __ldcg(d + k) * a * a;
+        else {
+            s1 = s1 - a * __ldcg(o1 + k);
+            if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
+        }
+    }
+    if (MODE == 2) { d[i] = (T)1 / s1; return; }
+    o1[i] = s1 * di;
+    if (NR == 2) o2[i] = s2 * di;
+}
+
+template <typename T, int NR, int MODE>
+__global__ void __launch_bounds__(TFS_SWEEP_TPB)
+k_sweep_lv(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
+           T *o1, T *o2, const T *y1, const T *y2, TileTable tt, SweepCtl *ctl,
+           unsigned long long *cnt_all, DevState *st)
+{
+    if (st->done) return;
+    constexpr int KIND = MODE == 2 ? 0 : (MODE == 0 ? 1 : 2);
+    unsigned long long *cnt = cnt_all + (size_t)KIND * tt.n_levels;
+    __shared__ int s_tile;
+    const unsigned long long e = *(volatile unsigned long long *)&ctl->epoch[KIND] + 1ull;
+    const bool has_tail = tt.tail_level < tt.n_levels;
+    if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl->ticket[KIND], 1u);
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= tt.n_tiles) break;
+        const int tix = MODE == 1 ? tt.n_tiles - 1 - t : t;
+        if (has_tail && tix == tt.n_tiles - 1) {
+            // The tail: all small levels by this block, level after level.
+            if (MODE != 1 && threadIdx.x == 0 && tt.tail_level > 0) {
+                int dep = tt.tail_level - 1;
+                wait_count(cnt + dep, e * (unsigned long long)__ldg(tt.lvl_tiles + dep), ctl);
+                __threadfence();
+            }
+            __syncthreads();
+            const int nt = tt.n_levels - tt.tail_level;
+            for (int q = 0; q < nt; q++) {
+                const int lev = MODE == 1 ? tt.n_levels - 1 - q : tt.tail_level + q;
+                const int r1 = __ldg(tt.lvl_begin + lev + 1);
+                for (int i = __ldg(tt.lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
+                    RowGeom g = row_geom(A, i);
+                    sweep_row<T, NR, MODE, 0>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, nullptr, nullptr);
+                }
+                __threadfence();
+                __syncthreads();
+                if (threadIdx.x == 0) atomicAdd(cnt + lev, 1ull);
+            }
+            continue;
+        }
+        const int2 tinfo = __ldg(tt.tile + tix);
+        const int lev = tinfo.y;
+        const int i = tinfo.x + threadIdx.x;
+        const bool active = i < __ldg(tt.lvl_begin + lev + 1);
+        RowGeom g{0, 0, 0};
+        if (active) g = row_geom(A, i);
+        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+        // Prefetch the first entries of the row before waiting.
+        int kk[4];
+        T aa[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int j = j0 + q;
+            kk[q] = 0;
+            aa[q] = (T)0;
+            if (j < j1) { int ee = g.off + (j << 5); kk[q] = __ldg(A.col + ee); aa[q] = __ldg(val + ee); }
+        }
+        const int dep = MODE == 1 ? lev + 1 : lev - 1;
+        if (threadIdx.x == 0 && dep >= 0 && dep < tt.n_levels) {
+            wait_count(cnt + dep, e * (unsigned long long)__ldg(tt.lvl_tiles + dep), ctl);
+            __threadfence();
+        }
+        __syncthreads();
+        if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa);
         __threadfence();
-        st_release(flag + i, e);
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(cnt + lev, 1ull);
     }
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&ctl->done, 1u) == gridDim.x - 1) {
-            ctl->ticket = 0u;
-            ctl->done = 0u;
-            ctl->epoch = e;
+        if (atomicAdd(&ctl->done[KIND], 1u) == gridDim.x - 1) {
+            ctl->ticket[KIND] = 0u;
+            ctl->done[KIND] = 0u;
+            ctl->epoch[KIND] = e;
             if (ctl->abort) {
                 ctl->abort = 0u;
                 st->status = TFS_ERR_TIMEOUT;
@@ -507,7 +586,7 @@ k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
     double acc = 0.0;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        acc = acc + (METHOD == 0 ? V.r[i] * V.z[i] : V.z[i] * V.r2[i]);
+        acc = METHOD == 0 ? fma(V.r[i], V.z[i], acc) : fma(V.z[i], V.r2[i], acc);
     }
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
@@ -544,7 +623,7 @@ k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ 
         RowGeom g = row_geom(A, i);
         double s = row_accum<false, double, double, double>(0.0, A.col, val, p, g.off, 0, g.len);
         q[i] = s;
-        acc = acc + p[i] * s;
+        acc = fma(p[i], s, acc);
     }
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
@@ -571,8 +650,8 @@ k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditio
         V.x[i] = V.x[i] + alfa * V.p[i];
         double r = V.r[i] - alfa * V.q[i];
         V.r[i] = r;
-        e2 = e2 + r * r;
-        if (FUSED) { double z = r / V.d[i]; rz = rz + r * z; }
+        e2 = fma(r, r, e2);
+        if (FUSED) { double z = r / V.d[i]; V.z[i] = z; rz = fma(r, z, rz); }
     }
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
@@ -611,7 +690,7 @@ k_spmv2_pq(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
         row_accum2<false, double, double, double>(s1, s2, A.col, val, V.p, V.p2, g.off, 0, g.len);
         V.q[i] = s1;
         V.q2[i] = s2;
-        acc = acc + V.p2[i] * s1;
+        acc = fma(V.p2[i], s1, acc);
     }
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
@@ -640,8 +719,13 @@ k_bicg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphCondit
         double r2 = V.r2[i] - alfa * V.q2[i];
         V.r[i] = r1;
         V.r2[i] = r2;
-        e2 = e2 + r1 * r1;
-        if (FUSED) { double z1 = r1 / V.d[i]; rz = rz + z1 * r2; }
+        e2 = fma(r1, r1, e2);
+        if (FUSED) {
+            double di = V.d[i], z1 = r1 / di;
+            V.z[i] = z1;
+            V.z2[i] = r2 / di;
+            rz = fma(z1, r2, rz);
+        }
     }
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
@@ -684,7 +768,7 @@ k_spmv_v(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, doubl
         RowGeom g = row_geom(A, i);
         double s = row_accum<false, double, double, double>(0.0, A.col, val, V.p2, g.off, 0, g.len);
         V.v2[i] = s;
-        acc = acc + V.r2[i] * s;
+        acc = fma(V.r2[i], s, acc);
     }
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
@@ -733,8 +817,8 @@ k_cgs_spmv_r(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, d
         double q2 = row_accum<false, double, double, double>(0.0, A.col, val, V.p, g.off, 0, g.len);
         double r1 = V.r[i] - alfa * q2;
         V.r[i] = r1;
-        e2 = e2 + r1 * r1;
-        rr = rr + r1 * V.r2[i];
+        e2 = fma(r1, r1, e2);
+        rr = fma(r1, V.r2[i], rr);
     }
     double v[2] = {e2, rr};
     if (grid_reduce<2>(v, part, &st->counter)) {

@@ -3,9 +3,14 @@
 // The Krylov recurrences run on binary32 matrix values and binary32 vectors
 // (r, p, q, z, ...), which cuts the bytes per iteration by about a third.
 // Binary64 is kept where the accuracy is decided:
-//   - every dot product (rho, (p,q), ||r||) accumulates in binary64;
+//   - every dot product (rho, (p,q), ||r||) is reduced in binary64 across
+//     threads and blocks; a thread first sums its own few rows (about 7 for
+//     a 2M-row system) in binary32 -- GB300's binary64 pipe is narrow, and
+//     per-element conversions to binary64 made these kernels FP64-bound;
 //   - alpha and beta are binary64 scalars;
-//   - the solution x is binary64 and takes x += alpha * p in binary64;
+//   - the solution x is binary64: the binary32 corrections alpha * p are
+//     summed in a binary32 vector e, which is added to x in binary64 (and
+//     cleared) right before every binary64 true residual;
 //   - the true residual r = b - A x is recomputed in binary64 with the
 //     binary64 matrix ("reliable update" defect correction) whenever the
 //     binary32 recursive residual has dropped by the factor delta (0.1) since
@@ -47,18 +52,24 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         double b;
-        if (INIT) { b = V.r[i]; V.u1[i] = b; } else b = V.u1[i];
+        if (INIT) { b = V.r[i]; V.u1[i] = b; F.e[i] = 0.f; } else b = V.u1[i];
         RowGeom g = row_geom(A, i);
         double r = row_accum<true, double, double, double>(b, A.col, val, V.x, g.off, 0, g.len);
         V.r[i] = r;
         float r32 = (float)r;
         F.r[i] = r32;
         if (INIT && METHOD != 0) F.r2[i] = r32;
-        e2 = e2 + r * r;
-        if (METHOD == 2) rz = rz + (double)r32 * (double)F.r2[i];
+        e2 = fma(r, r, e2);
+        if (METHOD == 2) rz = fma((double)r32, (double)F.r2[i], rz);
         else if (fused) {
-            float z = r32 / F.d[i];
-            rz = rz + (METHOD == 0 ? (double)r32 * (double)z : (double)z * (double)F.r2[i]);
+            float d32 = F.d[i], z = r32 / d32;
+            F.z[i] = z;
+            if (METHOD == 0) rz = fma((double)r32, (double)z, rz);
+            else {
+                float r2 = INIT ? r32 : F.r2[i];
+                F.z2[i] = r2 / d32;
+                rz = fma((double)z, (double)r2, rz);
+            }
         }
     }
     double v[2] = {e2, rz};
@@ -94,6 +105,18 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
     }
 }
 
+// x += e in binary64 and e = 0, right before a binary64 true residual.
+__global__ void __launch_bounds__(TFS_TPB) k_mx_fold(int n_chunks, Vec64 V, Vec32 F, const DevState *st)
+{
+    if (st->done || !st->need_true) return;
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        float e = F.e[i];
+        V.x[i] = V.x[i] + (double)e;
+        F.e[i] = 0.f;
+    }
+}
+
 // End of a binary32 iteration: either finish it on the recursive residual or
 // hand over to k_mx_true for a binary64 residual first.
 __device__ __forceinline__ void mx_end_iteration(DevState *st, double e2, double rz, bool fused)
@@ -120,12 +143,12 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho(int n_chunks, Vec32 F, D
         st->sweep_ns += gtimer() - st->t_sweep0;
         st->sweep_n += 1;
     }
-    double acc = 0.0;
+    float acc = 0.f;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        acc = acc + (METHOD == 0 ? dd(F.r[i]) * dd(F.z[i]) : dd(F.z[i]) * dd(F.r2[i]));
+        acc = METHOD == 0 ? fmaf(F.r[i], F.z[i], acc) : fmaf(F.z[i], F.r2[i], acc);
     }
-    double v[1] = {acc};
+    double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
 }
 
@@ -151,15 +174,15 @@ k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__
 {
     if (st->done || st->need_true) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
-    double acc = 0.0;
+    float acc = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
         float s = row_accum<false, float, float, float>(0.f, A.col, val, p, g.off, 0, g.len);
         q[i] = s;
-        acc = acc + dd(p[i]) * dd(s);
+        acc = fmaf(p[i], s, acc);
     }
-    double v[1] = {acc};
+    double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
@@ -174,16 +197,16 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
     if (st->done || st->need_true) return;
     const double alfa = st->alpha;
     const float alfa32 = (float)alfa;
-    double e2 = 0.0, rz = 0.0;
+    float e2 = 0.f, rz = 0.f;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
-        float r = F.r[i] - alfa32 * F.q[i];
+        F.e[i] = fmaf(alfa32, F.p[i], F.e[i]);
+        float r = fmaf(-alfa32, F.q[i], F.r[i]);
         F.r[i] = r;
-        e2 = e2 + dd(r) * dd(r);
-        if (FUSED) { float z = r / F.d[i]; rz = rz + dd(r) * dd(z); }
+        e2 = fmaf(r, r, e2);
+        if (FUSED) { float z = r / F.d[i]; F.z[i] = z; rz = fmaf(r, z, rz); }
     }
-    double v[2] = {e2, rz};
+    double v[2] = {(double)e2, (double)rz};
     if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
 
@@ -210,7 +233,7 @@ k_mx_spmv2_pq(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, d
 {
     if (st->done || st->need_true) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
-    double acc = 0.0;
+    float acc = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
@@ -218,9 +241,9 @@ k_mx_spmv2_pq(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, d
         row_accum2<false, float, float, float>(s1, s2, A.col, val, F.p, F.p2, g.off, 0, g.len);
         F.q[i] = s1;
         F.q2[i] = s2;
-        acc = acc + dd(F.p2[i]) * dd(s1);
+        acc = fmaf(F.p2[i], s1, acc);
     }
-    double v[1] = {acc};
+    double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
@@ -235,18 +258,23 @@ k_mx_bicg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
     if (st->done || st->need_true) return;
     const double alfa = st->alpha;
     const float alfa32 = (float)alfa;
-    double e2 = 0.0, rz = 0.0;
+    float e2 = 0.f, rz = 0.f;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
-        float r1 = F.r[i] - alfa32 * F.q[i];
-        float r2 = F.r2[i] - alfa32 * F.q2[i];
+        F.e[i] = fmaf(alfa32, F.p[i], F.e[i]);
+        float r1 = fmaf(-alfa32, F.q[i], F.r[i]);
+        float r2 = fmaf(-alfa32, F.q2[i], F.r2[i]);
         F.r[i] = r1;
         F.r2[i] = r2;
-        e2 = e2 + dd(r1) * dd(r1);
-        if (FUSED) { float z1 = r1 / F.d[i]; rz = rz + dd(z1) * dd(r2); }
+        e2 = fmaf(r1, r1, e2);
+        if (FUSED) {
+            float di = F.d[i], z1 = r1 / di;
+            F.z[i] = z1;
+            F.z2[i] = r2 / di;
+            rz = fmaf(z1, r2, rz);
+        }
     }
-    double v[2] = {e2, rz};
+    double v[2] = {(double)e2, (double)rz};
     if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
 
@@ -278,15 +306,15 @@ k_mx_spmv_v(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, dou
 {
     if (st->done || st->need_true) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
-    double acc = 0.0;
+    float acc = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
         float s = row_accum<false, float, float, float>(0.f, A.col, val, F.p2, g.off, 0, g.len);
         F.v2[i] = s;
-        acc = acc + dd(F.r2[i]) * dd(s);
+        acc = fmaf(F.r2[i], s, acc);
     }
-    double v[1] = {acc};
+    double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
@@ -318,18 +346,18 @@ k_mx_cgs_spmv_r(SellDev A, const float *__restrict__ val, Vec64 V, Vec32 F, DevS
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
     const double alfa = st->alpha;
     const float alfa32 = (float)alfa;
-    double e2 = 0.0, rr = 0.0;
+    float e2 = 0.f, rr = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        V.x[i] = V.x[i] + alfa * dd(F.p[i]);
+        F.e[i] = fmaf(alfa32, F.p[i], F.e[i]);
         RowGeom g = row_geom(A, i);
         float q2 = row_accum<false, float, float, float>(0.f, A.col, val, F.p, g.off, 0, g.len);
-        float r1 = F.r[i] - alfa32 * q2;
+        float r1 = fmaf(-alfa32, q2, F.r[i]);
         F.r[i] = r1;
-        e2 = e2 + dd(r1) * dd(r1);
-        rr = rr + dd(r1) * dd(F.r2[i]);
+        e2 = fmaf(r1, r1, e2);
+        rr = fmaf(r1, F.r2[i], rr);
     }
-    double v[2] = {e2, rr};
+    double v[2] = {(double)e2, (double)rr};
     if (grid_reduce<2>(v, part, &st->counter)) {
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
