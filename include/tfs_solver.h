@@ -162,7 +162,7 @@ int tfs_get_stats(const tfs_handle *h, tfs_stats *out);
 
 /* Level of every row (0-based levels, natural row order) of the DIC
  * dependency analysis done on the device at registration. */
-int tfs_get_levels(const tfs_handle *h, int32_t *levels);
+int tfs_get_levels(tfs_handle *h, int32_t *levels);
 
 /* Device time of one SpMV launch averaged over `reps` back-to-back launches
  * on the handle's stream (CUDA events), with values val (host, nnz), in the
@@ -175,6 +175,42 @@ const char *tfs_status_string(int status);
 
 /* Text of the last error recorded by this thread (CUDA error names etc.). */
 const char *tfs_last_error(void);
+
+/* ---- batches of independent systems -------------------------------------
+ * Many registered topologies solved together by one persistent kernel: each
+ * system is solved start to finish by one thread-block cluster, clusters take
+ * systems longest first from a device queue, and a system's result does not
+ * depend on what else is in the batch (bitwise).  CG or BiCG with no or
+ * diagonal preconditioning (the pressure and transport solves of
+ * Compute_Pressure_Fractional.f90:203 / Compute_Scalar.f90:619), in
+ * TFS_FP64 or TFS_MIXED.  Per-system arrays are indexed like `handles`.
+ * Replaces: a loop of Cg.f90:2-4 / Bicg.f90:2-4 calls, one per system. */
+typedef struct tfs_batch tfs_batch;
+
+int tfs_batch_create(int n_sys, tfs_handle *const *handles, tfs_batch **out);
+int tfs_batch_release(tfs_batch *b);
+
+/* Cluster size (1..16, power of two) and threads per CTA (128, 256, 512). */
+int tfs_batch_configure(tfs_batch *b, int cluster_size, int threads_per_cta);
+
+/* Device arrays (natural order) per system; niter/tol per system in,
+ * niter_out/ini_res/fin_res/status per system out (ini_res untouched on the
+ * ||b|| < tol exit).  Returns the first non-OK system status, or TFS_OK. */
+int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mode,
+                           const double *const *d_val, double *const *d_x,
+                           double *const *d_r1, const int32_t *niter,
+                           const double *tol, int32_t *niter_out,
+                           double *ini_res, double *fin_res, int32_t *status);
+
+/* The same with host arrays (copied through each handle's staging buffers). */
+int tfs_batch_solve(tfs_batch *b, int method, int prec, int mode,
+                    const double *const *val, double *const *x,
+                    double *const *r1, const int32_t *niter, const double *tol,
+                    int32_t *niter_out, double *ini_res, double *fin_res,
+                    int32_t *status);
+
+/* Device time (CUDA events) of the last batch solve, gather included. */
+int tfs_batch_last_ms(const tfs_batch *b, double *ms);
 
 /* ---- device and timing helpers ------------------------------------------
  * For callers without a CUDA runtime of their own (the benchmark harness, a

@@ -1,0 +1,315 @@
+// tfs_batch.cuh -- many independent systems in one persistent launch.
+//
+// Each system of a batch is solved, start to finish, by one thread-block
+// cluster (C CTAs on C SMs, 2 <= C <= 16).  Clusters take systems from a
+// queue sorted by decreasing size (longest first), so a batch of uneven
+// systems packs onto the GPU and small systems fill the gaps left by large
+// ones.  Inside a cluster every synchronisation is the hardware cluster
+// barrier, and every reduction sums one partial per CTA through distributed
+// shared memory in CTA-rank order: there are no spin-waits, and a system's
+// result depends only on (C, threads per CTA), never on which cluster ran it
+// or on what else was in the batch -- a system gives bitwise the same result
+// alone and in any mix.
+//
+// Methods: CG and BiCG (A, not A^T, on the shadow system) with no or diagonal
+// preconditioning, in binary64 (the reference's per-row arithmetic) or mixed
+// precision (binary32 iteration, binary64 reliable updates, as tfs_mixed.cuh).
+#pragma once
+#include <cooperative_groups.h>
+
+#include "tfs_kernels.cuh"
+
+namespace tfs {
+
+namespace cg = cooperative_groups;
+
+// One system of a batch (device memory, written by the host per solve).
+struct BatchSys {
+    SellDev A;
+    const double *val;        // SELL binary64 values (gathered by the kernel)
+    float *val32;             // SELL binary32 values (mixed)
+    const int *vmap;          // SELL -> CSR position
+    int nnz_pad;
+    const int *perm;          // internal -> natural row
+    Vec64 V;
+    Vec32 F;
+    const double *val_csr;    // caller's CSR values (natural order)
+    const double *b;          // caller's right-hand side (natural order)
+    double *x;                // caller's x (natural order, in/out)
+    double *r_out;            // r1 on return (natural order)
+    double tol;
+    int niter_max;
+    int prec;
+    // outputs
+    int niter_out, status, early, true_res;
+    double ini_res, fin_res;
+};
+
+struct BatchCtl {
+    unsigned int head;        // next queue position
+    unsigned int pad;
+};
+
+#define TFS_BATCH_MAX_TPB 512
+
+// Sum of NV values over the cluster: block sum, one partial per CTA in
+// shared memory, cluster barrier, every thread adds the C partials in rank
+// order.  Two partial slots alternate, so a slot is rewritten only after the
+// next barrier, by which time every reader of its previous contents is done.
+template <int NV>
+__device__ __forceinline__ void cluster_sum(double (&v)[NV], double (*s_part)[4], int &parity,
+                                            cg::cluster_group &cl)
+{
+    __shared__ double sm[NV][TFS_BATCH_MAX_TPB / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = v[k] + __shfl_down_sync(FULL, v[k], o);
+        if (lane == 0) sm[k][warp] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = sm[k][0];
+            for (int w = 1; w < nw; w++) s = s + sm[k][w];
+            s_part[parity][k] = s;
+        }
+    }
+    cl.sync();
+    const unsigned C = cl.num_blocks();
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double s = 0.0;
+        for (unsigned r = 0; r < C; r++) {
+            double(*rp)[4] = cl.map_shared_rank(s_part, r);
+            s = s + rp[parity][k];
+        }
+        v[k] = s;
+    }
+    parity ^= 1;
+}
+
+template <typename VT>
+struct BatchVecs;
+template <>
+struct BatchVecs<double> {
+    double *r, *r2, *p, *p2, *q, *q2, *z, *z2;
+    __device__ BatchVecs(const BatchSys &S)
+        : r(S.V.r), r2(S.V.r2), p(S.V.p), p2(S.V.p2), q(S.V.q), q2(S.V.q2), z(S.V.z), z2(S.V.z2) {}
+};
+template <>
+struct BatchVecs<float> {
+    float *r, *r2, *p, *p2, *q, *q2, *z, *z2;
+    __device__ BatchVecs(const BatchSys &S)
+        : r(S.F.r), r2(S.F.r2), p(S.F.p), p2(S.F.p2), q(S.F.q), q2(S.F.q2), z(S.F.z), z2(S.F.z2) {}
+};
+
+// The whole solve of one system by the calling cluster.  VT = double:
+// binary64 with the reference's per-row arithmetic; VT = float: mixed.
+template <int METHOD, typename VT>
+__device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_part)[4], int &parity)
+{
+    constexpr bool MIXED = sizeof(VT) == 4;
+    const int C = (int)cl.num_blocks();
+    const int stride = C * (int)blockDim.x;
+    const int gtid = (int)cl.block_rank() * (int)blockDim.x + (int)threadIdx.x;
+    const SellDev A = S.A;
+    const int n_int = A.n_int;
+    const Vec64 V = S.V;
+    const Vec32 F = S.F;
+    BatchVecs<VT> W(S);
+    const VT *valT;
+    if constexpr (MIXED) valT = S.val32; else valT = S.val;
+    const double tol = S.tol;
+    const int niter_max = S.niter_max;
+    const bool diag = S.prec == 1;
+
+    // b, x0 in internal order, d, ||b|| (Cg.f90:48-58).  The values were
+    // gathered into SELL order by k_batch_gather before this launch.
+    double acc[2] = {0.0, 0.0};
+    for (int i = gtid; i < n_int; i += stride) {
+        int o = __ldg(S.perm + i);
+        double bi = 0.0, xi = 0.0;
+        if (o >= 0) { bi = S.b[o]; xi = S.x[o]; }
+        V.r[i] = bi;
+        V.u1[i] = bi;
+        V.x[i] = xi;
+        acc[0] = fma(bi, bi, acc[0]);
+    }
+    for (int i = gtid; i < n_int; i += stride) {
+        RowGeom g = row_geom(A, i);
+        double di = (diag && g.len > 0) ? S.val[g.off + (g.dpos << 5)] : 1.0;
+        V.d[i] = di;
+        if (MIXED) { F.d[i] = (float)di; F.e[i] = 0.f; }
+    }
+    {
+        double v1[1] = {acc[0]};
+        cluster_sum<1>(v1, s_part, parity, cl);
+        double bnrm2 = sqrt(v1[0]);
+        if (bnrm2 < tol) {
+            // Early exit 1: x, r1 untouched, ini_res untouched (Cg.f90:55-58).
+            if (cl.block_rank() == 0 && threadIdx.x == 0) {
+                S.niter_out = 0; S.early = 1; S.fin_res = bnrm2; S.status = TFS_OK; S.true_res = 0;
+            }
+            return;
+        }
+    }
+    // True residual r = b - A x; r2 = r (shadow); z = M^-1 r; ||r0||; rho.
+    auto true_residual = [&](bool init, double &e2, double &rz) {
+        e2 = 0.0;
+        rz = 0.0;
+        for (int i = gtid; i < n_int; i += stride) {
+            RowGeom g = row_geom(A, i);
+            double r = row_accum<true, double, double, double>(V.u1[i], A.col, S.val, V.x, g.off, 0, g.len);
+            V.r[i] = r;
+            e2 = fma(r, r, e2);
+            VT rT = (VT)r, dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
+            if (MIXED) W.r[i] = rT;
+            VT z = rT / dT;
+            W.z[i] = z;
+            if (METHOD == 1) {
+                // The shadow residual equals r1 (see k_mx_true): reset both.
+                W.r2[i] = rT;
+                W.z2[i] = z;
+                rz = fma((double)z, (double)rT, rz);
+            } else {
+                rz = fma((double)rT, (double)z, rz);
+            }
+        }
+    };
+    double e2, rz;
+    true_residual(true, e2, rz);
+    double v2[2] = {e2, rz};
+    cluster_sum<2>(v2, s_part, parity, cl);
+    double err = sqrt(v2[0]);
+    double ini = err, rho = v2[1], rho_old = 0.0, r_true = err;
+    int true_res = 1, status = TFS_OK, niter_out = 0, early = 0;
+    int iter = 1;
+    bool done = false;
+    if (!(err <= DBL_MAX)) { status = TFS_ERR_NONFINITE; niter_out = (niter_max > 0 ? niter_max : 0) + 1; done = true; }
+    else if (err < tol) { niter_out = 0; early = 2; done = true; }
+    else if (niter_max <= 0) { niter_out = 1; done = true; }
+
+    while (!done) {
+        // p = z + beta p (Cg.f90:114-123; both directions for BiCG).
+        const double beta = iter == 1 ? 0.0 : rho / rho_old;
+        const VT betaT = (VT)beta;
+        for (int i = gtid; i < n_int; i += stride) {
+            VT z = W.z[i];
+            W.p[i] = iter == 1 ? z : z + betaT * W.p[i];
+            if (METHOD == 1) { VT z2 = W.z2[i]; W.p2[i] = iter == 1 ? z2 : z2 + betaT * W.p2[i]; }
+        }
+        cl.sync();
+        // q = A p and alpha (Cg.f90:128-153 / Bicg.f90:136-165).
+        double pq = 0.0;
+        for (int i = gtid; i < n_int; i += stride) {
+            RowGeom g = row_geom(A, i);
+            if (METHOD == 1) {
+                VT s1 = (VT)0, s2 = (VT)0;
+                row_accum2<false, VT, VT, VT>(s1, s2, A.col, valT, W.p, W.p2, g.off, 0, g.len);
+                W.q[i] = s1;
+                W.q2[i] = s2;
+                pq = fma((double)W.p2[i], (double)s1, pq);
+            } else {
+                VT s = row_accum<false, VT, VT, VT>((VT)0, A.col, valT, W.p, g.off, 0, g.len);
+                W.q[i] = s;
+                pq = fma((double)W.p[i], (double)s, pq);
+            }
+        }
+        double v1[1] = {pq};
+        cluster_sum<1>(v1, s_part, parity, cl);
+        const double alfa = rho / v1[0];
+        const VT alfaT = (VT)alfa;
+        // x (or e) += alpha p, r -= alpha q, z = M^-1 r, ||r||, next rho.
+        e2 = 0.0;
+        rz = 0.0;
+        for (int i = gtid; i < n_int; i += stride) {
+            if (MIXED) F.e[i] = fmaf((float)alfaT, (float)W.p[i], F.e[i]);
+            else V.x[i] = V.x[i] + alfa * (double)W.p[i];
+            VT r1 = W.r[i] - alfaT * W.q[i];
+            W.r[i] = r1;
+            VT dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
+            VT z1 = r1 / dT;
+            W.z[i] = z1;
+            e2 = fma((double)r1, (double)r1, e2);
+            if (METHOD == 1) {
+                VT r2 = W.r2[i] - alfaT * W.q2[i];
+                W.r2[i] = r2;
+                W.z2[i] = r2 / dT;
+                rz = fma((double)z1, (double)r2, rz);
+            } else {
+                rz = fma((double)r1, (double)z1, rz);
+            }
+        }
+        double v3[2] = {e2, rz};
+        cluster_sum<2>(v3, s_part, parity, cl);
+        double est = sqrt(v3[0]);
+        double rho_next = v3[1];
+        bool need_true = MIXED && (!(est <= DBL_MAX) || est < tol || est < 0.1 * r_true || iter >= niter_max);
+        if (need_true) {
+            for (int i = gtid; i < n_int; i += stride) {
+                V.x[i] = V.x[i] + (double)F.e[i];
+                F.e[i] = 0.f;
+            }
+            cl.sync();
+            true_residual(false, e2, rz);
+            double v4[2] = {e2, rz};
+            cluster_sum<2>(v4, s_part, parity, cl);
+            est = sqrt(v4[0]);
+            rho_next = v4[1];
+            r_true = est;
+            true_res++;
+        }
+        err = est;
+        if (!(err <= DBL_MAX)) { status = TFS_ERR_NONFINITE; niter_out = (niter_max > 0 ? niter_max : 0) + 1; done = true; }
+        else if (err < tol) { niter_out = iter; done = true; }
+        else if (iter >= niter_max) { niter_out = iter + 1; done = true; }
+        else { iter++; rho_old = rho; rho = rho_next; }
+    }
+    cl.sync();
+    // x and r1 back to natural order.
+    for (int i = gtid; i < n_int; i += stride) {
+        int o = __ldg(S.perm + i);
+        if (o >= 0) { S.x[o] = V.x[i]; S.r_out[o] = V.r[i]; }
+    }
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+        S.niter_out = niter_out; S.status = status; S.early = early; S.true_res = true_res;
+        S.ini_res = ini; S.fin_res = err;
+    }
+}
+
+// SELL values of every system from the callers' CSR values (blockIdx.y =
+// system), and the queue head reset for the launch that follows.
+__global__ void k_batch_gather(BatchSys *sys, BatchCtl *ctl, int mixed)
+{
+    const BatchSys &S = sys[blockIdx.y];
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) ctl->head = 0u;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S.nnz_pad; e += gridDim.x * blockDim.x) {
+        int m = __ldg(S.vmap + e);
+        double v = m >= 0 ? S.val_csr[m] : 0.0;
+        ((double *)S.val)[e] = v;
+        if (mixed) S.val32[e] = (float)v;
+    }
+}
+
+template <int METHOD, typename VT>
+__global__ void k_batch(BatchSys *sys, const int *order, int n_sys, BatchCtl *ctl)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ double s_part[2][4];
+    __shared__ int s_sys;
+    int parity = 0;
+    for (;;) {
+        if (cl.block_rank() == 0 && threadIdx.x == 0) s_sys = (int)atomicAdd(&ctl->head, 1u);
+        cl.sync();
+        const int q = *cl.map_shared_rank(&s_sys, 0);
+        cl.sync();   // every CTA has read rank 0's s_sys before it changes
+        if (q >= n_sys) break;
+        batch_solve_one<METHOD, VT>(sys[order[q]], cl, s_part, parity);
+        cl.sync();
+    }
+}
+
+}  // namespace tfs

@@ -81,6 +81,62 @@ static SellDev sell_of(const tfs_handle *h)
     return A;
 }
 
+// Kernel launch with programmatic dependent launch allowed (PDL) when pdl.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
+                             Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, ((KArgs)args)...);
+}
+
+// One kernel per large level (PDL-chained), then the tail levels in one
+// block; MODE 1 runs the tail first and the levels in descending order.
+template <typename T, int NR, int MODE>
+static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, const T *b1, const T *b2,
+                         T *o1, T *o2, const T *y1, const T *y2, int *count)
+{
+    SellDev A = sell_of(h);
+    const int L = h->n_levels, tail = h->tail_level;
+    const bool pdl = h->use_pdl != 0;
+    int first = 1;
+    auto tail_launch = [&]() -> cudaError_t {
+        if (tail >= L) return cudaSuccess;
+        (*count)++;
+        cudaError_t e = launch_ex(pdl, k_sweep_tail<T, NR, MODE>, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, o1, o2,
+                                  y1, y2, (const int *)h->d_lvl_begin, tail, L, h->st, first);
+        first = 0;
+        return e;
+    };
+    if (MODE == 1) {
+        cudaError_t e = tail_launch();
+        if (e != cudaSuccess) return tfs_engine_error(e, "tail launch");
+    }
+    for (int q = 0; q < tail; q++) {
+        const int l = MODE == 1 ? tail - 1 - q : q;
+        const int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
+        cudaError_t e = launch_ex(pdl, k_sweep_level<T, NR, MODE>, (r1 - r0 + TFS_TPB - 1) / TFS_TPB, TFS_TPB, s,
+                                  A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        if (e != cudaSuccess) return tfs_engine_error(e, "level launch");
+        first = 0;
+        (*count)++;
+    }
+    if (MODE != 1) {
+        cudaError_t e = tail_launch();
+        if (e != cudaSuccess) return tfs_engine_error(e, "tail launch");
+    }
+    return TFS_OK;
+}
+
 static TileTable tile_table(const tfs_handle *h)
 {
     TileTable t;
@@ -245,35 +301,124 @@ static int compute_levels(tfs_handle *h, const std::vector<int> &lrow, const std
     return TFS_OK;
 }
 
-static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1, const int32_t *dia1)
+// Reverse Cuthill-McKee order of the (structurally symmetrised) pattern: BFS
+// from a pseudo-peripheral row of each connected component, neighbours by
+// increasing degree, the whole order reversed.  rcm_pos[row] = position.
+// Keeping rows that are close in the mesh close in memory lets the 32 lanes
+// of a warp gather from shared 32-byte sectors: with the random cell numbers
+// of the workloads this cuts the gathered sectors per SpMV about 2.4x inside
+// a DIC level and about 8x without levels (measured on the 64^3 system).
+static void rcm_order(int n, const std::vector<int> &row0, const std::vector<int> &col0,
+                      std::vector<int> &rcm_pos)
+{
+    std::vector<int> deg(n);
+    for (int i = 0; i < n; i++) deg[i] = row0[i + 1] - row0[i];
+    std::vector<int> order;
+    order.reserve(n);
+    std::vector<char> seen(n, 0);
+    std::vector<int> nb;
+    auto bfs = [&](int start, std::vector<int> &out, std::vector<int> *depth) {
+        size_t head = out.size();
+        out.push_back(start);
+        seen[start] = 1;
+        if (depth) (*depth)[start] = 0;
+        while (head < out.size()) {
+            int u = out[head++];
+            nb.clear();
+            for (int j = row0[u]; j < row0[u + 1]; j++) {
+                int v = col0[j];
+                if (!seen[v]) { seen[v] = 1; nb.push_back(v); }
+            }
+            std::sort(nb.begin(), nb.end(), [&](int a, int c) { return deg[a] != deg[c] ? deg[a] < deg[c] : a < c; });
+            for (int v : nb) {
+                if (depth) (*depth)[v] = (*depth)[u] + 1;
+                out.push_back(v);
+            }
+        }
+    };
+    std::vector<int> comp, depth(n, 0);
+    for (int s0 = 0; s0 < n; s0++) {
+        if (seen[s0]) continue;
+        // Pseudo-peripheral start: two BFS sweeps from s0.
+        comp.clear();
+        bfs(s0, comp, &depth);
+        int far = comp.back();
+        for (int v : comp) seen[v] = 0;
+        comp.clear();
+        bfs(far, comp, &depth);
+        int far2 = comp.back();
+        for (int v : comp) seen[v] = 0;
+        size_t before = order.size();
+        bfs(far2, order, nullptr);
+        std::reverse(order.begin() + (long)before, order.end());
+    }
+    rcm_pos.assign(n, 0);
+    for (int k = 0; k < n; k++) rcm_pos[order[k]] = k;
+}
+
+static void free_layout(tfs_handle *h)
+{
+    for (auto &kv : h->graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    h->graphs.clear();
+    void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
+                    h->tiles, h->d_lvl_begin, h->d_lvl_tiles, h->lvl_cnt, h->vec_pool, h->vec32_pool,
+                    h->part};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    h->perm = h->iperm = h->slice_off = h->col = h->vmap = nullptr;
+    h->rowinfo = nullptr;
+    h->val = nullptr;
+    h->val32 = nullptr;
+    h->tiles = nullptr;
+    h->d_lvl_begin = h->d_lvl_tiles = nullptr;
+    h->lvl_cnt = nullptr;
+    h->vec_pool = h->vec32_pool = nullptr;
+    h->part = nullptr;
+    h->device_bytes = h->fixed_bytes;
+    h->layout = -1;
+}
+
+// Device layout in one of two row orders: TFS_LAYOUT_RCM (reverse
+// Cuthill-McKee) for solves without DIC, TFS_LAYOUT_LEVELS (DIC level, then
+// RCM position inside a level) which every preconditioner can use.
+static int build_layout(tfs_handle *h, int kind)
 {
     const int n = h->n, nnz = h->nnz;
-    std::vector<int> row0(n + 1), col0((size_t)nnz), dia0(n);
-    for (int i = 0; i <= n; i++) row0[i] = row1[i] - 1;
-    for (int j = 0; j < nnz; j++) col0[j] = col1[j] - 1;
-    for (int i = 0; i < n; i++) dia0[i] = dia1[i] - 1;
-
-    std::vector<int32_t> level;
-    std::vector<int> lrow, lcol;
-    dependency_lists(n, row0, col0, dia0, lrow, lcol);
-    int rc = compute_levels(h, lrow, lcol, level);
-    if (rc) return rc;
-    int nl = 0;
-    for (int i = 0; i < n; i++) {
-        if (level[i] < 0 || level[i] >= n) { tfs_set_error_text("level analysis failed"); return TFS_ERR_CUDA; }
-        if (level[i] + 1 > nl) nl = level[i] + 1;
+    const std::vector<int> &row0 = h->row0, &col0 = h->col0, &dia0 = h->dia0;
+    CK(cudaStreamSynchronize(h->stream));
+    free_layout(h);
+    int rc;
+    int nl = 1;
+    std::vector<int32_t> level(n, 0);
+    if (kind == TFS_LAYOUT_LEVELS) {
+        std::vector<int> lrow, lcol;
+        dependency_lists(n, row0, col0, dia0, lrow, lcol);
+        if ((rc = compute_levels(h, lrow, lcol, level))) return rc;
+        nl = 0;
+        for (int i = 0; i < n; i++) {
+            if (level[i] < 0 || level[i] >= n) { tfs_set_error_text("level analysis failed"); return TFS_ERR_CUDA; }
+            if (level[i] + 1 > nl) nl = level[i] + 1;
+        }
+        h->levels_nat.assign(level.begin(), level.end());
     }
-    // Bucket rows by level (stable), each level padded to a multiple of 32.
+    // Rows by (level, RCM position); each level padded to a multiple of 32.
+    std::vector<int> byrcm(n);
+    for (int i = 0; i < n; i++) byrcm[h->rcm_pos[i]] = i;
     std::vector<int> cnt(nl, 0);
     for (int i = 0; i < n; i++) cnt[level[i]]++;
     h->lvl_begin.assign(nl + 1, 0);
     for (int l = 0; l < nl; l++) h->lvl_begin[l + 1] = h->lvl_begin[l] + ((cnt[l] + 31) & ~31);
-    int64_t n_int64 = ((int64_t)h->lvl_begin[nl] + TFS_TPB - 1) / TFS_TPB * TFS_TPB;
+    const int quad = 4 * TFS_TPB;
+    int64_t n_int64 = ((int64_t)h->lvl_begin[nl] + quad - 1) / quad * quad;
     if (n_int64 > INT32_MAX / 2) { tfs_set_error_text("matrix too large"); return TFS_ERR_ARG; }
     const int n_int = (int)n_int64;
     std::vector<int> perm(n_int, -1), iperm(n), fillp(nl);
     for (int l = 0; l < nl; l++) fillp[l] = h->lvl_begin[l];
-    for (int i = 0; i < n; i++) {
+    for (int k = 0; k < n; k++) {
+        int i = byrcm[k];
         int p = fillp[level[i]]++;
         perm[p] = i;
         iperm[i] = p;
@@ -314,7 +459,6 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     h->n_slices = n_slices;
     h->nnz_pad = nnz_pad;
     h->n_levels = nl;
-    h->levels_nat.assign(level.begin(), level.end());
     int g = h->sm_count * 8;
     h->grid = h->n_chunks < g ? h->n_chunks : g;
     if (h->grid < 1) h->grid = 1;
@@ -323,12 +467,8 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
         (rc = dalloc(h, &h->rowinfo, n_int)) || (rc = dalloc(h, &h->slice_off, n_slices + 1)) ||
         (rc = dalloc(h, &h->col, nnz_pad)) || (rc = dalloc(h, &h->vmap, nnz_pad)) ||
         (rc = dalloc(h, &h->val, nnz_pad)) || (rc = dalloc(h, &h->val32, nnz_pad)) ||
-        (rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
-        (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)) ||
-        (rc = dalloc(h, &h->st, 1)) || (rc = dalloc(h, &h->params, 1)) ||
-        (rc = dalloc(h, &h->ctl, 1)))
+        (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)))
         return rc;
-    CK(cudaMemsetAsync(h->ctl, 0, sizeof(SweepCtl), h->stream));
     {
         // Sweep work items: tiles of at most TFS_SWEEP_TPB rows inside one
         // level, then one item for the tail (the levels after the last level
@@ -356,16 +496,13 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
         CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_begin.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->d_lvl_tiles, lvl_tiles.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemsetAsync(h->lvl_cnt, 0, sizeof(unsigned long long) * 3 * (size_t)nl, h->stream));
+        CK(cudaMemsetAsync(h->ctl, 0, sizeof(SweepCtl), h->stream));
         int occ = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_lv<double, 2, 0>, TFS_SWEEP_TPB, 0));
         if (occ < 1) occ = 1;
         int gs = h->sm_count * occ;
         h->sweep_grid = h->n_tiles < gs ? h->n_tiles : gs;
         if (h->sweep_grid < 1) h->sweep_grid = 1;
-        const char *env = getenv("TFS_SWEEP");
-        if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
-        env = getenv("TFS_GRAPH");
-        if (env && strcmp(env, "0") == 0) h->eager = 1;
     }
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
@@ -376,7 +513,6 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     CK(cudaMemsetAsync(h->val, 0, sizeof(double) * (size_t)nnz_pad, h->stream));
     CK(cudaMemsetAsync(h->val32, 0, sizeof(float) * (size_t)nnz_pad, h->stream));
     CK(cudaMemsetAsync(h->part, 0, sizeof(double) * (TFS_NPART * (size_t)h->grid + 64), h->stream));
-    CK(cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream));
 
     // Work vectors: 16 binary64 + 16 binary32, zero so padding rows stay zero.
     const size_t nv64 = 16, nv32 = 16;
@@ -395,7 +531,20 @@ static int build_layout(tfs_handle *h, const int32_t *row1, const int32_t *col1,
     for (size_t k = 0; k < nv32; k++) f[k] = pool32 + k * (size_t)n_int;
     h->f = Vec32{f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10], f[11], f[12], f[13], f[14], f[15]};
     CK(cudaStreamSynchronize(h->stream));
+    h->layout = kind;
+    h->stats.n_levels = h->n_levels;
+    h->stats.device_bytes = h->device_bytes;
     return TFS_OK;
+}
+
+// The layout a solve with preconditioner `prec` needs: a level layout serves
+// every preconditioner; DIC needs one.  Built on first use.
+static int ensure_layout(tfs_handle *h, int prec)
+{
+    if (h->layout == TFS_LAYOUT_LEVELS) return TFS_OK;
+    if (prec == 2 || h->layout_pref == TFS_LAYOUT_LEVELS) return build_layout(h, TFS_LAYOUT_LEVELS);
+    if (h->layout == TFS_LAYOUT_RCM) return TFS_OK;
+    return build_layout(h, TFS_LAYOUT_RCM);
 }
 
 static void free_handle(tfs_handle *h)
@@ -403,14 +552,8 @@ static void free_handle(tfs_handle *h)
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (auto &kv : h->graphs) {
-        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-    }
-    void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
-                    h->stage_val, h->stage_b, h->stage_x, h->part, h->st, h->params, h->ctl,
-                    h->lvl_cnt, h->tiles, h->d_lvl_begin, h->d_lvl_tiles,
-                    h->vec_pool, h->vec32_pool};
+    free_layout(h);
+    void *ptrs[] = {h->stage_val, h->stage_b, h->stage_x, h->st, h->params, h->ctl};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_params) cudaFreeHost(h->h_params);
@@ -451,10 +594,31 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     CKH(cudaMallocHost((void **)&h->h_params, sizeof(DevParams)));
     CKH(cudaMallocHost((void **)&h->h_state, sizeof(DevState)));
 #undef CKH
-    rc = build_layout(h, row1, col1, dia1);
-    if (rc) { free_handle(h); return rc; }
-    h->stats.n_levels = h->n_levels;
-    h->stats.device_bytes = h->device_bytes;
+    h->row0.resize(n + 1);
+    h->col0.resize((size_t)nnz);
+    h->dia0.resize(n);
+    for (int i = 0; i <= n; i++) h->row0[i] = row1[i] - 1;
+    for (int j = 0; j < nnz; j++) h->col0[j] = col1[j] - 1;
+    for (int i = 0; i < n; i++) h->dia0[i] = dia1[i] - 1;
+    rcm_order(n, h->row0, h->col0, h->rcm_pos);
+    if ((rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
+        (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->st, 1)) ||
+        (rc = dalloc(h, &h->params, 1)) || (rc = dalloc(h, &h->ctl, 1))) {
+        free_handle(h);
+        return rc;
+    }
+    h->fixed_bytes = h->device_bytes;
+    cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream);
+    const char *env = getenv("TFS_SWEEP");
+    if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
+    env = getenv("TFS_PDL");
+    if (env && strcmp(env, "0") == 0) h->use_pdl = 0;
+    env = getenv("TFS_GRAPH");
+    if (env && strcmp(env, "0") == 0) h->eager = 1;
+    env = getenv("TFS_LAYOUT");
+    if (env && strcmp(env, "levels") == 0) h->layout_pref = TFS_LAYOUT_LEVELS;
+    env = getenv("TFS_BICG");
+    if (env && strcmp(env, "literal") == 0) h->bicg_literal = 1;
     *out = h;
     return TFS_OK;
 }
@@ -487,11 +651,11 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
                                                              h->lvl_cnt, h->st);
         return 1;
     }
-    for (int l = 0; l < h->n_levels; l++) {
-        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-        k_dic_form<<<(r1 - r0 + T - 1) / T, T, 0, s>>>(A, h->val, h->v.d, r0, r1, h->st);
-    }
-    return h->n_levels;
+    int cnt = 0;
+    if (launch_levels<double, 1, 2>(h, s, h->val, h->v.d, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                    nullptr, &cnt))
+        return cnt;
+    return cnt;
 }
 
 static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int prec, cudaGraphConditionalHandle cond);
@@ -551,20 +715,14 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         CKL("sweep launch");
         return TFS_OK;
     }
-    for (int l = 0; l < h->n_levels; l++) {
-        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-        int g = (r1 - r0 + T_ - 1) / T_;
-        if (nr == 1) k_fwd<T, 1><<<g, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, r0, r1, h->st, l == 0);
-        else k_fwd<T, 2><<<g, T_, 0, s>>>(A, val, d, b1, b2, y1, y2, r0, r1, h->st, l == 0);
+    int rc;
+    if (nr == 1) {
+        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count))) return rc;
+        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count))) return rc;
+    } else {
+        if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count))) return rc;
+        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count))) return rc;
     }
-    for (int l = h->n_levels - 1; l >= 0; l--) {
-        int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-        int g = (r1 - r0 + T_ - 1) / T_;
-        if (nr == 1) k_bwd<T, 1><<<g, T_, 0, s>>>(A, val, d, y1, y2, z1, z2, r0, r1, h->st);
-        else k_bwd<T, 2><<<g, T_, 0, s>>>(A, val, d, y1, y2, z1, z2, r0, r1, h->st);
-    }
-    *count += 2 * h->n_levels;
-    CKL("sweep launch");
     return TFS_OK;
 }
 
@@ -827,6 +985,12 @@ static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
     if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
     GraphEntry ge;
     int rc = build_graph(h, method, prec, ge);
+    if (rc && h->use_pdl) {
+        // A driver that cannot keep programmatic edges inside a conditional
+        // body gets plain stream-ordered level launches instead.
+        h->use_pdl = 0;
+        rc = build_graph(h, method, prec, ge);
+    }
     if (rc) return rc;
     h->graphs[key] = ge;
     *out = &h->graphs[key];
@@ -842,8 +1006,17 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
     if (!h || !val || !x || !r1 || !niter || !ini_res || !fin_res) return TFS_ERR_ARG;
     if (method < TFS_CG || method > TFS_CGS || prec < 0 || prec > 2) return TFS_ERR_ARG;
     CK(cudaSetDevice(h->device));
+    int rc = ensure_layout(h, prec);
+    if (rc) return rc;
+    // The reference's BiCG starts its shadow residual as r1 and drives it
+    // with A, not A^T (Bicg.f90:91-93, 107-108, 136-144, 171-175): the shadow
+    // sequence equals the primary one bit for bit, rho = (z1, r2) = (r1, z1)
+    // and (p2, q1) = (p1, q1), so every iterate is exactly the CG iterate.
+    // It therefore runs through the CG kernels (half the work, same bits);
+    // TFS_BICG=literal runs the two sequences explicitly.
+    const int kmethod = (method == TFS_BICG && !h->bicg_literal) ? TFS_CG : method;
     GraphEntry *ge = nullptr;
-    int rc = get_graph(h, method, prec, &ge);
+    rc = get_graph(h, kmethod, prec, &ge);
     if (rc) return rc;
     cudaStream_t s = h->stream;
     DevParams &P = *h->h_params;
@@ -861,7 +1034,7 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
     }
     CK(cudaEventRecord(h->ev0, s));
     if (h->eager) {
-        if ((rc = run_eager(h, method, prec, ge))) return rc;
+        if ((rc = run_eager(h, kmethod, prec, ge))) return rc;
     } else {
         CK(cudaGraphLaunch(ge->exec, s));
     }
@@ -967,8 +1140,10 @@ extern "C" int tfs_cgs(int32_t n, int32_t nnz, const int32_t *row1, const int32_
 // ------------------------------------------------------ single routines
 
 // Uploads val and runs the gather with a fresh DevState (tol 0, one iteration).
-static int prepare_values(tfs_handle *h, const double *val)
+static int prepare_values(tfs_handle *h, const double *val, int prec = 0)
 {
+    int rc = ensure_layout(h, prec);
+    if (rc) return rc;
     cudaStream_t s = h->stream;
     DevParams &P = *h->h_params;
     P.tol = 0.0;
@@ -1041,7 +1216,7 @@ extern "C" int tfs_prec_form(tfs_handle *h, const double *val, int32_t prec, dou
     if (!h || !val || !d || prec < 0 || prec > 2) return TFS_ERR_ARG;
     CK(cudaSetDevice(h->device));
     int rc;
-    if ((rc = prepare_values(h, val)) || (rc = form_prec(h, prec))) return rc;
+    if ((rc = prepare_values(h, val, prec)) || (rc = form_prec(h, prec))) return rc;
     return vec_out(h, h->v.d, d);
 }
 
@@ -1050,7 +1225,7 @@ extern "C" int tfs_prec_solve(tfs_handle *h, const double *val, int32_t prec, co
     if (!h || !val || !b || !x || prec < 0 || prec > 2) return TFS_ERR_ARG;
     CK(cudaSetDevice(h->device));
     int rc;
-    if ((rc = prepare_values(h, val)) || (rc = form_prec(h, prec)) || (rc = vec_in(h, b, h->v.r))) return rc;
+    if ((rc = prepare_values(h, val, prec)) || (rc = form_prec(h, prec)) || (rc = vec_in(h, b, h->v.r))) return rc;
     if (prec == 2) {
         int cnt = 0;
         if ((rc = launch_sweeps<double>(h, h->stream, 1, h->v.r, nullptr, h->v.y, nullptr, h->v.z, nullptr, &cnt))) return rc;
@@ -1068,9 +1243,12 @@ extern "C" int tfs_get_stats(const tfs_handle *h, tfs_stats *out)
     return TFS_OK;
 }
 
-extern "C" int tfs_get_levels(const tfs_handle *h, int32_t *levels)
+extern "C" int tfs_get_levels(tfs_handle *h, int32_t *levels)
 {
     if (!h || !levels) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_layout(h, 2);
+    if (rc) return rc;
     memcpy(levels, h->levels_nat.data(), sizeof(int32_t) * (size_t)h->n);
     return TFS_OK;
 }
@@ -1171,5 +1349,228 @@ extern "C" int tfs_timer_stop(tfs_handle *h, double *ms)
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, h->tev0, h->tev1));
     *ms = (double)t;
+    return TFS_OK;
+}
+
+// ------------------------------------------------------------ batches
+
+#include "tfs_batch.cuh"
+
+struct tfs_batch {
+    int n = 0;
+    int device = 0;
+    int cluster = 8, tpb = 256;
+    std::vector<tfs_handle *> hs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    BatchSys *d_sys = nullptr, *h_sys = nullptr;
+    BatchCtl *d_ctl = nullptr;
+    int *d_order = nullptr;
+    double last_ms = 0.0;
+    int64_t launches = 0;
+};
+
+static void free_batch(tfs_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->d_sys) cudaFree(b->d_sys);
+    if (b->d_ctl) cudaFree(b->d_ctl);
+    if (b->d_order) cudaFree(b->d_order);
+    if (b->h_sys) cudaFreeHost(b->h_sys);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+extern "C" int tfs_batch_create(int n_sys, tfs_handle *const *handles, tfs_batch **out)
+{
+    if (!out || n_sys < 1 || !handles) return TFS_ERR_ARG;
+    *out = nullptr;
+    for (int k = 0; k < n_sys; k++) {
+        if (!handles[k]) return TFS_ERR_ARG;
+        CK(cudaSetDevice(handles[k]->device));
+        int rc = ensure_layout(handles[k], 1);
+        if (rc) return rc;
+    }
+    tfs_batch *b = new tfs_batch;
+    b->n = n_sys;
+    b->hs.assign(handles, handles + n_sys);
+    b->device = handles[0]->device;
+#define CKB(call)                                                              \
+    do {                                                                       \
+        cudaError_t _e = (call);                                               \
+        if (_e != cudaSuccess) { int _r = tfs_engine_error(_e, #call); free_batch(b); return _r; } \
+    } while (0)
+    CKB(cudaSetDevice(b->device));
+    CKB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CKB(cudaEventCreate(&b->ev0));
+    CKB(cudaEventCreate(&b->ev1));
+    CKB(cudaMalloc(&b->d_sys, sizeof(BatchSys) * (size_t)n_sys));
+    CKB(cudaMalloc(&b->d_ctl, sizeof(BatchCtl)));
+    CKB(cudaMalloc(&b->d_order, sizeof(int) * (size_t)n_sys));
+    CKB(cudaMallocHost(&b->h_sys, sizeof(BatchSys) * (size_t)n_sys));
+    // Longest systems first.
+    std::vector<int> order(n_sys);
+    for (int k = 0; k < n_sys; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return handles[a]->nnz > handles[c]->nnz;
+    });
+    CKB(cudaMemcpy(b->d_order, order.data(), sizeof(int) * (size_t)n_sys, cudaMemcpyHostToDevice));
+#undef CKB
+    *out = b;
+    return TFS_OK;
+}
+
+extern "C" int tfs_batch_release(tfs_batch *b)
+{
+    if (!b) return TFS_ERR_ARG;
+    free_batch(b);
+    return TFS_OK;
+}
+
+extern "C" int tfs_batch_configure(tfs_batch *b, int cluster_size, int threads_per_cta)
+{
+    if (!b || cluster_size < 1 || cluster_size > 16 || (cluster_size & (cluster_size - 1)) ||
+        (threads_per_cta != 128 && threads_per_cta != 256 && threads_per_cta != TFS_BATCH_MAX_TPB))
+        return TFS_ERR_ARG;
+    b->cluster = cluster_size;
+    b->tpb = threads_per_cta;
+    return TFS_OK;
+}
+
+template <int METHOD, typename VT>
+static int launch_batch_kernel(tfs_batch *b)
+{
+    auto kernel = k_batch<METHOD, VT>;
+    if (b->cluster > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)b->cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3((unsigned)b->tpb);
+    cfg.gridDim = dim3((unsigned)b->cluster);
+    cfg.stream = b->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n_clusters = 0;
+    CK(cudaOccupancyMaxActiveClusters(&n_clusters, kernel, &cfg));
+    if (n_clusters < 1) {
+        tfs_set_error_text("cluster configuration cannot be resident");
+        return TFS_ERR_ARG;
+    }
+    if (n_clusters > b->n) n_clusters = b->n;
+    cfg.gridDim = dim3((unsigned)(n_clusters * b->cluster));
+    CK(cudaLaunchKernelEx(&cfg, kernel, b->d_sys, (const int *)b->d_order, b->n, b->d_ctl));
+    return TFS_OK;
+}
+
+extern "C" int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mode,
+                                      const double *const *d_val, double *const *d_x,
+                                      double *const *d_r1, const int32_t *niter, const double *tol,
+                                      int32_t *niter_out, double *ini_res, double *fin_res,
+                                      int32_t *status)
+{
+    if (!b || !d_val || !d_x || !d_r1 || !niter || !tol || !niter_out || !ini_res || !fin_res || !status)
+        return TFS_ERR_ARG;
+    if ((method != TFS_CG && method != TFS_BICG) || (prec != 0 && prec != 1) ||
+        (mode != TFS_FP64 && mode != TFS_MIXED)) {
+        tfs_set_error_text("batches run CG or BiCG with no or diagonal preconditioning");
+        return TFS_ERR_ARG;
+    }
+    CK(cudaSetDevice(b->device));
+    int64_t max_nnz = 0;
+    for (int k = 0; k < b->n; k++) {
+        tfs_handle *h = b->hs[k];
+        BatchSys &S = b->h_sys[k];
+        memset(&S, 0, sizeof S);
+        S.A = sell_of(h);
+        S.val = h->val;
+        S.val32 = h->val32;
+        S.vmap = h->vmap;
+        S.nnz_pad = h->nnz_pad;
+        S.perm = h->perm;
+        S.V = h->v;
+        S.F = h->f;
+        S.val_csr = d_val[k];
+        S.b = d_r1[k];
+        S.x = d_x[k];
+        S.r_out = d_r1[k];
+        S.tol = tol[k];
+        S.niter_max = niter[k];
+        S.prec = prec;
+        if (h->nnz_pad > max_nnz) max_nnz = h->nnz_pad;
+    }
+    CK(cudaMemcpyAsync(b->d_sys, b->h_sys, sizeof(BatchSys) * (size_t)b->n, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaEventRecord(b->ev0, b->stream));
+    int gx = (int)((max_nnz + 255) / 256);
+    if (gx > 64) gx = 64;
+    if (gx < 1) gx = 1;
+    k_batch_gather<<<dim3((unsigned)gx, (unsigned)b->n), 256, 0, b->stream>>>(b->d_sys, b->d_ctl, mode == TFS_MIXED);
+    CKL("batch gather");
+    int rc;
+    // BiCG iterates equal CG's (see solve_impl): one sequence suffices.
+    const char *lit = getenv("TFS_BICG");
+    if (method == TFS_BICG && !(lit && strcmp(lit, "literal") == 0)) method = TFS_CG;
+    if (method == TFS_CG) rc = mode == TFS_MIXED ? launch_batch_kernel<0, float>(b) : launch_batch_kernel<0, double>(b);
+    else rc = mode == TFS_MIXED ? launch_batch_kernel<1, float>(b) : launch_batch_kernel<1, double>(b);
+    if (rc) return rc;
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaMemcpyAsync(b->h_sys, b->d_sys, sizeof(BatchSys) * (size_t)b->n, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->last_ms = ms;
+    b->launches = 2;
+    int worst = TFS_OK;
+    for (int k = 0; k < b->n; k++) {
+        const BatchSys &S = b->h_sys[k];
+        niter_out[k] = S.niter_out;
+        if (S.early != 1) ini_res[k] = S.ini_res;
+        fin_res[k] = S.fin_res;
+        status[k] = S.status;
+        if (S.status != TFS_OK && worst == TFS_OK) worst = S.status;
+    }
+    return worst;
+}
+
+extern "C" int tfs_batch_solve(tfs_batch *b, int method, int prec, int mode,
+                               const double *const *val, double *const *x, double *const *r1,
+                               const int32_t *niter, const double *tol, int32_t *niter_out,
+                               double *ini_res, double *fin_res, int32_t *status)
+{
+    if (!b || !val || !x || !r1) return TFS_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    std::vector<const double *> dv(b->n);
+    std::vector<double *> dx(b->n), dr(b->n);
+    for (int k = 0; k < b->n; k++) {
+        tfs_handle *h = b->hs[k];
+        CK(cudaMemcpyAsync(h->stage_val, val[k], sizeof(double) * (size_t)h->nnz, cudaMemcpyHostToDevice, b->stream));
+        CK(cudaMemcpyAsync(h->stage_b, r1[k], sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, b->stream));
+        CK(cudaMemcpyAsync(h->stage_x, x[k], sizeof(double) * (size_t)h->n, cudaMemcpyHostToDevice, b->stream));
+        dv[k] = h->stage_val;
+        dx[k] = h->stage_x;
+        dr[k] = h->stage_b;
+    }
+    int rc = tfs_batch_solve_device(b, method, prec, mode, dv.data(), dx.data(), dr.data(), niter, tol,
+                                    niter_out, ini_res, fin_res, status);
+    if (rc != TFS_OK && rc != TFS_ERR_NONFINITE) return rc;
+    for (int k = 0; k < b->n; k++) {
+        tfs_handle *h = b->hs[k];
+        CK(cudaMemcpyAsync(x[k], h->stage_x, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaMemcpyAsync(r1[k], h->stage_b, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    return rc;
+}
+
+extern "C" int tfs_batch_last_ms(const tfs_batch *b, double *ms)
+{
+    if (!b || !ms) return TFS_ERR_ARG;
+    *ms = b->last_ms;
     return TFS_OK;
 }

@@ -24,8 +24,10 @@
 #include "../../include/tfs_solver.h"
 
 #define TFS_TPB 256           // threads per block = rows per chunk
+#define TFS_LAYOUT_RCM 0      // rows in reverse Cuthill-McKee order
+#define TFS_LAYOUT_LEVELS 1   // rows by DIC level, RCM order inside a level
 #define TFS_SWEEP_TPB 1024    // threads per block = rows per tile of the level sweeps
-#define TFS_TAIL_ROWS 4096    // levels after the last one above this size form the tail
+#define TFS_TAIL_ROWS 1024    // levels after the last one above this size form the tail
 #define TFS_NPART 4           // values reduced at once, at most
 
 // Device-resident state of one solve.  Written by k_init from DevParams and
@@ -103,12 +105,19 @@ struct tfs_handle {
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int grid = 0;                      // blocks of the chunk kernels
     int sweep_grid = 0;                // blocks of the dataflow sweeps
-    int sweep_mode = 1;                // 1: dataflow single launch, 0: one launch per level
+    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch
+    int use_pdl = 1;                   // programmatic dependent launch between level kernels
     int eager = 0;                     // 1: launch kernels directly, no CUDA graph
+    int bicg_literal = 0;              // 1: BiCG runs its shadow sequence explicitly
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row
     uint64_t fingerprint = 0;
+    std::vector<int> row0, col0, dia0;  // the topology, 0-based (host copy)
+    std::vector<int> rcm_pos;          // RCM position of every natural row
+    int layout = -1;                   // TFS_LAYOUT_* built, -1 none yet
+    int layout_pref = TFS_LAYOUT_RCM;  // TFS_LAYOUT=levels forces level order
+    int64_t fixed_bytes = 0;           // device bytes independent of the layout
     // device arrays
     int *perm = nullptr, *iperm = nullptr, *slice_off = nullptr, *col = nullptr, *vmap = nullptr;
     uint32_t *rowinfo = nullptr;

@@ -152,6 +152,23 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict_
     return false;
 }
 
+// Row loops of the vector kernels: four chunks per step, with every load of
+// the four rows issued before any of them is used (memory-level parallelism;
+// the stores of one row could otherwise alias the loads of the next).
+#define TFS_QUAD_BEGIN(nch)                                                   \
+    for (int _c0 = blockIdx.x; _c0 < (nch); _c0 += 4 * (int)gridDim.x) {    \
+        int _i[4];                                                           \
+        bool _ok[4];                                                         \
+        _Pragma("unroll") for (int _q = 0; _q < 4; _q++) {                   \
+            int _c = _c0 + _q * (int)gridDim.x;                              \
+            _ok[_q] = _c < (nch);                                            \
+            _i[_q] = _ok[_q] ? _c * TFS_TPB + (int)threadIdx.x : 0;          \
+        }
+#define TFS_QLOAD(arr, ptr)                                                   \
+    _Pragma("unroll") for (int _q = 0; _q < 4; _q++) arr[_q] = (ptr)[_i[_q]];
+#define TFS_QUAD_FOR _Pragma("unroll") for (int _q = 0; _q < 4; _q++) if (_ok[_q])
+#define TFS_QUAD_END }
+
 __device__ __forceinline__ void set_cond(cudaGraphConditionalHandle cond, unsigned v)
 {
     if (cond) cudaGraphSetConditional(cond, v);
@@ -573,6 +590,93 @@ k_sweep_lv(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
     }
 }
 
+// ------------------------------------------------ one launch per level
+//
+// The default schedule: one kernel per large level, launched with
+// programmatic dependent launch (PDL).  A level kernel first reads what does
+// not depend on the previous level (row geometry and its first four column
+// indices and values), then lets the next level's kernel start
+// (cudaTriggerProgrammaticLaunchCompletion) and waits for the previous one
+// (cudaGridDependencySynchronize), so launch latency and prefetch overlap the
+// previous level.  The small trailing levels run in one single-block kernel
+// (k_sweep_tail) with __syncthreads() between levels.
+template <typename T, int NR, int MODE>
+__global__ void __launch_bounds__(TFS_TPB)
+k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
+              T *o2, const T *y1, const T *y2, int row0, int row1, DevState *st, int first)
+{
+    const int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
+    const bool active = i < row1;
+    RowGeom g{0, 0, 0};
+    int kk[4] = {0, 0, 0, 0};
+    T aa[4] = {(T)0, (T)0, (T)0, (T)0};
+    if (active) {
+        g = row_geom(A, i);
+        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (j0 + q < j1) {
+                int ee = g.off + ((j0 + q) << 5);
+                kk[q] = __ldg(A.col + ee);
+                aa[q] = __ldg(val + ee);
+            }
+    }
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    if (st->done) return;
+    if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa);
+}
+
+// Levels [l_begin, l_end) of a sweep in one block (descending for MODE 1);
+// every level has at most TFS_SWEEP_TPB rows, one row per thread.  While a
+// level is computed, the row geometry and the first entries of the thread's
+// row of the next level are already being loaded, so each level costs little
+// more than its dependent gathers and a __syncthreads().
+template <typename T, int NR, int MODE>
+__global__ void __launch_bounds__(TFS_SWEEP_TPB)
+k_sweep_tail(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
+             T *o2, const T *y1, const T *y2, const int *__restrict__ lvl_begin, int l_begin,
+             int l_end, DevState *st, int first)
+{
+    const int nl = l_end - l_begin;
+    auto level_of = [&](int q) { return MODE == 1 ? l_end - 1 - q : l_begin + q; };
+    auto fetch = [&](int q, int &i, RowGeom &g, int (&kk)[4], T (&aa)[4]) {
+        const int lev = level_of(q);
+        i = __ldg(lvl_begin + lev) + (int)threadIdx.x;
+        const int r1 = __ldg(lvl_begin + lev + 1);
+        g = RowGeom{0, 0, 0};
+        if (i >= r1) { i = -1; return; }
+        g = row_geom(A, i);
+        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+#pragma unroll
+        for (int q2 = 0; q2 < 4; q2++)
+            if (j0 + q2 < j1) {
+                int ee = g.off + ((j0 + q2) << 5);
+                kk[q2] = __ldg(A.col + ee);
+                aa[q2] = __ldg(val + ee);
+            }
+    };
+    int i = -1, ni = -1;
+    RowGeom g, ng;
+    int kk[4] = {0, 0, 0, 0}, nkk[4] = {0, 0, 0, 0};
+    T aa[4] = {(T)0, (T)0, (T)0, (T)0}, naa[4] = {(T)0, (T)0, (T)0, (T)0};
+    if (nl > 0) fetch(0, i, g, kk, aa);
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    if (st->done) return;
+    if (MODE == 0 && first && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    for (int q = 0; q < nl; q++) {
+        if (q + 1 < nl) fetch(q + 1, ni, ng, nkk, naa);
+        if (i >= 0) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa);
+        __syncthreads();
+        i = ni;
+        g = ng;
+#pragma unroll
+        for (int q2 = 0; q2 < 4; q2++) { kk[q2] = nkk[q2]; aa[q2] = naa[q2]; }
+    }
+}
+
 // rho after the sweeps: CG (r, z) (Cg.f90:108-112); BiCG (z1, r2) (Bicg.f90:113-117).
 template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)
@@ -584,10 +688,12 @@ k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
         st->sweep_n += 1;
     }
     double acc = 0.0;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        acc = METHOD == 0 ? fma(V.r[i], V.z[i], acc) : fma(V.z[i], V.r2[i], acc);
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        double a[4], b[4];
+        TFS_QLOAD(a, METHOD == 0 ? V.r : V.z);
+        TFS_QLOAD(b, METHOD == 0 ? V.z : V.r2);
+        TFS_QUAD_FOR acc = fma(a[_q], b[_q], acc);
+    TFS_QUAD_END
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
 }
@@ -602,11 +708,13 @@ __global__ void __launch_bounds__(TFS_TPB) k_cg_p(int n_chunks, Vec64 V, const D
     if (st->done) return;
     const int it = st->iter;
     const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        double z = FROMZ ? V.z[i] : V.r[i] / V.d[i];
-        V.p[i] = it == 1 ? z : z + beta * V.p[i];
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        double z[4], p[4];
+        if (FROMZ) { TFS_QLOAD(z, V.z); }
+        else { double r[4], d[4]; TFS_QLOAD(r, V.r); TFS_QLOAD(d, V.d); TFS_QUAD_FOR z[_q] = r[_q] / d[_q]; }
+        TFS_QLOAD(p, V.p);
+        TFS_QUAD_FOR V.p[_i[_q]] = it == 1 ? z[_q] : z[_q] + beta * p[_q];
+    TFS_QUAD_END
 }
 
 // q = A p (Cg.f90:128-134) fused with (p, q) and alpha = rho / (p, q)
@@ -645,14 +753,19 @@ k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditio
     }
     const double alfa = st->alpha;
     double e2 = 0.0, rz = 0.0;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        V.x[i] = V.x[i] + alfa * V.p[i];
-        double r = V.r[i] - alfa * V.q[i];
-        V.r[i] = r;
-        e2 = fma(r, r, e2);
-        if (FUSED) { double z = r / V.d[i]; V.z[i] = z; rz = fma(r, z, rz); }
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        double x[4], p[4], r[4], q[4], d[4];
+        TFS_QLOAD(x, V.x); TFS_QLOAD(p, V.p); TFS_QLOAD(r, V.r); TFS_QLOAD(q, V.q);
+        if (FUSED) { TFS_QLOAD(d, V.d); }
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            V.x[i] = x[_q] + alfa * p[_q];
+            double rn = r[_q] - alfa * q[_q];
+            V.r[i] = rn;
+            e2 = fma(rn, rn, e2);
+            if (FUSED) { double z = rn / d[_q]; V.z[i] = z; rz = fma(rn, z, rz); }
+        }
+    TFS_QUAD_END
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
 }
@@ -665,14 +778,21 @@ __global__ void __launch_bounds__(TFS_TPB) k_bicg_p(int n_chunks, Vec64 V, const
     if (st->done) return;
     const int it = st->iter;
     const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        double z1, z2;
-        if (FROMZ) { z1 = V.z[i]; z2 = V.z2[i]; }
-        else { double di = V.d[i]; z1 = V.r[i] / di; z2 = V.r2[i] / di; }
-        if (it == 1) { V.p[i] = z1; V.p2[i] = z2; }
-        else { V.p[i] = z1 + beta * V.p[i]; V.p2[i] = z2 + beta * V.p2[i]; }
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        double z1[4], z2[4], p1[4], p2[4];
+        if (FROMZ) { TFS_QLOAD(z1, V.z); TFS_QLOAD(z2, V.z2); }
+        else {
+            double r1[4], r2[4], d[4];
+            TFS_QLOAD(r1, V.r); TFS_QLOAD(r2, V.r2); TFS_QLOAD(d, V.d);
+            TFS_QUAD_FOR { z1[_q] = r1[_q] / d[_q]; z2[_q] = r2[_q] / d[_q]; }
+        }
+        TFS_QLOAD(p1, V.p); TFS_QLOAD(p2, V.p2);
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            if (it == 1) { V.p[i] = z1[_q]; V.p2[i] = z2[_q]; }
+            else { V.p[i] = z1[_q] + beta * p1[_q]; V.p2[i] = z2[_q] + beta * p2[_q]; }
+        }
+    TFS_QUAD_END
 }
 
 // q1 = A p1 and q2 = A p2 in one pass over A (Bicg.f90:136-144), fused with
@@ -712,21 +832,27 @@ k_bicg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphCondit
     }
     const double alfa = st->alpha;
     double e2 = 0.0, rz = 0.0;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        V.x[i] = V.x[i] + alfa * V.p[i];
-        double r1 = V.r[i] - alfa * V.q[i];
-        double r2 = V.r2[i] - alfa * V.q2[i];
-        V.r[i] = r1;
-        V.r2[i] = r2;
-        e2 = fma(r1, r1, e2);
-        if (FUSED) {
-            double di = V.d[i], z1 = r1 / di;
-            V.z[i] = z1;
-            V.z2[i] = r2 / di;
-            rz = fma(z1, r2, rz);
+    TFS_QUAD_BEGIN(n_chunks)
+        double x[4], p[4], r1[4], q1[4], r2[4], q2[4], d[4];
+        TFS_QLOAD(x, V.x); TFS_QLOAD(p, V.p); TFS_QLOAD(r1, V.r); TFS_QLOAD(q1, V.q);
+        TFS_QLOAD(r2, V.r2); TFS_QLOAD(q2, V.q2);
+        if (FUSED) { TFS_QLOAD(d, V.d); }
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            V.x[i] = x[_q] + alfa * p[_q];
+            double a1 = r1[_q] - alfa * q1[_q];
+            double a2 = r2[_q] - alfa * q2[_q];
+            V.r[i] = a1;
+            V.r2[i] = a2;
+            e2 = fma(a1, a1, e2);
+            if (FUSED) {
+                double z1 = a1 / d[_q];
+                V.z[i] = z1;
+                V.z2[i] = a2 / d[_q];
+                rz = fma(z1, a2, rz);
+            }
         }
-    }
+    TFS_QUAD_END
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
 }

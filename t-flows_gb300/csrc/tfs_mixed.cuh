@@ -58,7 +58,10 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
         V.r[i] = r;
         float r32 = (float)r;
         F.r[i] = r32;
-        if (INIT && METHOD != 0) F.r2[i] = r32;
+        // The shadow residual of the reference's BiCG equals r1 at every step
+        // (it starts as r1 and is driven by A, not A^T), so a reliable update
+        // resets it together with r1; CGS keeps its initial shadow.
+        if (METHOD == 1 || (INIT && METHOD == 2)) F.r2[i] = r32;
         e2 = fma(r, r, e2);
         if (METHOD == 2) rz = fma((double)r32, (double)F.r2[i], rz);
         else if (fused) {
@@ -66,9 +69,8 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
             F.z[i] = z;
             if (METHOD == 0) rz = fma((double)r32, (double)z, rz);
             else {
-                float r2 = INIT ? r32 : F.r2[i];
-                F.z2[i] = r2 / d32;
-                rz = fma((double)z, (double)r2, rz);
+                F.z2[i] = z;
+                rz = fma((double)z, (double)r32, rz);
             }
         }
     }
@@ -109,12 +111,12 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_fold(int n_chunks, Vec64 V, Vec32 F, const DevState *st)
 {
     if (st->done || !st->need_true) return;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        float e = F.e[i];
-        V.x[i] = V.x[i] + (double)e;
-        F.e[i] = 0.f;
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        float e[4];
+        double x[4];
+        TFS_QLOAD(e, F.e); TFS_QLOAD(x, V.x);
+        TFS_QUAD_FOR { V.x[_i[_q]] = x[_q] + (double)e[_q]; F.e[_i[_q]] = 0.f; }
+    TFS_QUAD_END
 }
 
 // End of a binary32 iteration: either finish it on the recursive residual or
@@ -144,10 +146,12 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho(int n_chunks, Vec32 F, D
         st->sweep_n += 1;
     }
     float acc = 0.f;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        acc = METHOD == 0 ? fmaf(F.r[i], F.z[i], acc) : fmaf(F.z[i], F.r2[i], acc);
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        float a[4], b[4];
+        TFS_QLOAD(a, METHOD == 0 ? F.r : F.z);
+        TFS_QLOAD(b, METHOD == 0 ? F.z : F.r2);
+        TFS_QUAD_FOR acc = fmaf(a[_q], b[_q], acc);
+    TFS_QUAD_END
     double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
 }
@@ -160,11 +164,13 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p(int n_chunks, Vec32 F, cons
     if (st->done || st->need_true) return;
     const int it = st->iter;
     const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        float z = FROMZ ? F.z[i] : F.r[i] / F.d[i];
-        F.p[i] = it == 1 ? z : z + beta * F.p[i];
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        float z[4], p[4];
+        if (FROMZ) { TFS_QLOAD(z, F.z); }
+        else { float r[4], d[4]; TFS_QLOAD(r, F.r); TFS_QLOAD(d, F.d); TFS_QUAD_FOR z[_q] = r[_q] / d[_q]; }
+        TFS_QLOAD(p, F.p);
+        TFS_QUAD_FOR F.p[_i[_q]] = it == 1 ? z[_q] : fmaf(beta, p[_q], z[_q]);
+    TFS_QUAD_END
 }
 
 // q = A p in binary32 with (p, q) in binary64 and alpha.
@@ -198,14 +204,19 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
     const double alfa = st->alpha;
     const float alfa32 = (float)alfa;
     float e2 = 0.f, rz = 0.f;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        F.e[i] = fmaf(alfa32, F.p[i], F.e[i]);
-        float r = fmaf(-alfa32, F.q[i], F.r[i]);
-        F.r[i] = r;
-        e2 = fmaf(r, r, e2);
-        if (FUSED) { float z = r / F.d[i]; F.z[i] = z; rz = fmaf(r, z, rz); }
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        float e[4], p[4], r[4], q[4], d[4];
+        TFS_QLOAD(e, F.e); TFS_QLOAD(p, F.p); TFS_QLOAD(r, F.r); TFS_QLOAD(q, F.q);
+        if (FUSED) { TFS_QLOAD(d, F.d); }
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            F.e[i] = fmaf(alfa32, p[_q], e[_q]);
+            float rn = fmaf(-alfa32, q[_q], r[_q]);
+            F.r[i] = rn;
+            e2 = fmaf(rn, rn, e2);
+            if (FUSED) { float z = rn / d[_q]; F.z[i] = z; rz = fmaf(rn, z, rz); }
+        }
+    TFS_QUAD_END
     double v[2] = {(double)e2, (double)rz};
     if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
@@ -218,14 +229,21 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_bicg_p(int n_chunks, Vec32 F, co
     if (st->done || st->need_true) return;
     const int it = st->iter;
     const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        float z1, z2;
-        if (FROMZ) { z1 = F.z[i]; z2 = F.z2[i]; }
-        else { float di = F.d[i]; z1 = F.r[i] / di; z2 = F.r2[i] / di; }
-        if (it == 1) { F.p[i] = z1; F.p2[i] = z2; }
-        else { F.p[i] = z1 + beta * F.p[i]; F.p2[i] = z2 + beta * F.p2[i]; }
-    }
+    TFS_QUAD_BEGIN(n_chunks)
+        float z1[4], z2[4], p1[4], p2[4];
+        if (FROMZ) { TFS_QLOAD(z1, F.z); TFS_QLOAD(z2, F.z2); }
+        else {
+            float r1[4], r2[4], d[4];
+            TFS_QLOAD(r1, F.r); TFS_QLOAD(r2, F.r2); TFS_QLOAD(d, F.d);
+            TFS_QUAD_FOR { z1[_q] = r1[_q] / d[_q]; z2[_q] = r2[_q] / d[_q]; }
+        }
+        TFS_QLOAD(p1, F.p); TFS_QLOAD(p2, F.p2);
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            if (it == 1) { F.p[i] = z1[_q]; F.p2[i] = z2[_q]; }
+            else { F.p[i] = fmaf(beta, p1[_q], z1[_q]); F.p2[i] = fmaf(beta, p2[_q], z2[_q]); }
+        }
+    TFS_QUAD_END
 }
 
 __global__ void __launch_bounds__(TFS_TPB)
@@ -259,21 +277,27 @@ k_mx_bicg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
     const double alfa = st->alpha;
     const float alfa32 = (float)alfa;
     float e2 = 0.f, rz = 0.f;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        int i = c * TFS_TPB + threadIdx.x;
-        F.e[i] = fmaf(alfa32, F.p[i], F.e[i]);
-        float r1 = fmaf(-alfa32, F.q[i], F.r[i]);
-        float r2 = fmaf(-alfa32, F.q2[i], F.r2[i]);
-        F.r[i] = r1;
-        F.r2[i] = r2;
-        e2 = fmaf(r1, r1, e2);
-        if (FUSED) {
-            float di = F.d[i], z1 = r1 / di;
-            F.z[i] = z1;
-            F.z2[i] = r2 / di;
-            rz = fmaf(z1, r2, rz);
+    TFS_QUAD_BEGIN(n_chunks)
+        float e[4], p[4], r1[4], q1[4], r2[4], q2[4], d[4];
+        TFS_QLOAD(e, F.e); TFS_QLOAD(p, F.p); TFS_QLOAD(r1, F.r); TFS_QLOAD(q1, F.q);
+        TFS_QLOAD(r2, F.r2); TFS_QLOAD(q2, F.q2);
+        if (FUSED) { TFS_QLOAD(d, F.d); }
+        TFS_QUAD_FOR {
+            const int i = _i[_q];
+            F.e[i] = fmaf(alfa32, p[_q], e[_q]);
+            float a1 = fmaf(-alfa32, q1[_q], r1[_q]);
+            float a2 = fmaf(-alfa32, q2[_q], r2[_q]);
+            F.r[i] = a1;
+            F.r2[i] = a2;
+            e2 = fmaf(a1, a1, e2);
+            if (FUSED) {
+                float z1 = a1 / d[_q];
+                F.z[i] = z1;
+                F.z2[i] = a2 / d[_q];
+                rz = fmaf(z1, a2, rz);
+            }
         }
-    }
+    TFS_QUAD_END
     double v[2] = {(double)e2, (double)rz};
     if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }

@@ -10,10 +10,11 @@ from .lib import (TFS_OK, TFS_CG, TFS_BICG, TFS_CGS, TFS_PREC_NONE, TFS_PREC_DIA
 from .matrix_mod import Matrix_Type, Matrix_Mod_Topology
 from .solvers_mod import Cg, Bicg, Cgs, Prec_Form, Prec_Solve, Residual, Solver, spmv
 from .synth import SynthSystem
+from .batch import Batch
 
 __all__ = [
     "TFS_OK", "TFS_CG", "TFS_BICG", "TFS_CGS", "TFS_PREC_NONE", "TFS_PREC_DIAG", "TFS_PREC_DIC",
     "TFS_FP64", "TFS_MIXED", "TfsError", "load_library", "lib_path", "Matrix_Type",
     "Matrix_Mod_Topology", "Cg", "Bicg", "Cgs", "Prec_Form", "Prec_Solve", "Residual",
-    "Solver", "spmv", "SynthSystem",
+    "Solver", "spmv", "SynthSystem", "Batch",
 ]

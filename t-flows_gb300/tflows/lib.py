@@ -55,6 +55,16 @@ SIGNATURES = {
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_status_string": (C.c_char_p, [C.c_int]),
     "tfs_last_error": (C.c_char_p, []),
+    "tfs_batch_create": (C.c_int, [C.c_int, C.POINTER(P_void), C.POINTER(P_void)]),
+    "tfs_batch_release": (C.c_int, [P_void]),
+    "tfs_batch_configure": (C.c_int, [P_void, C.c_int, C.c_int]),
+    "tfs_batch_solve_device": (C.c_int, [P_void, C.c_int, C.c_int, C.c_int, C.POINTER(P_void),
+                                         C.POINTER(P_void), C.POINTER(P_void), P_i32, P_dbl, P_i32,
+                                         P_dbl, P_dbl, P_i32]),
+    "tfs_batch_solve": (C.c_int, [P_void, C.c_int, C.c_int, C.c_int, C.POINTER(P_void),
+                                  C.POINTER(P_void), C.POINTER(P_void), P_i32, P_dbl, P_i32, P_dbl,
+                                  P_dbl, P_i32]),
+    "tfs_batch_last_ms": (C.c_int, [P_void, P_dbl]),
     "tfs_use_device": (C.c_int, [C.c_int]),
     "tfs_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),
     "tfs_device_free": (C.c_int, [P_void]),

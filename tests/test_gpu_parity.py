@@ -314,3 +314,27 @@ def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
         x, r = np.zeros(s.n), s.b.copy()
         res = sol.solve(TFS_BICG, s.val, x, r, 2, 2000, ref["tol"])
         assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+
+
+@pytest.mark.parametrize("mode", [TFS_FP64, TFS_MIXED])
+@pytest.mark.parametrize("prec", [1, 2])
+def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
+    """The reference's BiCG (shadow residual r2 = r1, driven by A) produces the
+    CG iterates bit for bit; the library runs it through the CG kernels.  The
+    literal two-sequence BiCG (TFS_BICG=literal) and CG agree bitwise."""
+    s = system(CONVDIFF, 9, 8, 8)
+    tol = 1e-8 * np.linalg.norm(s.b)
+    out = {}
+    for tag in ("cg", "literal"):
+        if tag == "literal":
+            monkeypatch.setenv("TFS_BICG", "literal")
+        with Solver(s.matrix(), precision=mode) as sol:
+            x, r = np.zeros(s.n), s.b.copy()
+            method = TFS_CG if tag == "cg" else TFS_BICG
+            out[tag] = (x, r, sol.solve(method, s.val, x, r, prec, 2000, tol))
+    (xa, ra, resa), (xb, rb, resb) = out["cg"], out["literal"]
+    assert np.array_equal(xa, xb) and np.array_equal(ra, rb)
+    assert resa == resb
+    # and the oracle's Bicg equals its Cg
+    ref_b, ref_c = oracle_solve(s, TFS_BICG, prec), oracle_solve(s, TFS_CG, prec)
+    assert np.array_equal(ref_b["x"], ref_c["x"]) and ref_b["niter"] == ref_c["niter"]
