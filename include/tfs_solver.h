@@ -239,6 +239,31 @@ int tfs_sync(tfs_handle *h);
 int tfs_timer_start(tfs_handle *h);
 int tfs_timer_stop(tfs_handle *h, double *ms);
 
+/* ---- no-allocation entry point -------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory at the time of the call: code handed a fixed device arena by its
+ * host framework, work issued while another thread captures a CUDA graph
+ * (cudaMalloc is not allowed then), or a coupling loop that must never block
+ * in the allocator.
+ *
+ * r1 <- r1 - A x with the per-row arithmetic of Residual.f90:22-27, and
+ * *d_norm = ||r1||_2, for a 1-based CSR matrix (row1/col1/val as in
+ * Matrix_Type) whose arrays, like x, r1 and the norm, already live in device
+ * memory.  Nothing is allocated: the only scratch is a static device array
+ * holding one partial sum per 256 rows, sized for TFS_NOALLOC_MAX_ROWS rows;
+ * every GPU that loads the library keeps it (about 128 KB) until the process
+ * exits.  Larger n is rejected with TFS_ERR_ARG.  The call is asynchronous on
+ * `stream` (a cudaStream_t; NULL = the default stream).  The first call on a
+ * device looks up the scratch array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  Calls share the scratch
+ * array, so calls that overlap on the GPU (different streams or threads)
+ * race: serialise them. */
+#define TFS_NOALLOC_MAX_ROWS 4194304
+int tfs_residual_norm_noalloc(int32_t n, const int32_t *d_row1,
+                              const int32_t *d_col1, const double *d_val,
+                              const double *d_x, double *d_r1, double *d_norm,
+                              void *stream);
+
 /* ---- host-side mesh utilities ------------------------------------------ */
 
 /* Count of stored entries of the face-connectivity matrix (one per cell plus
