@@ -52,6 +52,10 @@ WORKLOADS = {
     "convdiff160_diag_bicg": (1, 160, 1, 1, "160^3 jittered-hex upwind convection-diffusion, diagonal BiCG"),
     "convdiff160_diag_cgs": (1, 160, 2, 1, "160^3 jittered-hex upwind convection-diffusion, diagonal CGS"),
 }
+BATCH_WORKLOAD = "batched256_poisson_cg"
+BATCH_DESC = ("256 independent jittered-hex pressure-Poisson systems, cells log-uniform in "
+              "[5k, 500k] (k x k x m meshes), jitter U(0, 25%), own seed and permutation each; "
+              "diagonal CG, all in one persistent cluster launch")
 
 
 def log(*a):
@@ -356,6 +360,227 @@ def run_ours(args, dist: Dist) -> dict | None:
     return line if dist.rank == 0 else None
 
 
+# ---------------------------------------------------------------- batched arm
+
+def batch_specs(n_sys: int, seed: int) -> list[tuple[int, int, int, float, int]]:
+    """(nx, ny, nz, jitter, seed) of every system of the batched workload."""
+    from tflows.synth import loguniform, uniform
+    out = []
+    for k in range(n_sys):
+        n = loguniform(5000, 500000, seed, k)
+        kk = max(2, int(round(n ** (1.0 / 3.0))))
+        m = max(1, int(round(n / (kk * kk))))
+        jit = 0.25 * uniform(seed, 21, k)
+        out.append((kk, kk, m, jit, seed * 1000 + k))
+    return out
+
+
+def run_batched(args, dist: Dist) -> dict | None:
+    """256 uneven systems: mixed-precision batched cluster solve vs the plain
+    binary64 single-system path (one tfs_solve_device per system)."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    import tflows
+    from tflows.lib import TFS_CG, TFS_FP64, TFS_MIXED, check, load_library
+
+    lib = load_library()
+    check(lib.tfs_use_device(dist.local_rank), "tfs_use_device")
+    specs = batch_specs(args.batch_systems, BASE_SEED + dist.rank)
+    t0 = time.perf_counter()
+
+    def make(spec):
+        nx, ny, nz, jit, sd = spec
+        lib.tfs_use_device(dist.local_rank)
+        s = tflows.SynthSystem(0, nx, ny, nz, jitter=jit, seed=sd)
+        return s, tflows.Solver(s.matrix())
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        pairs = list(ex.map(make, specs))
+    systems = [p[0] for p in pairs]
+    solvers = [p[1] for p in pairs]
+    n_rows = sum(s.n for s in systems)
+    nnz_all = sum(s.nnz for s in systems)
+    log(f"[bench] batch of {len(systems)} systems, {n_rows} cells, {nnz_all} entries "
+        f"({time.perf_counter() - t0:.1f}s to build and register)")
+
+    def dalloc(nbytes):
+        p = C.c_void_p()
+        check(lib.tfs_device_alloc(nbytes, C.byref(p)), "tfs_device_alloc")
+        return p.value
+
+    d_val, d_b, d_x, d_r, d_zero = [], [], [], [], []
+    for s, sv in zip(systems, solvers):
+        d_val.append(dalloc(8 * s.nnz)); d_b.append(dalloc(8 * s.n)); d_x.append(dalloc(8 * s.n))
+        d_r.append(dalloc(8 * s.n)); d_zero.append(dalloc(8 * s.n))
+        z = np.zeros(s.n)
+        check(lib.tfs_copy(sv.h, C.c_void_p(d_val[-1]), s.val.ctypes.data_as(C.c_void_p), 8 * s.nnz), "copy")
+        check(lib.tfs_copy(sv.h, C.c_void_p(d_b[-1]), s.b.ctypes.data_as(C.c_void_p), 8 * s.n), "copy")
+        check(lib.tfs_copy(sv.h, C.c_void_p(d_zero[-1]), z.ctypes.data_as(C.c_void_p), 8 * s.n), "copy")
+        check(lib.tfs_sync(sv.h), "sync")
+    tols = np.array([REL_TOL * float(np.linalg.norm(s.b)) for s in systems])
+    nsys = len(systems)
+    batch = tflows.Batch(solvers)
+    ptrs = lambda a: (C.c_void_p * len(a))(*a)
+    reset_dst = ptrs(d_x + d_r)
+    reset_src = ptrs(d_zero + d_b)
+    reset_bytes = (C.c_size_t * (2 * nsys))(*([8 * s.n for s in systems] * 2))
+
+    def batch_step(mode):
+        check(lib.tfs_batch_copy(batch.b, 2 * nsys, reset_dst, reset_src, reset_bytes), "tfs_batch_copy")
+        return batch.solve_device(TFS_CG, 1, d_val, d_x, d_r, args.niter, tols, mode=mode)
+
+    # Autotune the cluster shape on the workload itself (one solve per shape).
+    tune = {}
+    for cl in (4, 8, 16):
+        for tpb in (256, 512):
+            try:
+                batch.configure(cl, tpb)
+                t = time.perf_counter()
+                batch_step(TFS_MIXED)
+                tune[(cl, tpb)] = time.perf_counter() - t
+            except Exception as e:  # a shape that cannot be resident
+                log(f"[bench] cluster {cl} x {tpb}: {e}")
+    best = min(tune, key=tune.get)
+    batch.configure(*best)
+    log(f"[bench] autotuned cluster {best[0]} x {best[1]} threads: "
+        + ", ".join(f"{k[0]}x{k[1]}={v * 1e3:.1f}ms" for k, v in sorted(tune.items())))
+
+    results = {}
+    launches = 0
+    clock_info = None
+    for mode, name in ((TFS_FP64, "batched_fp64"), (TFS_MIXED, "batched_mixed")):
+        for _ in range(args.warmup):
+            res = batch_step(mode)
+        dist.barrier()
+        sampler = ClockSampler(dist.local_rank) if mode == TFS_MIXED else None
+        if sampler:
+            sampler.__enter__()
+        t = time.perf_counter()
+        lat = []
+        for _ in range(args.steps):
+            res = batch_step(mode)
+            lat.append(res.ms)
+        wall = time.perf_counter() - t
+        if sampler:
+            sampler.__exit__(None, None, None)
+            clock_info = sampler.summary()
+        dist.barrier()
+        wall = dist.max(wall)
+        results[name] = {"solves_per_s": dist.sum(nsys * args.steps) / wall,
+                         "ms_per_batch": wall / args.steps * 1e3,
+                         "device_ms_per_batch": statistics.mean(lat),
+                         "iterations_total": int(res.niter.sum()),
+                         "iterations_max": int(res.niter.max()),
+                         "failed": int((res.status != 0).sum())}
+        if mode == TFS_MIXED:
+            launches = 2 * args.steps
+        log(f"[bench] {name}: {results[name]['solves_per_s']:.1f} solves/s")
+
+    # Plain binary64 path: one graph-captured single-system solve per system.
+    for sv in solvers:
+        sv.set_precision(TFS_FP64)
+    def plain_pass():
+        its = 0
+        for k, sv in enumerate(solvers):
+            check(lib.tfs_copy(sv.h, C.c_void_p(d_x[k]), C.c_void_p(d_zero[k]), 8 * systems[k].n), "copy")
+            check(lib.tfs_copy(sv.h, C.c_void_p(d_r[k]), C.c_void_p(d_b[k]), 8 * systems[k].n), "copy")
+            r = sv.solve_device(TFS_CG, d_val[k], d_x[k], d_r[k], 1, args.niter, float(tols[k]))
+            its += r.niter
+        return its
+    plain_pass()
+    t = time.perf_counter()
+    plain_steps = max(1, args.steps // 5)
+    for _ in range(plain_steps):
+        its = plain_pass()
+    wall = dist.max(time.perf_counter() - t)
+    results["plain_fp64"] = {"solves_per_s": dist.sum(nsys * plain_steps) / wall,
+                             "ms_per_pass": wall / plain_steps * 1e3, "iterations_total": its}
+    log(f"[bench] plain fp64: {results['plain_fp64']['solves_per_s']:.1f} solves/s")
+
+    # Error of the mixed batched solutions against the binary64 single path.
+    res = batch_step(TFS_MIXED)
+    errs = []
+    x_m, x_p = np.empty(1), np.empty(1)
+    for k, (s, sv) in enumerate(zip(systems, solvers)):
+        x_m = np.empty(s.n)
+        check(lib.tfs_copy(sv.h, x_m.ctypes.data_as(C.c_void_p), C.c_void_p(d_x[k]), 8 * s.n), "copy")
+        check(lib.tfs_sync(sv.h), "sync")
+        errs.append(x_m)
+    plain_pass()
+    max_err = 0.0
+    for k, (s, sv) in enumerate(zip(systems, solvers)):
+        x_p = np.empty(s.n)
+        check(lib.tfs_copy(sv.h, x_p.ctypes.data_as(C.c_void_p), C.c_void_p(d_x[k]), 8 * s.n), "copy")
+        check(lib.tfs_sync(sv.h), "sync")
+        max_err = max(max_err, float(np.linalg.norm(errs[k] - x_p) / np.linalg.norm(x_p)))
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = batched_cpu_baseline(specs, args)
+
+    mixed = results["batched_mixed"]
+    line = {
+        "metric": METRIC, "value": round(mixed["solves_per_s"], 3), "unit": UNIT,
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(mixed["ms_per_batch"], 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic (seeded jittered-hex meshes, random cell numbering, RHS U[-1,1])",
+        "config": {"workload": BATCH_WORKLOAD, "description": BATCH_DESC, "systems": nsys,
+                   "cells": n_rows, "nnz": nnz_all, "solver": "CG", "prec": "diag",
+                   "stop": "||b-Ax|| < 1e-8 ||b|| per system, x0 = 0",
+                   "cluster": best[0], "threads_per_cta": best[1],
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{dist.world}"},
+        "batched_mixed": mixed, "batched_fp64": results["batched_fp64"],
+        "plain_fp64": results["plain_fp64"],
+        "mixed_batched_over_plain_fp64": round(mixed["solves_per_s"] / results["plain_fp64"]["solves_per_s"], 3),
+        "max_rel_err_vs_fp64": max_err, "autotune_ms": {f"{k[0]}x{k[1]}": round(v * 1e3, 2) for k, v in tune.items()},
+        "gpu_launches": launches, "clocks": clock_info,
+        "e2e": None,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    batch.close()
+    for p in d_val + d_b + d_x + d_r + d_zero:
+        lib.tfs_device_free(C.c_void_p(p))
+    return line if dist.rank == 0 else None
+
+
+def _batched_cpu_one(spec):
+    sys.path[:0] = [str(REPO), str(REPO / "t-flows_gb300")]
+    import numpy as np
+    import tflows
+    from oracle import tfs_oracle as O
+    nx, ny, nz, jit, sd = spec
+    s = tflows.SynthSystem(0, nx, ny, nz, jitter=jit, seed=sd)
+    x, r = np.zeros(s.n), s.b.copy()
+    tol = REL_TOL * float(np.linalg.norm(s.b))
+    t = time.perf_counter()
+    it, _, _ = O.solve(0, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 5000, tol)
+    return time.perf_counter() - t, s.n, it
+
+
+def batched_cpu_baseline(specs, args) -> dict:
+    """The oracle on all host cores, one system per core, on a sample of the
+    batch; scaled to all systems by their share of n^(4/3) (work ~ n x iterations)."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    sample = specs[:cores]
+    ctx = mp.get_context("spawn")
+    t = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_batched_cpu_one, sample)
+    wall = time.perf_counter() - t
+    w = lambda spec: (spec[0] * spec[1] * spec[2]) ** (4.0 / 3.0)
+    scale = sum(w(sp) for sp in specs) / sum(w(sp) for sp in sample)
+    est = wall * scale
+    return {"value": round(len(specs) / est, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the first {len(sample)} systems of the batch, one single-threaded binary64 "
+                      f"diagonal-CG solve per core ({wall:.1f} s wall), scaled to the {len(specs)} "
+                      f"systems by sum(n^(4/3))"}
+
+
 # ---------------------------------------------------------------- reference arm
 
 _REF = {}
@@ -431,7 +656,8 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="poisson128_dic_cg")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + [BATCH_WORKLOAD], default="poisson128_dic_cg")
+    ap.add_argument("--batch-systems", type=int, default=256)
     ap.add_argument("--niter", type=int, default=5000)
     ap.add_argument("--spmv-reps", type=int, default=50)
     ap.add_argument("--ref-sample-iters", type=int, default=30)
@@ -452,7 +678,7 @@ def main(argv=None) -> int:
     __graft_entry__.build()
     dist = Dist()
     try:
-        line = run_ours(args, dist)
+        line = run_batched(args, dist) if args.workload == BATCH_WORKLOAD else run_ours(args, dist)
     finally:
         dist.close()
     if line is not None:

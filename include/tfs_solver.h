@@ -212,6 +212,11 @@ int tfs_batch_solve(tfs_batch *b, int method, int prec, int mode,
 /* Device time (CUDA events) of the last batch solve, gather included. */
 int tfs_batch_last_ms(const tfs_batch *b, double *ms);
 
+/* n copies dst[k] <- src[k] (bytes[k]) ordered on the batch's stream, e.g.
+ * to reset every system's x and r1 before a solve. */
+int tfs_batch_copy(tfs_batch *b, int n, void *const *dst, const void *const *src,
+                   const size_t *bytes);
+
 /* ---- device and timing helpers ------------------------------------------
  * For callers without a CUDA runtime of their own (the benchmark harness, a
  * Fortran driver).  None of these replaces a reference interface. */

@@ -1574,3 +1574,13 @@ extern "C" int tfs_batch_last_ms(const tfs_batch *b, double *ms)
     *ms = b->last_ms;
     return TFS_OK;
 }
+
+extern "C" int tfs_batch_copy(tfs_batch *b, int n, void *const *dst, const void *const *src,
+                              const size_t *bytes)
+{
+    if (!b || n < 0 || (n > 0 && (!dst || !src || !bytes))) return TFS_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    for (int k = 0; k < n; k++)
+        CK(cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDefault, b->stream));
+    return TFS_OK;
+}

@@ -65,6 +65,8 @@ SIGNATURES = {
                                   C.POINTER(P_void), C.POINTER(P_void), P_i32, P_dbl, P_i32, P_dbl,
                                   P_dbl, P_i32]),
     "tfs_batch_last_ms": (C.c_int, [P_void, P_dbl]),
+    "tfs_batch_copy": (C.c_int, [P_void, C.c_int, C.POINTER(P_void), C.POINTER(P_void),
+                                 C.POINTER(C.c_size_t)]),
     "tfs_residual_norm_noalloc": (C.c_int, [i32, P_void, P_void, P_void, P_void, P_void, P_void, P_void]),
     "tfs_use_device": (C.c_int, [C.c_int]),
     "tfs_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),

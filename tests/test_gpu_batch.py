@@ -48,7 +48,10 @@ def test_batch_fp64_matches_oracle(method, prec, systems):
 
 @pytest.mark.parametrize("method", [TFS_CG, TFS_BICG])
 def test_batch_mixed_converges(method, systems):
-    sel = [t for t in systems if method == TFS_BICG or t[0].kind == POISSON]
+    # The convection-diffusion systems are excluded: the reference's BiCG
+    # (= CG, see the BiCG test of test_gpu_parity) does not converge on them
+    # even in binary64, so there is no tolerance to reach.
+    sel = [t for t in systems if t[0].kind == POISSON]
     with Batch([sv for _, sv in sel], cluster=8, threads=256) as b:
         xs, rs, res = _run(b, sel, method, 1, TFS_MIXED)
     from oracle import tfs_oracle as O

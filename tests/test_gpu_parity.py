@@ -338,3 +338,32 @@ def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
     # and the oracle's Bicg equals its Cg
     ref_b, ref_c = oracle_solve(s, TFS_BICG, prec), oracle_solve(s, TFS_CG, prec)
     assert np.array_equal(ref_b["x"], ref_c["x"]) and ref_b["niter"] == ref_c["niter"]
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_mixed_cgs_nonsymmetric(prec, convdiff12):
+    """Mixed-precision CGS on the non-symmetric convection-diffusion system
+    reaches the binary64 tolerance on the true residual."""
+    s, _ = convdiff12
+    ref = oracle_solve(s, TFS_CGS, prec)
+    assert ref["niter"] < 2000
+    with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+        x, r = np.zeros(s.n), s.b.copy()
+        res = sol.solve(TFS_CGS, s.val, x, r, prec, 2000, ref["tol"])
+    assert res.status == 0 and res.fin_res < ref["tol"]
+    rt = s.b.copy()
+    O.residual(s.n, s.row, s.col, s.val, x, rt)
+    assert np.linalg.norm(rt) < ref["tol"]
+    assert rel_l2(x, ref["x"]) < 1e-6
+
+
+def test_bicg_nonconvergence_matches_reference(convdiff12):
+    """On the non-symmetric system the reference's BiCG (= CG) does not reach
+    1e-8 within the limit; the library reproduces the limit+1 return and the
+    iterate."""
+    s, sol = convdiff12
+    ref = oracle_solve(s, TFS_BICG, 1, niter=300)
+    x, r = np.zeros(s.n), s.b.copy()
+    res = sol.solve(TFS_BICG, s.val, x, r, 1, 300, ref["tol"])
+    assert ref["niter"] == 301 and res.niter == 301
+    assert res.fin_res == pytest.approx(ref["fin"], rel=1e-6)
