@@ -29,7 +29,9 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import itertools
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -52,6 +54,12 @@ WORKLOADS = {
     "convdiff160_diag_bicg": (1, 160, 1, 1, "160^3 jittered-hex upwind convection-diffusion, diagonal BiCG"),
     "convdiff160_diag_cgs": (1, 160, 2, 1, "160^3 jittered-hex upwind convection-diffusion, diagonal CGS"),
 }
+SERVE_WORKLOAD = "serving_trace"
+SERVE_DESC = ("Poisson arrivals at 400/s (seeded): 70% pressure solves (jittered-hex Poisson, "
+              "diagonal CG, tol 1e-6 or 1e-8 relative at 50/50, limit 2000), 30% transport solves "
+              "(upwind convection-diffusion, diagonal BiCG with the call sites' limit of 10 "
+              "iterations, Compute_Scalar.f90:615-618); cells log-uniform in [10k, 2M] over a pool of "
+              "resident systems; 150 GB device budget")
 BATCH_WORKLOAD = "batched256_poisson_cg"
 BATCH_DESC = ("256 independent jittered-hex pressure-Poisson systems, cells log-uniform in "
               "[5k, 500k] (k x k x m meshes), jitter U(0, 25%), own seed and permutation each; "
@@ -360,6 +368,142 @@ def run_ours(args, dist: Dist) -> dict | None:
     return line if dist.rank == 0 else None
 
 
+# ---------------------------------------------------------------- serving arm
+
+def run_serving(args, dist: Dist) -> dict | None:
+    """Replay a seeded Poisson-arrival trace through tfs_server, mixed then
+    binary64; latency = submit -> completion."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    import tflows
+    from tflows.lib import TFS_BICG, TFS_CG, TFS_FP64, TFS_MIXED, check, load_library
+    from tflows.synth import loguniform, uniform
+
+    lib = load_library()
+    check(lib.tfs_use_device(dist.local_rank), "tfs_use_device")
+    seed = BASE_SEED + 7 + dist.rank
+    n_pool = args.serve_pool
+    specs = []
+    for k in range(n_pool):
+        kind = 0 if uniform(seed, 31, k) < 0.7 else 1
+        n = loguniform(10000, 2000000, seed, 1000 + k)
+        kk = max(2, int(round(n ** (1.0 / 3.0))))
+        m = max(1, int(round(n / (kk * kk))))
+        specs.append((kind, kk, kk, m, seed * 100 + k))
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        systems = list(ex.map(lambda sp: tflows.SynthSystem(sp[0], sp[1], sp[2], sp[3], jitter=0.2,
+                                                            seed=sp[4]), specs))
+    log(f"[bench] serving pool: {len(systems)} systems, {sum(s.n for s in systems)} cells "
+        f"({time.perf_counter() - t0:.1f}s)")
+
+    def dalloc(nbytes):
+        p = C.c_void_p()
+        check(lib.tfs_device_alloc(nbytes, C.byref(p)), "tfs_device_alloc")
+        return p.value
+
+    import ctypes.util
+    rt = C.CDLL("libcudart.so.13") if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else C.CDLL("libcudart.so")
+    rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    slots = args.serve_slots
+    dev = []
+    for s in systems:
+        d = {"val": dalloc(8 * s.nnz), "b": dalloc(8 * s.n),
+             "x": [dalloc(8 * s.n) for _ in range(slots)], "r": [dalloc(8 * s.n) for _ in range(slots)]}
+        rt.cudaMemcpy(C.c_void_p(d["val"]), s.val.ctypes.data, 8 * s.nnz, 1)
+        rt.cudaMemcpy(C.c_void_p(d["b"]), s.b.ctypes.data, 8 * s.n, 1)
+        dev.append(d)
+    # The trace: exponential inter-arrival times, request kind from the pool.
+    rng_t = [uniform(seed, 41, j) for j in range(args.serve_requests)]
+    gaps = [-math.log(1.0 - u) / args.serve_rate for u in rng_t]
+    arrivals = list(itertools.accumulate(gaps))
+    reqs = []
+    for j in range(args.serve_requests):
+        k = min(n_pool - 1, int(uniform(seed, 42, j) * n_pool))
+        tol_rel = 1e-6 if uniform(seed, 43, j) < 0.5 else 1e-8
+        reqs.append((arrivals[j], k, tol_rel))
+    tols = [float(np.linalg.norm(s.b)) for s in systems]
+
+    def replay(mode):
+        budget = int(args.serve_budget_gb * 1e9)
+        lat, qd, runm, its, status = [], [], [], [], []
+        with tflows.Server(budget, max_inflight=args.serve_inflight, device=dist.local_rank) as srv:
+            ids = [srv.add_system(s.n, s.row, s.col, s.dia) for s in systems]
+            # Warm every system once (layout, graphs), outside the trace.
+            warm = []
+            for k, s in enumerate(systems):
+                method = TFS_CG if specs[k][0] == 0 else TFS_BICG
+                warm.append(srv.submit(ids[k], method, 1, dev[k]["val"], dev[k]["x"][0], dev[k]["r"][0],
+                                       10, 0.0, mode=mode, d_b=dev[k]["b"], x0_zero=True))
+            for t in warm:
+                srv.wait(t)
+            pending = {}            # (system, slot) -> ticket still using it
+            next_slot = [0] * len(systems)
+            tickets = []
+            start = time.perf_counter()
+            for (t_arr, k, tol_rel) in reqs:
+                now = time.perf_counter() - start
+                if t_arr > now:
+                    time.sleep(t_arr - now)
+                slot = next_slot[k] % slots
+                next_slot[k] += 1
+                if (k, slot) in pending:       # slot still in use: wait for it
+                    res = srv.wait(pending.pop((k, slot)))
+                    tickets.append(res)
+                method = TFS_CG if specs[k][0] == 0 else TFS_BICG
+                niter = 2000 if method == TFS_CG else 10
+                t = srv.submit(ids[k], method, 1, dev[k]["val"], dev[k]["x"][slot], dev[k]["r"][slot],
+                               niter, tol_rel * tols[k], mode=mode, d_b=dev[k]["b"], x0_zero=True)
+                pending[(k, slot)] = t
+            for t in pending.values():
+                tickets.append(srv.wait(t))
+            span = time.perf_counter() - start
+            stats = srv.stats()
+        for res in tickets:
+            lat.append(res["latency_ms"]); qd.append(res["queued_ms"]); runm.append(res["run_ms"])
+            its.append(res["niter"]); status.append(res["status"])
+        return {"solves_per_s": len(tickets) / span, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                "mean_ms": statistics.mean(lat), "queue_p99_ms": pct(qd, 99), "run_p50_ms": pct(runm, 50),
+                "requests": len(tickets), "span_s": span, "failed": sum(1 for x in status if x != 0),
+                "evictions": stats["evictions"], "resident_gb": stats["resident_bytes"] / 1e9}
+
+    results = {}
+    clock_info = None
+    for mode, name in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
+        dist.barrier()
+        sampler = ClockSampler(dist.local_rank) if mode == TFS_MIXED else None
+        if sampler:
+            sampler.__enter__()
+        results[name] = replay(mode)
+        if sampler:
+            sampler.__exit__(None, None, None)
+            clock_info = sampler.summary()
+        log(f"[bench] serving {name}: {results[name]['solves_per_s']:.1f} solves/s, "
+            f"p50 {results[name]['p50_ms']:.2f} ms, p99 {results[name]['p99_ms']:.2f} ms")
+    for d in dev:
+        for p in [d["val"], d["b"]] + d["x"] + d["r"]:
+            lib.tfs_device_free(C.c_void_p(p))
+    mixed = results["mixed"]
+    line = {
+        "metric": METRIC, "value": round(dist.sum(mixed["solves_per_s"]), 3), "unit": UNIT,
+        "n_gpus": dist.world, "steps": len(reqs), "warmup": len(systems),
+        "ms_per_step": round(mixed["mean_ms"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic (seeded jittered-hex meshes, random cell numbering, RHS U[-1,1], seeded trace)",
+        "config": {"workload": SERVE_WORKLOAD, "description": SERVE_DESC, "pool": len(systems),
+                   "requests": len(reqs), "rate_per_s": args.serve_rate,
+                   "max_inflight": args.serve_inflight, "budget_gb": args.serve_budget_gb,
+                   "parallelism": f"replicas x{dist.world}"},
+        "p50_ms": round(mixed["p50_ms"], 3), "p99_ms": round(mixed["p99_ms"], 3),
+        "mixed": mixed, "fp64": results["fp64"],
+        "mixed_over_fp64": round(mixed["solves_per_s"] / results["fp64"]["solves_per_s"], 3),
+        "gpu_launches": None, "clocks": clock_info, "e2e": None,
+    }
+    return line if dist.rank == 0 else None
+
+
 # ---------------------------------------------------------------- batched arm
 
 def batch_specs(n_sys: int, seed: int) -> list[tuple[int, int, int, float, int]]:
@@ -656,7 +800,14 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + [BATCH_WORKLOAD], default="poisson128_dic_cg")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD],
+                    default="poisson128_dic_cg")
+    ap.add_argument("--serve-pool", type=int, default=32)
+    ap.add_argument("--serve-requests", type=int, default=1200)
+    ap.add_argument("--serve-rate", type=float, default=400.0)
+    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-inflight", type=int, default=16)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--batch-systems", type=int, default=256)
     ap.add_argument("--niter", type=int, default=5000)
     ap.add_argument("--spmv-reps", type=int, default=50)
@@ -678,7 +829,12 @@ def main(argv=None) -> int:
     __graft_entry__.build()
     dist = Dist()
     try:
-        line = run_batched(args, dist) if args.workload == BATCH_WORKLOAD else run_ours(args, dist)
+        if args.workload == BATCH_WORKLOAD:
+            line = run_batched(args, dist)
+        elif args.workload == SERVE_WORKLOAD:
+            line = run_serving(args, dist)
+        else:
+            line = run_ours(args, dist)
     finally:
         dist.close()
     if line is not None:

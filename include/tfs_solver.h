@@ -244,6 +244,51 @@ int tfs_sync(tfs_handle *h);
 int tfs_timer_start(tfs_handle *h);
 int tfs_timer_stop(tfs_handle *h, double *ms);
 
+/* ---- serving: solves that arrive over time --------------------------------
+ * A request loop for the solves a flow solver (or many of them) issues over
+ * time: pressure and transport systems of different sizes.  A worker thread
+ * admits each request as soon as its system is idle and a slot is free, so
+ * requests that arrive while others run start at once and their work
+ * overlaps on the GPU (each solve is one graph launch on its system's
+ * stream).  Matrix layouts, preconditioners and Krylov vectors stay resident
+ * between requests; systems are admitted against a device-memory budget and
+ * idle ones are evicted, least recently used first, when a new one does not
+ * fit (an evicted system is rebuilt on its next request).  A result does not
+ * depend on what else was running.  Replaces: the sequence of Cg.f90 /
+ * Bicg.f90 / Cgs.f90 calls of one or more Process runs. */
+typedef struct tfs_server tfs_server;
+
+typedef struct tfs_result {
+    int64_t ticket;
+    int32_t niter, status;          /* as the solve entry points return them  */
+    double  ini_res, fin_res;
+    double  queued_ms, run_ms, latency_ms;  /* submit->start, start->done, submit->done */
+} tfs_result;
+
+typedef struct tfs_server_stats {
+    int64_t submitted, completed, refused, evictions, registrations;
+    int64_t resident_bytes, resident_systems, running, queued;
+} tfs_server_stats;
+
+int tfs_server_create(int device, int64_t hbm_budget_bytes, int max_inflight,
+                      tfs_server **out);
+/* Waits for running solves, then frees every resident system. */
+int tfs_server_destroy(tfs_server *s);
+/* Register a topology (1-based CSR, copied); device state is built lazily. */
+int tfs_server_add_system(tfs_server *s, int32_t n, int32_t nnz, const int32_t *row1,
+                          const int32_t *col1, const int32_t *dia1, int64_t *sys_id);
+/* Queue one solve on device arrays (natural order; valid until done).
+ * b is read from d_b (NULL: from d_r1, the in/out convention of Cg.f90);
+ * r1 is written to d_r1; x starts from zero when x0_zero, else from d_x.
+ * mode: TFS_FP64 or TFS_MIXED.  Returns at once with a ticket. */
+int tfs_server_submit(tfs_server *s, int64_t sys_id, int method, int prec, int mode,
+                      const double *d_val, const double *d_b, double *d_x, double *d_r1,
+                      int x0_zero, int32_t niter, double tol, int64_t *ticket);
+/* Wait up to timeout_s for a ticket; TFS_ERR_TIMEOUT if still running.  A
+ * ticket is returned once. */
+int tfs_server_wait(tfs_server *s, int64_t ticket, double timeout_s, tfs_result *out);
+int tfs_server_get_stats(tfs_server *s, tfs_server_stats *out);
+
 /* ---- no-allocation entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory at the time of the call: code handed a fixed device arena by its

@@ -196,26 +196,54 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         // p = z + beta p (Cg.f90:114-123; both directions for BiCG).
         const double beta = iter == 1 ? 0.0 : rho / rho_old;
         const VT betaT = (VT)beta;
-        for (int i = gtid; i < n_int; i += stride) {
-            VT z = W.z[i];
-            W.p[i] = iter == 1 ? z : z + betaT * W.p[i];
-            if (METHOD == 1) { VT z2 = W.z2[i]; W.p2[i] = iter == 1 ? z2 : z2 + betaT * W.p2[i]; }
+        for (int i0 = gtid; i0 < n_int; i0 += 2 * stride) {
+            const int i1 = i0 + stride;
+            const bool ok1 = i1 < n_int;
+            VT z0 = W.z[i0], p0 = W.p[i0], z1 = ok1 ? W.z[i1] : (VT)0, p1 = ok1 ? W.p[i1] : (VT)0;
+            VT a0 = (VT)0, b0 = (VT)0, a1 = (VT)0, b1 = (VT)0;
+            if (METHOD == 1) {
+                a0 = W.z2[i0]; b0 = W.p2[i0];
+                if (ok1) { a1 = W.z2[i1]; b1 = W.p2[i1]; }
+            }
+            W.p[i0] = iter == 1 ? z0 : z0 + betaT * p0;
+            if (METHOD == 1) W.p2[i0] = iter == 1 ? a0 : a0 + betaT * b0;
+            if (ok1) {
+                W.p[i1] = iter == 1 ? z1 : z1 + betaT * p1;
+                if (METHOD == 1) W.p2[i1] = iter == 1 ? a1 : a1 + betaT * b1;
+            }
         }
         cl.sync();
         // q = A p and alpha (Cg.f90:128-153 / Bicg.f90:136-165).
         double pq = 0.0;
-        for (int i = gtid; i < n_int; i += stride) {
-            RowGeom g = row_geom(A, i);
-            if (METHOD == 1) {
+        if (METHOD == 1) {
+            for (int i = gtid; i < n_int; i += stride) {
+                RowGeom g = row_geom(A, i);
                 VT s1 = (VT)0, s2 = (VT)0;
                 row_accum2<false, VT, VT, VT>(s1, s2, A.col, valT, W.p, W.p2, g.off, 0, g.len);
                 W.q[i] = s1;
                 W.q2[i] = s2;
                 pq = fma((double)W.p2[i], (double)s1, pq);
-            } else {
-                VT s = row_accum<false, VT, VT, VT>((VT)0, A.col, valT, W.p, g.off, 0, g.len);
-                W.q[i] = s;
-                pq = fma((double)W.p[i], (double)s, pq);
+            }
+        } else {
+            // Four rows per thread and step, all loads before any store.
+            for (int i0 = gtid; i0 < n_int; i0 += 4 * stride) {
+                int ii[4];
+                VT sv[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    ii[q] = i0 + q * stride;
+                    sv[q] = (VT)0;
+                    if (ii[q] < n_int) {
+                        RowGeom g = row_geom(A, ii[q]);
+                        sv[q] = row_accum<false, VT, VT, VT>((VT)0, A.col, valT, W.p, g.off, 0, g.len);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (ii[q] < n_int) {
+                        W.q[ii[q]] = sv[q];
+                        pq = fma((double)W.p[ii[q]], (double)sv[q], pq);
+                    }
             }
         }
         double v1[1] = {pq};
@@ -225,22 +253,48 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         // x (or e) += alpha p, r -= alpha q, z = M^-1 r, ||r||, next rho.
         e2 = 0.0;
         rz = 0.0;
-        for (int i = gtid; i < n_int; i += stride) {
-            if (MIXED) F.e[i] = fmaf((float)alfaT, (float)W.p[i], F.e[i]);
-            else V.x[i] = V.x[i] + alfa * (double)W.p[i];
-            VT r1 = W.r[i] - alfaT * W.q[i];
-            W.r[i] = r1;
-            VT dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
-            VT z1 = r1 / dT;
-            W.z[i] = z1;
-            e2 = fma((double)r1, (double)r1, e2);
-            if (METHOD == 1) {
+        if (METHOD == 1) {
+            for (int i = gtid; i < n_int; i += stride) {
+                if (MIXED) F.e[i] = fmaf((float)alfaT, (float)W.p[i], F.e[i]);
+                else V.x[i] = V.x[i] + alfa * (double)W.p[i];
+                VT r1 = W.r[i] - alfaT * W.q[i];
+                W.r[i] = r1;
+                VT dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
+                VT z1 = r1 / dT;
+                W.z[i] = z1;
+                e2 = fma((double)r1, (double)r1, e2);
                 VT r2 = W.r2[i] - alfaT * W.q2[i];
                 W.r2[i] = r2;
                 W.z2[i] = r2 / dT;
                 rz = fma((double)z1, (double)r2, rz);
-            } else {
-                rz = fma((double)r1, (double)z1, rz);
+            }
+        } else {
+            for (int i0 = gtid; i0 < n_int; i0 += 4 * stride) {
+                int ii[4];
+                VT pv[4], rv[4], qv[4], dv[4];
+                double xv[4];
+                float ev[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    ii[q] = i0 + q * stride;
+                    const int i = ii[q] < n_int ? ii[q] : i0;
+                    pv[q] = W.p[i]; rv[q] = W.r[i]; qv[q] = W.q[i];
+                    dv[q] = MIXED ? (VT)F.d[i] : (VT)V.d[i];
+                    if (MIXED) ev[q] = F.e[i]; else xv[q] = V.x[i];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (ii[q] >= n_int) continue;
+                    const int i = ii[q];
+                    if (MIXED) F.e[i] = fmaf((float)alfaT, (float)pv[q], ev[q]);
+                    else V.x[i] = xv[q] + alfa * (double)pv[q];
+                    VT r1 = rv[q] - alfaT * qv[q];
+                    W.r[i] = r1;
+                    VT z1 = r1 / dv[q];
+                    W.z[i] = z1;
+                    e2 = fma((double)r1, (double)r1, e2);
+                    rz = fma((double)r1, (double)z1, rz);
+                }
             }
         }
         double v3[2] = {e2, rz};

@@ -562,6 +562,7 @@ static void free_handle(tfs_handle *h)
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->tev0) cudaEventDestroy(h->tev0);
     if (h->tev1) cudaEventDestroy(h->tev1);
+    if (h->ev_done) cudaEventDestroy(h->ev_done);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->stream2) cudaStreamDestroy(h->stream2);
     delete h;
@@ -999,11 +1000,14 @@ static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
 
 // --------------------------------------------------------------- solve
 
-static int solve_impl(int method, tfs_handle *h, const double *val, double *x, double *r1,
-                      int32_t prec, int32_t *niter, double tol, double *ini_res, double *fin_res,
-                      bool device_ptrs)
+// Everything a solve puts on the handle's stream, without waiting: per-call
+// parameters, host-to-device copies (host arrays), the graph, device-to-host
+// copies and the state read-back, then h->ev_done.
+int tfs_solve_launch(int method, tfs_handle *h, const double *val, double *x, double *r1,
+                     int32_t prec, int32_t niter, double tol, bool device_ptrs,
+                     const double *b_in, int x0_zero)
 {
-    if (!h || !val || !x || !r1 || !niter || !ini_res || !fin_res) return TFS_ERR_ARG;
+    if (!h || !val || !x || !r1) return TFS_ERR_ARG;
     if (method < TFS_CG || method > TFS_CGS || prec < 0 || prec > 2) return TFS_ERR_ARG;
     CK(cudaSetDevice(h->device));
     int rc = ensure_layout(h, prec);
@@ -1018,12 +1022,14 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
     GraphEntry *ge = nullptr;
     rc = get_graph(h, kmethod, prec, &ge);
     if (rc) return rc;
+    h->last_graph = ge;
     cudaStream_t s = h->stream;
     DevParams &P = *h->h_params;
     P.tol = tol;
-    P.niter_max = *niter;
+    P.niter_max = niter;
+    P.x0_zero = x0_zero;
     P.val_csr = device_ptrs ? val : h->stage_val;
-    P.b = device_ptrs ? r1 : h->stage_b;
+    P.b = device_ptrs ? (b_in ? b_in : r1) : h->stage_b;
     P.x = device_ptrs ? x : h->stage_x;
     P.r_out = device_ptrs ? r1 : h->stage_b;
     CK(cudaMemcpyAsync(h->params, h->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s));
@@ -1044,7 +1050,14 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
         CK(cudaMemcpyAsync(r1, h->stage_b, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToHost, s));
     }
     CK(cudaMemcpyAsync(h->h_state, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    if (!h->ev_done) CK(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
+    CK(cudaEventRecord(h->ev_done, s));
+    return TFS_OK;
+}
+
+// Outputs of a launched solve once h->ev_done has completed.
+int tfs_solve_collect(tfs_handle *h, int32_t *niter, double *ini_res, double *fin_res)
+{
     const DevState &S = *h->h_state;
     if (S.early != 1) *ini_res = S.ini_res;
     *fin_res = S.fin_res;
@@ -1060,9 +1073,21 @@ static int solve_impl(int method, tfs_handle *h, const double *val, double *x, d
     T.spmv_launches = (int64_t)S.spmv_n;
     T.sweep_ns_total = (double)S.sweep_ns;
     T.sweep_launches = (int64_t)S.sweep_n;
-    T.kernel_launches = ge->prologue_kernels + (int64_t)S.loops * ge->body_kernels + ge->epilogue_kernels;
+    const GraphEntry *ge = h->last_graph;
+    T.kernel_launches = ge ? ge->prologue_kernels + (int64_t)S.loops * ge->body_kernels + ge->epilogue_kernels : 0;
     T.device_bytes = h->device_bytes;
     return S.status;
+}
+
+static int solve_impl(int method, tfs_handle *h, const double *val, double *x, double *r1,
+                      int32_t prec, int32_t *niter, double tol, double *ini_res, double *fin_res,
+                      bool device_ptrs)
+{
+    if (!h || !niter || !ini_res || !fin_res) return TFS_ERR_ARG;
+    int rc = tfs_solve_launch(method, h, val, x, r1, prec, *niter, tol, device_ptrs);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return tfs_solve_collect(h, niter, ini_res, fin_res);
 }
 
 extern "C" int tfs_solve_device(int method, tfs_handle *h, const double *d_val, double *d_x,
@@ -1148,6 +1173,7 @@ static int prepare_values(tfs_handle *h, const double *val, int prec = 0)
     DevParams &P = *h->h_params;
     P.tol = 0.0;
     P.niter_max = 1;
+    P.x0_zero = 0;
     P.val_csr = h->stage_val;
     P.b = h->stage_b;
     P.x = h->stage_x;

@@ -65,7 +65,7 @@ struct SweepCtl {
 struct DevParams {
     double tol;
     int niter_max;
-    int pad;
+    int x0_zero;             // 1: start from x0 = 0 instead of reading x
     const double *val_csr;   // natural CSR order, nnz
     const double *b;         // natural order, n (r1 on entry)
     double *x;               // natural order, n (in/out)
@@ -100,7 +100,8 @@ struct tfs_handle {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr, ev_done = nullptr;
+    const struct GraphEntry *last_graph = nullptr;
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int grid = 0;                      // blocks of the chunk kernels
@@ -146,3 +147,11 @@ struct tfs_handle {
 // tfs_engine.cu
 int tfs_engine_error(cudaError_t e, const char *what);
 void tfs_set_error_text(const char *msg);
+// Enqueue a whole solve on h->stream (ends with h->ev_done), then read its
+// outputs once h->ev_done has completed.
+int tfs_solve_launch(int method, tfs_handle *h, const double *val, double *x, double *r1,
+                     int32_t prec, int32_t niter, double tol, bool device_ptrs,
+                     const double *b_in = nullptr, int x0_zero = 0);
+int tfs_solve_collect(tfs_handle *h, int32_t *niter, double *ini_res, double *fin_res);
+// Device bytes a topology will hold once its layout is built (estimate).
+int64_t tfs_estimate_bytes(int32_t n, int32_t nnz);

@@ -11,10 +11,11 @@ from .matrix_mod import Matrix_Type, Matrix_Mod_Topology
 from .solvers_mod import Cg, Bicg, Cgs, Prec_Form, Prec_Solve, Residual, Solver, spmv
 from .synth import SynthSystem
 from .batch import Batch
+from .serve import Server
 
 __all__ = [
     "TFS_OK", "TFS_CG", "TFS_BICG", "TFS_CGS", "TFS_PREC_NONE", "TFS_PREC_DIAG", "TFS_PREC_DIC",
     "TFS_FP64", "TFS_MIXED", "TfsError", "load_library", "lib_path", "Matrix_Type",
     "Matrix_Mod_Topology", "Cg", "Bicg", "Cgs", "Prec_Form", "Prec_Solve", "Residual",
-    "Solver", "spmv", "SynthSystem", "Batch",
+    "Solver", "spmv", "SynthSystem", "Batch", "Server",
 ]

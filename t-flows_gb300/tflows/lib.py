@@ -29,6 +29,16 @@ class tfs_stats(C.Structure):
                 ("device_bytes", i64)]
 
 
+class tfs_result(C.Structure):
+    _fields_ = [("ticket", i64), ("niter", i32), ("status", i32), ("ini_res", dbl), ("fin_res", dbl),
+                ("queued_ms", dbl), ("run_ms", dbl), ("latency_ms", dbl)]
+
+
+class tfs_server_stats(C.Structure):
+    _fields_ = [(k, i64) for k in ("submitted", "completed", "refused", "evictions", "registrations",
+                                   "resident_bytes", "resident_systems", "running", "queued")]
+
+
 class TfsError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str = ""):
         self.status = status
@@ -67,6 +77,13 @@ SIGNATURES = {
     "tfs_batch_last_ms": (C.c_int, [P_void, P_dbl]),
     "tfs_batch_copy": (C.c_int, [P_void, C.c_int, C.POINTER(P_void), C.POINTER(P_void),
                                  C.POINTER(C.c_size_t)]),
+    "tfs_server_create": (C.c_int, [C.c_int, i64, C.c_int, C.POINTER(P_void)]),
+    "tfs_server_destroy": (C.c_int, [P_void]),
+    "tfs_server_add_system": (C.c_int, [P_void, i32, i32, P_i32, P_i32, P_i32, C.POINTER(i64)]),
+    "tfs_server_submit": (C.c_int, [P_void, i64, C.c_int, C.c_int, C.c_int, P_void, P_void, P_void,
+                                    P_void, C.c_int, i32, dbl, C.POINTER(i64)]),
+    "tfs_server_wait": (C.c_int, [P_void, i64, dbl, C.POINTER(tfs_result)]),
+    "tfs_server_get_stats": (C.c_int, [P_void, C.POINTER(tfs_server_stats)]),
     "tfs_residual_norm_noalloc": (C.c_int, [i32, P_void, P_void, P_void, P_void, P_void, P_void, P_void]),
     "tfs_use_device": (C.c_int, [C.c_int]),
     "tfs_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),
