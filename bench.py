@@ -747,10 +747,69 @@ def _ref_sample(arg):
     return time.perf_counter() - t
 
 
+def _serve_cpu_one(spec):
+    sys.path[:0] = [str(REPO), str(REPO / "t-flows_gb300")]
+    import numpy as np
+    import tflows
+    from oracle import tfs_oracle as O
+    kind, nx, ny, nz, sd, tol_rel = spec
+    s = tflows.SynthSystem(kind, nx, ny, nz, jitter=0.2, seed=sd)
+    x, r = np.zeros(s.n), s.b.copy()
+    method, niter = (0, 2000) if kind == 0 else (1, 10)
+    t = time.perf_counter()
+    O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 1, niter, tol_rel * float(np.linalg.norm(s.b)))
+    return time.perf_counter() - t
+
+
+def run_reference_other(args) -> dict:
+    """Reference arm of the batched and serving workloads: the oracle on all
+    host cores, one single-threaded solve per core, on a sample."""
+    import multiprocessing as mp
+    from tflows.synth import loguniform, uniform
+    cores = os.cpu_count() or 1
+    if args.workload == BATCH_WORKLOAD:
+        specs = batch_specs(args.batch_systems, BASE_SEED)
+        cpu = batched_cpu_baseline(specs, args)
+        desc, extra = BATCH_DESC, {"systems": len(specs)}
+    else:
+        seed = BASE_SEED + 7
+        pool = []
+        for k in range(args.serve_pool):
+            kind = 0 if uniform(seed, 31, k) < 0.7 else 1
+            n = loguniform(10000, 2000000, seed, 1000 + k)
+            kk = max(2, int(round(n ** (1.0 / 3.0))))
+            m = max(1, int(round(n / (kk * kk))))
+            pool.append((kind, kk, kk, m, seed * 100 + k))
+        sample = []
+        for j in range(cores):
+            k = min(args.serve_pool - 1, int(uniform(seed, 42, j) * args.serve_pool))
+            tol_rel = 1e-6 if uniform(seed, 43, j) < 0.5 else 1e-8
+            sample.append(pool[k] + (tol_rel,))
+        t = time.perf_counter()
+        with mp.get_context("spawn").Pool(cores) as p:
+            times = p.map(_serve_cpu_one, sample)
+        wall = time.perf_counter() - t
+        cpu = {"value": round(cores / statistics.mean(times), 4), "unit": UNIT, "cores": cores,
+               "kind": "port",
+               "sample": f"the first {cores} requests of the trace, one single-threaded binary64 solve "
+                         f"per core ({wall:.1f} s wall); throughput = cores / mean solve time"}
+        desc, extra = SERVE_DESC, {"requests_sampled": cores}
+    return {
+        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 0,
+        "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded systems as our arm)",
+        "config": dict({"workload": args.workload, "description": desc}, **extra),
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args) -> dict:
     import multiprocessing as mp
 
     import numpy as np
+    if args.workload not in WORKLOADS:
+        return run_reference_other(args)
     kind, nside, method, prec, desc = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
     # Full iteration count of the reference solve (one full solve, untimed).
