@@ -727,17 +727,12 @@ k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ 
     if (st->done) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
     double acc = 0.0;
-    // Two rows per thread and step: both rows' loads are in flight together.
-    for (int c0 = blockIdx.x; c0 < A.n_chunks; c0 += 2 * (int)gridDim.x) {
-        const int c1 = c0 + (int)gridDim.x;
-        const bool ok1 = c1 < A.n_chunks;
-        const int i0 = c0 * TFS_TPB + threadIdx.x, i1 = ok1 ? c1 * TFS_TPB + threadIdx.x : i0;
-        RowGeom g0 = row_geom(A, i0), g1 = row_geom(A, i1);
-        double s0 = row_accum<false, double, double, double>(0.0, A.col, val, p, g0.off, 0, g0.len);
-        double s1 = ok1 ? row_accum<false, double, double, double>(0.0, A.col, val, p, g1.off, 0, g1.len) : 0.0;
-        q[i0] = s0;
-        acc = fma(p[i0], s0, acc);
-        if (ok1) { q[i1] = s1; acc = fma(p[i1], s1, acc); }
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        double s = row_accum<false, double, double, double>(0.0, A.col, val, p, g.off, 0, g.len);
+        q[i] = s;
+        acc = fma(p[i], s, acc);
     }
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) {

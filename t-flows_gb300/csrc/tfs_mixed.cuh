@@ -181,17 +181,12 @@ k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__
     if (st->done || st->need_true) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
     float acc = 0.f;
-    // Two rows per thread and step: both rows' loads are in flight together.
-    for (int c0 = blockIdx.x; c0 < A.n_chunks; c0 += 2 * (int)gridDim.x) {
-        const int c1 = c0 + (int)gridDim.x;
-        const bool ok1 = c1 < A.n_chunks;
-        const int i0 = c0 * TFS_TPB + threadIdx.x, i1 = ok1 ? c1 * TFS_TPB + threadIdx.x : i0;
-        RowGeom g0 = row_geom(A, i0), g1 = row_geom(A, i1);
-        float s0 = row_accum<false, float, float, float>(0.f, A.col, val, p, g0.off, 0, g0.len);
-        float s1 = ok1 ? row_accum<false, float, float, float>(0.f, A.col, val, p, g1.off, 0, g1.len) : 0.f;
-        q[i0] = s0;
-        acc = fmaf(p[i0], s0, acc);
-        if (ok1) { q[i1] = s1; acc = fmaf(p[i1], s1, acc); }
+    for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
+        int i = c * TFS_TPB + threadIdx.x;
+        RowGeom g = row_geom(A, i);
+        float s = row_accum<false, float, float, float>(0.f, A.col, val, p, g.off, 0, g.len);
+        q[i] = s;
+        acc = fmaf(p[i], s, acc);
     }
     double v[1] = {(double)acc};
     if (grid_reduce<1>(v, part, &st->counter)) {

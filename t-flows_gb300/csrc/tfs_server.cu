@@ -74,10 +74,12 @@ struct tfs_server {
 
 int64_t tfs_estimate_bytes(int32_t n, int32_t nnz)
 {
-    // layout: perm/iperm/rowinfo (12 B/row), col/vmap/val/val32 (20 B/entry,
-    // ~3% SELL padding), 16 binary64 + 16 binary32 vectors (192 B/row),
-    // staging (8 B/entry + 16 B/row).
-    return (int64_t)n * (12 + 192 + 16) + (int64_t)nnz * 29 + (1 << 20);
+    // Layout: rows padded to 1024 (+ up to 31 per DIC level), perm/rowinfo
+    // (8 B/row), iperm (4 B/row), col/vmap/val/val32 (20 B/entry, SELL
+    // padding ~5%), 16 binary64 + 16 binary32 vectors (192 B/row), partials;
+    // fixed: staging val/b/x (8 B/entry + 16 B/row) and state.
+    const int64_t n_pad = ((int64_t)n + 1023) / 1024 * 1024 + 32 * 64;
+    return n_pad * 200 + (int64_t)n * 20 + (int64_t)nnz * 29 + (64 << 10);
 }
 
 static void release_system(tfs_server *S, System &sy)

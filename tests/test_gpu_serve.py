@@ -132,10 +132,16 @@ def test_budget_eviction_and_refusal(pool):
     the whole budget is refused."""
     from tflows.lib import load_library
     lib = load_library()
-    small = [pool[2], pool[0]]
-    est = max(s.n * 220 + s.nnz * 29 + (1 << 20) for s in small)
+    small = [pool[0], pool[3]]
+
+    def est(s):   # tfs_estimate_bytes
+        n_pad = (s.n + 1023) // 1024 * 1024 + 32 * 64
+        return n_pad * 200 + s.n * 20 + s.nnz * 29 + (64 << 10)
+
+    budget = int(1.15 * max(est(s) for s in small))
+    assert est(small[0]) + est(small[1]) > budget
     reqs = [(0, TFS_CG, 1, TFS_FP64), (1, TFS_CG, 1, TFS_FP64), (0, TFS_CG, 2, TFS_FP64)]
-    out, stats = _run(small, reqs, max_inflight=1, budget=int(est * 1.3))
+    out, stats = _run(small, reqs, max_inflight=1, budget=budget)
     for (res, x, _), (k, method, prec, mode) in zip(out, reqs):
         ref = oracle_solve(small[k], method, prec)
         assert res["status"] == 0 and rel_l2(x, ref["x"]) <= SOL_REL
