@@ -103,14 +103,14 @@ static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int b
 // block; MODE 1 runs the tail first and the levels in descending order.
 template <typename T, int NR, int MODE>
 static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, const T *b1, const T *b2,
-                         T *o1, T *o2, const T *y1, const T *y2, int *count)
+                         T *o1, T *o2, const T *y1, const T *y2, int *count, bool with_tail = true)
 {
     SellDev A = sell_of(h);
     const int L = h->n_levels, tail = h->tail_level;
     const bool pdl = h->use_pdl != 0;
     int first = 1;
     auto tail_launch = [&]() -> cudaError_t {
-        if (tail >= L) return cudaSuccess;
+        if (tail >= L || !with_tail) return cudaSuccess;
         (*count)++;
         cudaError_t e = launch_ex(pdl, k_sweep_tail<T, NR, MODE>, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, o1, o2,
                                   y1, y2, (const int *)h->d_lvl_begin, tail, L, h->st, first);
@@ -462,12 +462,19 @@ static int build_layout(tfs_handle *h, int kind)
     int g = h->sm_count * 8;
     h->grid = h->n_chunks < g ? h->n_chunks : g;
     if (h->grid < 1) h->grid = 1;
+    // SpMV-type kernels: one 256-row chunk per block (more rows in flight
+    // than a grid-stride loop); TFS_SPMV_GRID=sm8 selects 8 blocks per SM.
+    h->grid_spmv = h->n_chunks;
+    {
+        const char *env = getenv("TFS_SPMV_GRID");
+        if (env && strcmp(env, "sm8") == 0) h->grid_spmv = h->grid;
+    }
 
     if ((rc = dalloc(h, &h->perm, n_int)) || (rc = dalloc(h, &h->iperm, n)) ||
         (rc = dalloc(h, &h->rowinfo, n_int)) || (rc = dalloc(h, &h->slice_off, n_slices + 1)) ||
         (rc = dalloc(h, &h->col, nnz_pad)) || (rc = dalloc(h, &h->vmap, nnz_pad)) ||
         (rc = dalloc(h, &h->val, nnz_pad)) || (rc = dalloc(h, &h->val32, nnz_pad)) ||
-        (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->grid + 64)))
+        (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->n_chunks + 64)))
         return rc;
     {
         // Sweep work items: tiles of at most TFS_SWEEP_TPB rows inside one
@@ -512,7 +519,7 @@ static int build_layout(tfs_handle *h, int kind)
     CK(cudaMemcpyAsync(h->vmap, vmap.data(), sizeof(int) * (size_t)nnz_pad, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->val, 0, sizeof(double) * (size_t)nnz_pad, h->stream));
     CK(cudaMemsetAsync(h->val32, 0, sizeof(float) * (size_t)nnz_pad, h->stream));
-    CK(cudaMemsetAsync(h->part, 0, sizeof(double) * (TFS_NPART * (size_t)h->grid + 64), h->stream));
+    CK(cudaMemsetAsync(h->part, 0, sizeof(double) * (TFS_NPART * (size_t)h->n_chunks + 64), h->stream));
 
     // Work vectors: 16 binary64 + 16 binary32, zero so padding rows stay zero.
     const size_t nv64 = 16, nv32 = 16;
@@ -716,13 +723,24 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         CKL("sweep launch");
         return TFS_OK;
     }
+    // Forward levels, both tails in one block, backward levels.
     int rc;
+    const bool tails = h->tail_level < h->n_levels;
+    auto tail2 = [&](auto kernel) -> int {
+        if (!tails) return TFS_OK;
+        cudaError_t e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
+                                  z2, (const int *)h->d_lvl_begin, h->tail_level, h->n_levels, h->st);
+        (*count)++;
+        return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
+    };
     if (nr == 1) {
-        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count))) return rc;
-        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count))) return rc;
+        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 1>))) return rc;
+        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false))) return rc;
     } else {
-        if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count))) return rc;
-        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count))) return rc;
+        if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 2>))) return rc;
+        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false))) return rc;
     }
     return TFS_OK;
 }
@@ -748,67 +766,68 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
                           cudaGraphConditionalHandle cond, int *count)
 {
     SellDev A = sell_of(h);
-    const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
+    const int G = h->grid, GS = h->grid_spmv, T = TFS_TPB, nc = h->n_chunks;
     Vec64 &V = h->v;
     Vec32 &F = h->f;
     const float *v32 = h->val32;
     int rc;
     *count = 0;
     if (method == TFS_CG) {
+        const int n4 = h->n_int / 4, G4 = h->n_int / (4 * TFS_TPB);
         if (prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
-            k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
-            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
-            k_mx_cg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
-            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
+            k_mx_dot_rho4<<<G4, T, 0, s>>>(n4, F, h->st, h->part);
+            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
+            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 6;
+        } else {
+            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update4<true><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
+            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
-        } else {
-            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv_pq<<<G, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
-            k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
-            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
-            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 4;
         }
     } else if (method == TFS_BICG) {
         if (prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 2, F.r, F.r2, F.y, F.y2, F.z, F.z2, count))) return rc;
             k_mx_dot_rho<1><<<G, T, 0, s>>>(nc, F, h->st, h->part);
             k_mx_bicg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_spmv2_pq<<<GS, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_bicg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 5;
+            *count += 6;
         } else {
             k_mx_bicg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv2_pq<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_spmv2_pq<<<GS, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_bicg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<1, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 4;
+            *count += 5;
         }
     } else {
         if (prec == 2) {
             k_mx_cgs_u<false><<<G, T, 0, s>>>(nc, F, h->st);
             if ((rc = launch_sweeps<float>(h, s, 1, F.u2, nullptr, F.y, nullptr, F.p2, nullptr, count))) return rc;
-            k_mx_spmv_v<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_spmv_v<<<GS, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_cgs_q<false><<<G, T, 0, s>>>(nc, F, h->st);
             if ((rc = launch_sweeps<float>(h, s, 1, F.w, nullptr, F.y, nullptr, F.p, nullptr, count))) return rc;
-            k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_cgs_spmv_r<<<GS, T, 0, s>>>(A, v32, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 5;
+            *count += 6;
         } else {
             k_mx_cgs_u<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv_v<<<G, T, 0, s>>>(A, v32, F, h->st, h->part);
+            k_mx_spmv_v<<<GS, T, 0, s>>>(A, v32, F, h->st, h->part);
             k_mx_cgs_q<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_cgs_spmv_r<<<G, T, 0, s>>>(A, v32, V, F, h->st, h->part);
+            k_mx_cgs_spmv_r<<<GS, T, 0, s>>>(A, v32, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<2, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 5;
+            *count += 6;
         }
     }
     CKL("mixed body launch");
@@ -822,14 +841,14 @@ static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst)
 
 static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s)
 {
-    k_mx_spmv_pq<<<h->grid, TFS_TPB, 0, s>>>(sell_of(h), h->val32, h->f.p, h->f.q, h->st, h->part);
+    k_mx_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, s>>>(sell_of(h), h->val32, h->f.p, h->f.q, h->st, h->part);
 }
 
 static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
                        cudaGraphConditionalHandle cond, int *count)
 {
     SellDev A = sell_of(h);
-    const int G = h->grid, T = TFS_TPB, nc = h->n_chunks;
+    const int G = h->grid, GS = h->grid_spmv, T = TFS_TPB, nc = h->n_chunks;
     Vec64 &V = h->v;
     int rc;
     *count = 0;
@@ -838,12 +857,12 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
             k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_pq<<<G, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 4;
         } else {
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_pq<<<G, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
             k_cg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 3;
         }
@@ -852,12 +871,12 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             if ((rc = launch_sweeps<double>(h, s, 2, V.r, V.r2, V.y, V.y2, V.z, V.z2, count))) return rc;
             k_dot_rho<1><<<G, T, 0, s>>>(nc, V, h->st, h->part);
             k_bicg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv2_pq<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_spmv2_pq<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part);
             k_bicg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 4;
         } else {
             k_bicg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv2_pq<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_spmv2_pq<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part);
             k_bicg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 3;
         }
@@ -865,16 +884,16 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
         if (prec == 2) {
             k_cgs_u<false><<<G, T, 0, s>>>(nc, V, h->st);
             if ((rc = launch_sweeps<double>(h, s, 1, V.u2, nullptr, V.y, nullptr, V.p2, nullptr, count))) return rc;
-            k_spmv_v<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_spmv_v<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part);
             k_cgs_q<false><<<G, T, 0, s>>>(nc, V, h->st);
             if ((rc = launch_sweeps<double>(h, s, 1, V.w, nullptr, V.y, nullptr, V.p, nullptr, count))) return rc;
-            k_cgs_spmv_r<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
+            k_cgs_spmv_r<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
             *count += 4;
         } else {
             k_cgs_u<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_v<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part);
+            k_spmv_v<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part);
             k_cgs_q<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_cgs_spmv_r<<<G, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
+            k_cgs_spmv_r<<<GS, T, 0, s>>>(A, h->val, V, h->st, h->part, cond);
             *count += 4;
         }
     }
@@ -1220,7 +1239,7 @@ extern "C" int tfs_spmv(tfs_handle *h, const double *val, const double *p, doubl
     CK(cudaSetDevice(h->device));
     int rc;
     if ((rc = prepare_values(h, val)) || (rc = vec_in(h, p, h->v.p))) return rc;
-    k_spmv_pq<<<h->grid, TFS_TPB, 0, h->stream>>>(sell_of(h), h->val, h->v.p, h->v.q, h->st, h->part);
+    k_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, h->stream>>>(sell_of(h), h->val, h->v.p, h->v.q, h->st, h->part);
     CKL("spmv");
     return vec_out(h, h->v.q, q);
 }
@@ -1291,7 +1310,7 @@ extern "C" int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int rep
     k_diag_form<<<(h->n_int + 255) / 256, 256, 0, s>>>(A, h->val, h->v.p, 0);
     tfs_mixed_fill32(h, h->v.p, h->f.p);
     auto launch = [&]() {
-        if (mode == TFS_FP64) k_spmv_pq<<<h->grid, TFS_TPB, 0, s>>>(A, h->val, h->v.p, h->v.q, h->st, h->part);
+        if (mode == TFS_FP64) k_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, s>>>(A, h->val, h->v.p, h->v.q, h->st, h->part);
         else tfs_mixed_spmv_only(h, s);
     };
     for (int w = 0; w < 3; w++) launch();

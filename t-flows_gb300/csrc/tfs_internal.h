@@ -104,7 +104,8 @@ struct tfs_handle {
     const struct GraphEntry *last_graph = nullptr;
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
-    int grid = 0;                      // blocks of the chunk kernels
+    int grid = 0;                      // blocks of the vector kernels (grid-stride)
+    int grid_spmv = 0;                 // blocks of the SpMV-type kernels
     int sweep_grid = 0;                // blocks of the dataflow sweeps
     int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch
     int use_pdl = 1;                   // programmatic dependent launch between level kernels

@@ -678,6 +678,40 @@ k_sweep_tail(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b
     }
 }
 
+// Both tails of one preconditioner application in one block: the forward
+// sweep of the tail levels (ascending), then their backward sweep
+// (descending).  The backward rows of the tail depend only on tail rows and on
+// their own forward value, all produced by this block, so no grid-wide step
+// separates the two halves.
+template <typename T, int NR>
+__global__ void __launch_bounds__(TFS_SWEEP_TPB)
+k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
+              T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
+{
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    if (st->done) return;
+    const int nl = l_end - l_begin;
+    for (int q = 0; q < nl; q++) {
+        const int lev = l_begin + q;
+        const int r1 = __ldg(lvl_begin + lev + 1);
+        for (int i = __ldg(lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
+            RowGeom g = row_geom(A, i);
+            sweep_row<T, NR, 0, 0>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, i, g, nullptr, nullptr);
+        }
+        __syncthreads();
+    }
+    for (int q = 0; q < nl; q++) {
+        const int lev = l_end - 1 - q;
+        const int r1 = __ldg(lvl_begin + lev + 1);
+        for (int i = __ldg(lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
+            RowGeom g = row_geom(A, i);
+            sweep_row<T, NR, 1, 0>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, i, g, nullptr, nullptr);
+        }
+        __syncthreads();
+    }
+}
+
 // rho after the sweeps: CG (r, z) (Cg.f90:108-112); BiCG (z1, r2) (Bicg.f90:113-117).
 template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)

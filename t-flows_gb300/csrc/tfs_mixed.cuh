@@ -221,6 +221,84 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
     if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
 
+// ---------------------------------------------------- CG, four rows per thread
+//
+// The binary32 CG vector kernels with 16-byte loads: every thread owns four
+// consecutive rows (n_int is a multiple of 1024, the vectors are 16-byte
+// aligned), one block covers 1024 rows and the grid covers all rows, so a
+// launch keeps as many bytes in flight as the SMs can hold.
+
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p4(int n4, Vec32 F, const DevState *st)
+{
+    if (st->done || st->need_true) return;
+    const int it = st->iter;
+    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    const float4 *z4 = (const float4 *)F.z;
+    float4 *p4 = (float4 *)F.p;
+    for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
+        float4 z = z4[v], p = p4[v];
+        if (it == 1) p4[v] = z;
+        else p4[v] = make_float4(fmaf(beta, p.x, z.x), fmaf(beta, p.y, z.y), fmaf(beta, p.z, z.z), fmaf(beta, p.w, z.w));
+    }
+}
+
+__global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho4(int n4, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
+    }
+    const float4 *r4 = (const float4 *)F.r, *z4 = (const float4 *)F.z;
+    float acc = 0.f;
+    for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
+        float4 r = r4[v], z = z4[v];
+        acc = fmaf(r.x, z.x, acc); acc = fmaf(r.y, z.y, acc); acc = fmaf(r.z, z.z, acc); acc = fmaf(r.w, z.w, acc);
+    }
+    double v1[1] = {(double)acc};
+    if (grid_reduce<1>(v1, part, &st->counter)) st->rho = v1[0];
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part)
+{
+    if (st->done || st->need_true) return;
+    const float a = (float)st->alpha;
+    const float4 *p4 = (const float4 *)F.p, *q4 = (const float4 *)F.q, *d4 = (const float4 *)F.d;
+    float4 *e4 = (float4 *)F.e, *r4 = (float4 *)F.r, *zz4 = (float4 *)F.z;
+    float e2 = 0.f, rz = 0.f;
+    for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
+        float4 p = p4[v], q = q4[v], r = r4[v], e = e4[v], d;
+        if (FUSED) d = d4[v];
+        e4[v] = make_float4(fmaf(a, p.x, e.x), fmaf(a, p.y, e.y), fmaf(a, p.z, e.z), fmaf(a, p.w, e.w));
+        r = make_float4(fmaf(-a, q.x, r.x), fmaf(-a, q.y, r.y), fmaf(-a, q.z, r.z), fmaf(-a, q.w, r.w));
+        r4[v] = r;
+        e2 = fmaf(r.x, r.x, e2); e2 = fmaf(r.y, r.y, e2); e2 = fmaf(r.z, r.z, e2); e2 = fmaf(r.w, r.w, e2);
+        if (FUSED) {
+            float4 z = make_float4(r.x / d.x, r.y / d.y, r.z / d.z, r.w / d.w);
+            zz4[v] = z;
+            rz = fmaf(r.x, z.x, rz); rz = fmaf(r.y, z.y, rz); rz = fmaf(r.z, z.z, rz); rz = fmaf(r.w, z.w, rz);
+        }
+    }
+    double v2[2] = {(double)e2, (double)rz};
+    if (grid_reduce<2>(v2, part, &st->counter)) mx_end_iteration(st, v2[0], v2[1], FUSED);
+}
+
+__global__ void __launch_bounds__(TFS_TPB) k_mx_fold4(int n4, Vec64 V, Vec32 F, const DevState *st)
+{
+    if (st->done || !st->need_true) return;
+    float4 *e4 = (float4 *)F.e;
+    double2 *x2 = (double2 *)V.x;
+    for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
+        float4 e = e4[v];
+        double2 xa = x2[2 * v], xb = x2[2 * v + 1];
+        xa.x += (double)e.x; xa.y += (double)e.y; xb.x += (double)e.z; xb.y += (double)e.w;
+        x2[2 * v] = xa;
+        x2[2 * v + 1] = xb;
+        e4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 // -------------------------------------------------------------- BiCG
 
 template <bool FROMZ>
