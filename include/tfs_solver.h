@@ -170,6 +170,13 @@ int tfs_get_levels(tfs_handle *h, int32_t *levels);
 int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int reps,
                   double *ms_per_launch);
 
+/* Device time of one DIC preconditioner application (forward sweep,
+ * diagonal scaling, backward sweep; replaces Prec_Solve.f90:46-67 with prec
+ * = 2) averaged over `reps` back-to-back applications (CUDA events), with the
+ * factor formed from val (host, nnz), in the given arithmetic. */
+int tfs_time_prec(tfs_handle *h, const double *val, int mode, int reps,
+                  double *ms_per_application);
+
 /* Human-readable text for a status code. */
 const char *tfs_status_string(int status);
 

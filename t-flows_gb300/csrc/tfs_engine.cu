@@ -462,12 +462,25 @@ static int build_layout(tfs_handle *h, int kind)
     int g = h->sm_count * 8;
     h->grid = h->n_chunks < g ? h->n_chunks : g;
     if (h->grid < 1) h->grid = 1;
-    // SpMV-type kernels: one 256-row chunk per block (more rows in flight
-    // than a grid-stride loop); TFS_SPMV_GRID=sm8 selects 8 blocks per SM.
-    h->grid_spmv = h->n_chunks;
+    // SpMV-type kernels: 8 blocks per SM, grid-stride over the 256-row
+    // chunks (measured faster than one chunk per block on the 128^3
+    // system: 42.5 us against 72.9 us); TFS_SPMV_GRID=chunks selects the latter.
+    h->grid_spmv = h->grid;
     {
         const char *env = getenv("TFS_SPMV_GRID");
-        if (env && strcmp(env, "sm8") == 0) h->grid_spmv = h->grid;
+        if (env && strcmp(env, "chunks") == 0) h->grid_spmv = h->n_chunks;
+    }
+    // Binary32 CG vector kernels: 16-byte loads, grid-stride over the same
+    // grid as the other vector kernels.  TFS_VEC=full gives every thread
+    // exactly four rows (n_int / 1024 blocks); TFS_VEC=quad selects the
+    // scalar four-chunk kernels.
+    h->vec4 = 1;
+    h->grid_vec4 = h->grid < h->n_int / (4 * TFS_TPB) ? h->grid : h->n_int / (4 * TFS_TPB);
+    if (h->grid_vec4 < 1) h->grid_vec4 = 1;
+    {
+        const char *env = getenv("TFS_VEC");
+        if (env && strcmp(env, "full") == 0) h->grid_vec4 = h->n_int / (4 * TFS_TPB);
+        if (env && strcmp(env, "quad") == 0) h->vec4 = 0;
     }
 
     if ((rc = dalloc(h, &h->perm, n_int)) || (rc = dalloc(h, &h->iperm, n)) ||
@@ -773,8 +786,24 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     int rc;
     *count = 0;
     if (method == TFS_CG) {
-        const int n4 = h->n_int / 4, G4 = h->n_int / (4 * TFS_TPB);
-        if (prec == 2) {
+        const int n4 = h->n_int / 4, G4 = h->grid_vec4;
+        if (!h->vec4 && prec == 2) {
+            if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
+            k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
+            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 6;
+        } else if (!h->vec4) {
+            k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
+            k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        } else if (prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
             k_mx_dot_rho4<<<G4, T, 0, s>>>(n4, F, h->st, h->part);
             k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
@@ -1320,6 +1349,42 @@ extern "C" int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int rep
     CK(cudaEventRecord(h->ev1, s));
     CK(cudaEventSynchronize(h->ev1));
     CKL("spmv timing");
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
+    *ms = (double)t / reps;
+    return TFS_OK;
+}
+
+// DIC preconditioner application (forward sweep, diagonal scaling, backward
+// sweep: Prec_Solve.f90:46-67) timed alone: the factor is formed from val
+// once, then `reps` applications to r = 1 are launched back to back.
+extern "C" int tfs_time_prec(tfs_handle *h, const double *val, int mode, int reps, double *ms)
+{
+    if (!h || !val || !ms || reps < 1 || (mode != TFS_FP64 && mode != TFS_MIXED)) return TFS_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = prepare_values(h, val, 2);
+    if (rc) return rc;
+    if ((rc = form_prec(h, 2))) return rc;
+    SellDev A = sell_of(h);
+    cudaStream_t s = h->stream;
+    k_diag_form<<<(h->n_int + 255) / 256, 256, 0, s>>>(A, h->val, h->v.r, 0);
+    tfs_mixed_fill32(h, h->v.r, h->f.r);
+    tfs_mixed_fill32(h, h->v.d, h->f.d);
+    int count = 0;
+    auto launch = [&]() -> int {
+        if (mode == TFS_FP64)
+            return launch_sweeps<double>(h, s, 1, h->v.r, nullptr, h->v.y, nullptr, h->v.z, nullptr, &count);
+        return launch_sweeps<float>(h, s, 1, h->f.r, nullptr, h->f.y, nullptr, h->f.z, nullptr, &count);
+    };
+    for (int w = 0; w < 3; w++)
+        if ((rc = launch())) return rc;
+    CKL("prec warm-up");
+    CK(cudaEventRecord(h->ev0, s));
+    for (int r = 0; r < reps; r++)
+        if ((rc = launch())) return rc;
+    CK(cudaEventRecord(h->ev1, s));
+    CK(cudaEventSynchronize(h->ev1));
+    CKL("prec timing");
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
     *ms = (double)t / reps;

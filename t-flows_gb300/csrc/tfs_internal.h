@@ -106,6 +106,8 @@ struct tfs_handle {
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int grid = 0;                      // blocks of the vector kernels (grid-stride)
     int grid_spmv = 0;                 // blocks of the SpMV-type kernels
+    int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels
+    int vec4 = 1;                      // 1: binary32 CG vector kernels with 16-byte loads
     int sweep_grid = 0;                // blocks of the dataflow sweeps
     int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch
     int use_pdl = 1;                   // programmatic dependent launch between level kernels

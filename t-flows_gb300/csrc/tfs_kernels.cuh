@@ -40,12 +40,27 @@ __device__ __forceinline__ RowGeom row_geom(const SellDev &A, int i)
     return g;
 }
 
+// Gathers of the SpMV-type kernels through L1 (ld.global.nc, NC = true) or
+// past it (ld.global.cg).  NC is only legal where the gathered vector is not
+// written during the launch: the stand-alone SpMV and residual kernels.  With
+// rows in RCM order the 256 rows of a block share many gathered entries, and
+// caching them in L1 made the binary32 SpMV of the 128^3 system 5% faster
+// (40.4 against 42.6 us).  The level sweeps (which read rows written earlier
+// in the same launch or by a PDL predecessor) and the persistent batch kernel
+// always use .cg.
+#ifndef TFS_SPMV_NC
+#define TFS_SPMV_NC true
+#endif
+template <bool NC, typename T>
+__device__ __forceinline__ T gather(const T *p)
+{
+    if constexpr (NC) return __ldg(p);
+    else return __ldcg(p);
+}
+
 // Sequential sum s - sum_{j0<=j<j1} a_j x_col(j) (SUB) or s + ... (ADD),
 // loads of four entries issued before their products are summed in order.
-// The gathers of x bypass L1 (ld.global.cg): with the random cell numbering
-// of the workloads they almost never hit there, and allocating them in L1
-// made L1 throughput the limiter of the SpMV.
-template <bool SUB, typename VT, typename XT, typename AT>
+template <bool SUB, typename VT, typename XT, typename AT, bool NC = false>
 __device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
                                         const VT *__restrict__ val,
                                         const XT *__restrict__ x, int off, int j0, int j1)
@@ -55,20 +70,21 @@ __device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
         int e0 = off + (j << 5), e1 = e0 + 32, e2 = e0 + 64, e3 = e0 + 96;
         int k0 = __ldg(col + e0), k1 = __ldg(col + e1), k2 = __ldg(col + e2), k3 = __ldg(col + e3);
         AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1), a2 = (AT)__ldg(val + e2), a3 = (AT)__ldg(val + e3);
-        AT x0 = (AT)__ldcg(x + k0), x1 = (AT)__ldcg(x + k1), x2 = (AT)__ldcg(x + k2), x3 = (AT)__ldcg(x + k3);
+        AT x0 = (AT)gather<NC>(x + k0), x1 = (AT)gather<NC>(x + k1), x2 = (AT)gather<NC>(x + k2),
+           x3 = (AT)gather<NC>(x + k3);
         if (SUB) { s = s - a0 * x0; s = s - a1 * x1; s = s - a2 * x2; s = s - a3 * x3; }
         else     { s = s + a0 * x0; s = s + a1 * x1; s = s + a2 * x2; s = s + a3 * x3; }
     }
     for (; j < j1; j++) {
         int e = off + (j << 5);
-        AT a = (AT)__ldg(val + e), xv = (AT)__ldcg(x + __ldg(col + e));
+        AT a = (AT)__ldg(val + e), xv = (AT)gather<NC>(x + __ldg(col + e));
         if (SUB) s = s - a * xv; else s = s + a * xv;
     }
     return s;
 }
 
 // Two right-hand sides through one pass over the row (Bicg.f90:136-144).
-template <bool SUB, typename VT, typename XT, typename AT>
+template <bool SUB, typename VT, typename XT, typename AT, bool NC = false>
 __device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict__ col,
                                            const VT *__restrict__ val, const XT *__restrict__ x1,
                                            const XT *__restrict__ x2, int off, int j0, int j1)
@@ -78,7 +94,8 @@ __device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict
         int e0 = off + (j << 5), e1 = e0 + 32;
         int k0 = __ldg(col + e0), k1 = __ldg(col + e1);
         AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1);
-        AT p0 = (AT)__ldcg(x1 + k0), p1 = (AT)__ldcg(x1 + k1), q0 = (AT)__ldcg(x2 + k0), q1 = (AT)__ldcg(x2 + k1);
+        AT p0 = (AT)gather<NC>(x1 + k0), p1 = (AT)gather<NC>(x1 + k1), q0 = (AT)gather<NC>(x2 + k0),
+           q1 = (AT)gather<NC>(x2 + k1);
         if (SUB) { s1 = s1 - a0 * p0; s2 = s2 - a0 * q0; s1 = s1 - a1 * p1; s2 = s2 - a1 * q1; }
         else     { s1 = s1 + a0 * p0; s2 = s2 + a0 * q0; s1 = s1 + a1 * p1; s2 = s2 + a1 * q1; }
     }
@@ -86,7 +103,7 @@ __device__ __forceinline__ void row_accum2(AT &s1, AT &s2, const int *__restrict
         int e = off + (j << 5);
         int k = __ldg(col + e);
         AT a = (AT)__ldg(val + e);
-        AT p = (AT)__ldcg(x1 + k), q = (AT)__ldcg(x2 + k);
+        AT p = (AT)gather<NC>(x1 + k), q = (AT)gather<NC>(x2 + k);
         if (SUB) { s1 = s1 - a * p; s2 = s2 - a * q; }
         else     { s1 = s1 + a * p; s2 = s2 + a * q; }
     }
@@ -307,7 +324,7 @@ k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
-        double r = row_accum<true, double, double, double>(V.r[i], A.col, val, V.x, g.off, 0, g.len);
+        double r = row_accum<true, double, double, double, TFS_SPMV_NC>(V.r[i], A.col, val, V.x, g.off, 0, g.len);
         V.r[i] = r;
         if (METHOD != 0) V.r2[i] = r;
         e2 = fma(r, r, e2);
@@ -600,7 +617,11 @@ k_sweep_lv(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
 // (cudaTriggerProgrammaticLaunchCompletion) and waits for the previous one
 // (cudaGridDependencySynchronize), so launch latency and prefetch overlap the
 // previous level.  The small trailing levels run in one single-block kernel
-// (k_sweep_tail) with __syncthreads() between levels.
+// (k_sweep_tail) with __syncthreads() between levels.  One row per thread:
+// two or four rows per thread (fewer thread slots per level, so the next
+// level's blocks could become resident earlier) measured 1.4x and 2.3x
+// slower on the 128^3 system, since a thread's rows then run their dependent
+// gathers one after the other.
 template <typename T, int NR, int MODE>
 __global__ void __launch_bounds__(TFS_TPB)
 k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
@@ -764,7 +785,7 @@ k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ 
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
-        double s = row_accum<false, double, double, double>(0.0, A.col, val, p, g.off, 0, g.len);
+        double s = row_accum<false, double, double, double, TFS_SPMV_NC>(0.0, A.col, val, p, g.off, 0, g.len);
         q[i] = s;
         acc = fma(p[i], s, acc);
     }
@@ -842,7 +863,7 @@ k_spmv2_pq(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
         double s1 = 0.0, s2 = 0.0;
-        row_accum2<false, double, double, double>(s1, s2, A.col, val, V.p, V.p2, g.off, 0, g.len);
+        row_accum2<false, double, double, double, TFS_SPMV_NC>(s1, s2, A.col, val, V.p, V.p2, g.off, 0, g.len);
         V.q[i] = s1;
         V.q2[i] = s2;
         acc = fma(V.p2[i], s1, acc);
@@ -927,7 +948,7 @@ k_spmv_v(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, doubl
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
-        double s = row_accum<false, double, double, double>(0.0, A.col, val, V.p2, g.off, 0, g.len);
+        double s = row_accum<false, double, double, double, TFS_SPMV_NC>(0.0, A.col, val, V.p2, g.off, 0, g.len);
         V.v2[i] = s;
         acc = fma(V.r2[i], s, acc);
     }
@@ -975,7 +996,7 @@ k_cgs_spmv_r(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, d
         int i = c * TFS_TPB + threadIdx.x;
         V.x[i] = V.x[i] + alfa * V.p[i];
         RowGeom g = row_geom(A, i);
-        double q2 = row_accum<false, double, double, double>(0.0, A.col, val, V.p, g.off, 0, g.len);
+        double q2 = row_accum<false, double, double, double, TFS_SPMV_NC>(0.0, A.col, val, V.p, g.off, 0, g.len);
         double r1 = V.r[i] - alfa * q2;
         V.r[i] = r1;
         e2 = fma(r1, r1, e2);

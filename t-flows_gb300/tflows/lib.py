@@ -16,7 +16,8 @@ TFS_FP64, TFS_MIXED = 0, 1
 TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF = 0, 1
 
 _PKG = Path(__file__).resolve().parent
-lib_path = _PKG / "lib" / "libtfs_gb300.so"
+# TFS_LIBRARY selects another build of the library (same ABI).
+lib_path = Path(os.environ["TFS_LIBRARY"]) if os.environ.get("TFS_LIBRARY") else _PKG / "lib" / "libtfs_gb300.so"
 
 i32, i64, u64, dbl = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 P_i32, P_dbl, P_void = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p
@@ -63,6 +64,7 @@ SIGNATURES = {
     "tfs_get_stats": (C.c_int, [P_void, C.POINTER(tfs_stats)]),
     "tfs_get_levels": (C.c_int, [P_void, P_i32]),
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
+    "tfs_time_prec": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_status_string": (C.c_char_p, [C.c_int]),
     "tfs_last_error": (C.c_char_p, []),
     "tfs_batch_create": (C.c_int, [C.c_int, C.POINTER(P_void), C.POINTER(P_void)]),

@@ -134,6 +134,13 @@ class Solver:
                                      C.byref(ms)), "tfs_time_spmv")
         return ms.value
 
+    def time_prec(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
+        """Milliseconds per DIC preconditioner application (both sweeps)."""
+        ms = _dbl(0.0)
+        check(self.lib.tfs_time_prec(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), mode, reps,
+                                     C.byref(ms)), "tfs_time_prec")
+        return ms.value
+
 
 def _solver_of(A: Matrix_Type) -> Solver:
     if A._solver is None:

@@ -320,8 +320,15 @@ def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
 @pytest.mark.parametrize("prec", [1, 2])
 def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
     """The reference's BiCG (shadow residual r2 = r1, driven by A) produces the
-    CG iterates bit for bit; the library runs it through the CG kernels.  The
-    literal two-sequence BiCG (TFS_BICG=literal) and CG agree bitwise."""
+    CG iterates bit for bit; the library runs it through the CG kernels.  In
+    binary64 the literal two-sequence BiCG (TFS_BICG=literal) and CG agree
+    bitwise.  In mixed precision the CG vector kernels split the rows over the
+    threads differently from the BiCG kernels (16-byte loads), so the binary32
+    partial sums round differently: there both converge on the binary64 true
+    residual with iteration counts within 2% and solutions within the
+    tolerance-implied distance, or both reach the iteration limit where the
+    binary64 oracle does (this BiCG is CG and need not converge on a
+    non-symmetric system)."""
     s = system(CONVDIFF, 9, 8, 8)
     tol = 1e-8 * np.linalg.norm(s.b)
     out = {}
@@ -333,10 +340,18 @@ def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
             method = TFS_CG if tag == "cg" else TFS_BICG
             out[tag] = (x, r, sol.solve(method, s.val, x, r, prec, 2000, tol))
     (xa, ra, resa), (xb, rb, resb) = out["cg"], out["literal"]
-    assert np.array_equal(xa, xb) and np.array_equal(ra, rb)
-    assert resa == resb
-    # and the oracle's Bicg equals its Cg
+    if mode == TFS_FP64:
+        assert np.array_equal(xa, xb) and np.array_equal(ra, rb)
+        assert resa == resb
+    # the oracle's Bicg equals its Cg
     ref_b, ref_c = oracle_solve(s, TFS_BICG, prec), oracle_solve(s, TFS_CG, prec)
+    if mode == TFS_MIXED:
+        if ref_b["niter"] <= 2000:
+            assert resa.fin_res < tol and resb.fin_res < tol
+            assert iter_ok(resa.niter, resb.niter)
+            assert rel_l2(xa, xb) < 1e-5
+        else:
+            assert resa.niter == resb.niter == 2001
     assert np.array_equal(ref_b["x"], ref_c["x"]) and ref_b["niter"] == ref_c["niter"]
 
 
