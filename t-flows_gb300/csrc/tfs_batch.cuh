@@ -56,17 +56,27 @@ struct BatchCtl {
 // shared memory, cluster barrier, every thread adds the C partials in rank
 // order.  Two partial slots alternate, so a slot is rewritten only after the
 // next barrier, by which time every reader of its previous contents is done.
-template <int NV>
-__device__ __forceinline__ void cluster_sum(double (&v)[NV], double (*s_part)[4], int &parity,
-                                            cg::cluster_group &cl)
+//
+// AT is the type of the per-thread partials: binary64, or binary32 in the
+// mixed solves, whose warp sums then go through warp_sum_f (compensated
+// binary32, no binary64 instruction per lane).
+template <int NV, typename AT = double>
+__device__ __forceinline__ void cluster_sum(const AT (&in)[NV], double (&v)[NV], double (*s_part)[4],
+                                            int &parity, cg::cluster_group &cl)
 {
     __shared__ double sm[NV][TFS_BATCH_MAX_TPB / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
+        double w;
+        if constexpr (sizeof(AT) == 4) {
+            w = warp_sum_f(in[k]);
+        } else {
+            w = in[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] = v[k] + __shfl_down_sync(FULL, v[k], o);
-        if (lane == 0) sm[k][warp] = v[k];
+            for (int o = 16; o > 0; o >>= 1) w = w + __shfl_down_sync(FULL, w, o);
+        }
+        if (lane == 0) sm[k][warp] = w;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -108,10 +118,20 @@ struct BatchVecs<float> {
 
 // The whole solve of one system by the calling cluster.  VT = double:
 // binary64 with the reference's per-row arithmetic; VT = float: mixed.
+// Per-thread dot-product partial: binary64 fma in the binary64 solves (the
+// values are binary64 already), binary32 fmaf in the mixed ones.
+template <typename AccT, typename VT>
+__device__ __forceinline__ AccT acc_fma(VT a, VT b, AccT c)
+{
+    if constexpr (sizeof(AccT) == 4) return fmaf((float)a, (float)b, c);
+    else return fma((double)a, (double)b, c);
+}
+
 template <int METHOD, typename VT>
 __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_part)[4], int &parity)
 {
     constexpr bool MIXED = sizeof(VT) == 4;
+    using AccT = VT;
     const int C = (int)cl.num_blocks();
     const int stride = C * (int)blockDim.x;
     const int gtid = (int)cl.block_rank() * (int)blockDim.x + (int)threadIdx.x;
@@ -145,8 +165,9 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         if (MIXED) { F.d[i] = (float)di; F.e[i] = 0.f; }
     }
     {
-        double v1[1] = {acc[0]};
-        cluster_sum<1>(v1, s_part, parity, cl);
+        const double a1[1] = {acc[0]};
+        double v1[1];
+        cluster_sum<1>(a1, v1, s_part, parity, cl);
         double bnrm2 = sqrt(v1[0]);
         if (bnrm2 < tol) {
             // Early exit 1: x, r1 untouched, ini_res untouched (Cg.f90:55-58).
@@ -181,8 +202,9 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
     };
     double e2, rz;
     true_residual(true, e2, rz);
-    double v2[2] = {e2, rz};
-    cluster_sum<2>(v2, s_part, parity, cl);
+    const double a2[2] = {e2, rz};
+    double v2[2];
+    cluster_sum<2>(a2, v2, s_part, parity, cl);
     double err = sqrt(v2[0]);
     double ini = err, rho = v2[1], rho_old = 0.0, r_true = err;
     int true_res = 1, status = TFS_OK, niter_out = 0, early = 0;
@@ -214,7 +236,7 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         }
         cl.sync();
         // q = A p and alpha (Cg.f90:128-153 / Bicg.f90:136-165).
-        double pq = 0.0;
+        AccT pq = (AccT)0;
         if (METHOD == 1) {
             for (int i = gtid; i < n_int; i += stride) {
                 RowGeom g = row_geom(A, i);
@@ -222,7 +244,7 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                 row_accum2<false, VT, VT, VT>(s1, s2, A.col, valT, W.p, W.p2, g.off, 0, g.len);
                 W.q[i] = s1;
                 W.q2[i] = s2;
-                pq = fma((double)W.p2[i], (double)s1, pq);
+                pq = acc_fma(W.p2[i], s1, pq);
             }
         } else {
             // Four rows per thread and step, all loads before any store.
@@ -242,17 +264,17 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                 for (int q = 0; q < 4; q++)
                     if (ii[q] < n_int) {
                         W.q[ii[q]] = sv[q];
-                        pq = fma((double)W.p[ii[q]], (double)sv[q], pq);
+                        pq = acc_fma(W.p[ii[q]], sv[q], pq);
                     }
             }
         }
-        double v1[1] = {pq};
-        cluster_sum<1>(v1, s_part, parity, cl);
+        const AccT a1[1] = {pq};
+        double v1[1];
+        cluster_sum<1, AccT>(a1, v1, s_part, parity, cl);
         const double alfa = rho / v1[0];
         const VT alfaT = (VT)alfa;
         // x (or e) += alpha p, r -= alpha q, z = M^-1 r, ||r||, next rho.
-        e2 = 0.0;
-        rz = 0.0;
+        AccT e2a = (AccT)0, rza = (AccT)0;
         if (METHOD == 1) {
             for (int i = gtid; i < n_int; i += stride) {
                 if (MIXED) F.e[i] = fmaf((float)alfaT, (float)W.p[i], F.e[i]);
@@ -262,11 +284,11 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                 VT dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
                 VT z1 = r1 / dT;
                 W.z[i] = z1;
-                e2 = fma((double)r1, (double)r1, e2);
+                e2a = acc_fma(r1, r1, e2a);
                 VT r2 = W.r2[i] - alfaT * W.q2[i];
                 W.r2[i] = r2;
                 W.z2[i] = r2 / dT;
-                rz = fma((double)z1, (double)r2, rz);
+                rza = acc_fma(z1, r2, rza);
             }
         } else {
             for (int i0 = gtid; i0 < n_int; i0 += 4 * stride) {
@@ -292,13 +314,14 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                     W.r[i] = r1;
                     VT z1 = r1 / dv[q];
                     W.z[i] = z1;
-                    e2 = fma((double)r1, (double)r1, e2);
-                    rz = fma((double)r1, (double)z1, rz);
+                    e2a = acc_fma(r1, r1, e2a);
+                    rza = acc_fma(r1, z1, rza);
                 }
             }
         }
-        double v3[2] = {e2, rz};
-        cluster_sum<2>(v3, s_part, parity, cl);
+        const AccT a3[2] = {e2a, rza};
+        double v3[2];
+        cluster_sum<2, AccT>(a3, v3, s_part, parity, cl);
         double est = sqrt(v3[0]);
         double rho_next = v3[1];
         bool need_true = MIXED && (!(est <= DBL_MAX) || est < tol || est < 0.1 * r_true || iter >= niter_max);
@@ -309,8 +332,9 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
             }
             cl.sync();
             true_residual(false, e2, rz);
-            double v4[2] = {e2, rz};
-            cluster_sum<2>(v4, s_part, parity, cl);
+            const double a4[2] = {e2, rz};
+            double v4[2];
+            cluster_sum<2>(a4, v4, s_part, parity, cl);
             est = sqrt(v4[0]);
             rho_next = v4[1];
             r_true = est;

@@ -22,6 +22,7 @@
 #include "tfs_internal.h"
 #include "tfs_kernels.cuh"
 #include "tfs_mixed.cuh"
+#include "tfs_dic.cuh"
 
 using namespace tfs;
 
@@ -103,10 +104,11 @@ static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int b
 // block; MODE 1 runs the tail first and the levels in descending order.
 template <typename T, int NR, int MODE>
 static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, const T *b1, const T *b2,
-                         T *o1, T *o2, const T *y1, const T *y2, int *count, bool with_tail = true)
+                         T *o1, T *o2, const T *y1, const T *y2, int *count, bool with_tail = true,
+                         int tail_at = -1)
 {
     SellDev A = sell_of(h);
-    const int L = h->n_levels, tail = h->tail_level;
+    const int L = h->n_levels, tail = tail_at >= 0 ? tail_at : h->tail_level;
     const bool pdl = h->use_pdl != 0;
     int first = 1;
     auto tail_launch = [&]() -> cudaError_t {
@@ -497,6 +499,48 @@ static int build_layout(tfs_handle *h, int kind)
         while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= TFS_TAIL_ROWS) tail--;
         if (tail == 0) tail = nl > 1 ? 1 : nl;   // level 0 always runs as tiles
         h->tail_level = tail;
+        // A cluster tail of the per-level sweeps takes levels of up to
+        // C x TFS_SWEEP_TPB rows (C CTAs of one cluster), if such a cluster
+        // can be resident; else the single-block tail is used.
+        h->tail_cluster = 1;
+        {
+            // Default 1: on the 128^3 system the 8- and 16-CTA cluster tails
+            // (156 and 157 us per application) were slower than one block
+            // (144 us); TFS_TAIL_CLUSTER selects 2, 4, 8 or 16.
+            int C = 1;
+            const char *env = getenv("TFS_TAIL_CLUSTER");
+            if (env) C = atoi(env);
+            if (C != 1 && C != 2 && C != 4 && C != 8 && C != 16) C = 1;
+            if (C > 1) {
+                auto kc = k_sweep_tailc<double, 2>;
+                if (C > 8) cudaFuncSetAttribute(kc, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                auto kf = k_sweep_tailc<float, 2>;
+                if (C > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                auto kd1 = k_sweep_tailc<double, 1>;
+                if (C > 8) cudaFuncSetAttribute(kd1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                auto kf1 = k_sweep_tailc<float, 1>;
+                if (C > 8) cudaFuncSetAttribute(kf1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                cudaLaunchConfig_t cfg = {};
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = (unsigned)C;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.gridDim = dim3((unsigned)C);
+                cfg.blockDim = dim3(TFS_SWEEP_TPB);
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int ncl = 0;
+                if (cudaOccupancyMaxActiveClusters(&ncl, kc, &cfg) != cudaSuccess || ncl < 1) {
+                    cudaGetLastError();
+                    C = 1;
+                }
+            }
+            h->tail_cluster = C;
+            int ct = nl;
+            while (ct > 0 && h->lvl_begin[ct] - h->lvl_begin[ct - 1] <= C * TFS_SWEEP_TPB) ct--;
+            h->ctail_level = ct;
+        }
         std::vector<int2> tiles;
         std::vector<int> lvl_tiles(nl, 0);
         for (int l = 0; l < tail; l++)
@@ -632,6 +676,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream);
     const char *env = getenv("TFS_SWEEP");
     if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
+    if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
+    if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
     env = getenv("TFS_PDL");
     if (env && strcmp(env, "0") == 0) h->use_pdl = 0;
     env = getenv("TFS_GRAPH");
@@ -712,11 +758,64 @@ static int launch_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
 
 // Forward and backward level sweeps: z = M^-1 b for NR right-hand sides, in
 // binary64 (val, d of the handle) or binary32 (val32, d32).
+// One cooperative launch of k_dic_apply: z = M^-1 b through y, and with
+// FUSE rho = (b, z), p = z + beta p.  The grid is the co-resident maximum,
+// capped at the blocks the largest swept level needs.
+template <typename T, int R, bool FUSE>
+static cudaError_t launch_dic_k(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *p)
+{
+    auto kernel = k_dic_apply<T, R, FUSE>;
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, TFS_DIC_TPB, 0);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    const int big = h->tail_level;
+    int widest = 0;
+    for (int l = 0; l < big; l++) widest = std::max(widest, h->lvl_begin[l + 1] - h->lvl_begin[l]);
+    int need = (widest + R * TFS_DIC_TPB - 1) / (R * TFS_DIC_TPB);
+    int G = std::min(occ * h->sm_count, std::max(need, 1));
+    G = std::min(G, h->n_chunks);   // one partial per block fits h->part
+    const T *val;
+    const T *d;
+    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
+    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3((unsigned)G);
+    cfg.blockDim = dim3(TFS_DIC_TPB);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, sell_of(h), val, d, b, y, z, p, (const int *)h->d_lvl_begin,
+                              big, h->n_levels, h->n_int, h->st, h->part);
+}
+
+// Rows per thread of the cooperative sweep: 2 when one row per thread of
+// the co-resident grid does not cover the widest level.
+template <typename T, bool FUSE>
+static int launch_dic(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *p, int *count)
+{
+    if (h->dic_r == 0) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_dic_apply<T, 1, FUSE>, TFS_DIC_TPB, 0);
+        int widest = 0;
+        for (int l = 0; l < h->tail_level; l++) widest = std::max(widest, h->lvl_begin[l + 1] - h->lvl_begin[l]);
+        h->dic_r = (int64_t)occ * h->sm_count * TFS_DIC_TPB >= widest ? 1 : 2;
+    }
+    cudaError_t e = h->dic_r == 1 ? launch_dic_k<T, 1, FUSE>(h, s, b, y, z, p)
+                                  : launch_dic_k<T, 2, FUSE>(h, s, b, y, z, p);
+    (*count)++;
+    return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "cooperative DIC launch");
+}
+
 template <typename T>
 static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, const T *b2,
                          T *y1, T *y2, T *z1, T *z2, int *count)
 {
     SellDev A = sell_of(h);
+    if (h->sweep_mode == 2 && nr == 1) return launch_dic<T, false>(h, s, b1, y1, z1, nullptr, count);
     const int T_ = TFS_TPB;
     const T *val;
     T *d;
@@ -736,24 +835,45 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         CKL("sweep launch");
         return TFS_OK;
     }
-    // Forward levels, both tails in one block, backward levels.
+    // Forward levels, both tails in one block or one cluster, backward levels.
     int rc;
-    const bool tails = h->tail_level < h->n_levels;
-    auto tail2 = [&](auto kernel) -> int {
+    const int C = h->tail_cluster;
+    const int tail_at = C > 1 ? h->ctail_level : h->tail_level;
+    const bool tails = tail_at < h->n_levels;
+    auto tail2 = [&](auto kernel, auto kernel_c) -> int {
         if (!tails) return TFS_OK;
-        cudaError_t e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
-                                  z2, (const int *)h->d_lvl_begin, h->tail_level, h->n_levels, h->st);
+        cudaError_t e;
+        if (C > 1) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[2];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)C;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[1].val.programmaticStreamSerializationAllowed = 1;
+            cfg.gridDim = dim3((unsigned)C);
+            cfg.blockDim = dim3(TFS_SWEEP_TPB);
+            cfg.stream = s;
+            cfg.attrs = attr;
+            cfg.numAttrs = h->use_pdl ? 2 : 1;
+            e = cudaLaunchKernelEx(&cfg, kernel_c, A, val, d, b1, b2, y1, y2, z1, z2,
+                                   (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+        } else {
+            e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
+                          z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+        }
         (*count)++;
         return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
     };
     if (nr == 1) {
-        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false))) return rc;
-        if ((rc = tail2(k_sweep_tail2<T, 1>))) return rc;
-        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false))) return rc;
+        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
+        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at))) return rc;
     } else {
-        if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false))) return rc;
-        if ((rc = tail2(k_sweep_tail2<T, 2>))) return rc;
-        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false))) return rc;
+        if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 2>, k_sweep_tailc<T, 2>))) return rc;
+        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at))) return rc;
     }
     return TFS_OK;
 }
@@ -787,7 +907,14 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     *count = 0;
     if (method == TFS_CG) {
         const int n4 = h->n_int / 4, G4 = h->grid_vec4;
-        if (!h->vec4 && prec == 2) {
+        if (h->sweep_mode == 2 && prec == 2) {
+            if ((rc = launch_dic<float, true>(h, s, F.r, F.y, F.z, F.p, count))) return rc;
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
+            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 4;
+        } else if (!h->vec4 && prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
             k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
             k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
@@ -882,7 +1009,12 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     int rc;
     *count = 0;
     if (method == TFS_CG) {
-        if (prec == 2) {
+        if (prec == 2 && h->sweep_mode == 2) {
+            if ((rc = launch_dic<double, true>(h, s, V.r, V.y, V.z, V.p, count))) return rc;
+            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            *count += 2;
+        } else if (prec == 2) {
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
             k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
@@ -1034,6 +1166,12 @@ static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
     if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
     GraphEntry ge;
     int rc = build_graph(h, method, prec, ge);
+    if (rc && h->sweep_mode == 2 && prec == 2) {
+        // A driver that cannot capture a cooperative launch inside a
+        // conditional body gets the per-level schedule instead.
+        h->sweep_mode = 0;
+        rc = build_graph(h, method, prec, ge);
+    }
     if (rc && h->use_pdl) {
         // A driver that cannot keep programmatic edges inside a conditional
         // body gets plain stream-ordered level launches instead.

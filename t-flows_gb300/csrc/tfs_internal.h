@@ -49,6 +49,13 @@ struct DevState {
     double delta;        // reliable-update threshold
     int need_true;       // the next true-residual step must run
     int pad1;
+    // beta (above) = rho / rho_old of the coming p update (Cg.f90:114-119)
+    // and its binary32 rounding, computed once by the thread that finalises
+    // rho instead of by every thread
+    float beta32;
+    int pad3;
+    // grid barrier of the cooperative DIC kernel (zeroed with the state)
+    unsigned int bar_count, bar_gen, bar_abort, pad2;
 };
 
 // Control words of the single-launch level sweeps, one set per sweep kind
@@ -109,8 +116,9 @@ struct tfs_handle {
     int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels
     int vec4 = 1;                      // 1: binary32 CG vector kernels with 16-byte loads
     int sweep_grid = 0;                // blocks of the dataflow sweeps
-    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch
+    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative
     int use_pdl = 1;                   // programmatic dependent launch between level kernels
+    int dic_r = 0;                     // rows per thread of the cooperative sweep (0: not chosen yet)
     int eager = 0;                     // 1: launch kernels directly, no CUDA graph
     int bicg_literal = 0;              // 1: BiCG runs its shadow sequence explicitly
     int precision = TFS_FP64;
@@ -133,6 +141,7 @@ struct tfs_handle {
     int2 *tiles = nullptr;             // (first row, level) per sweep tile
     int *d_lvl_begin = nullptr, *d_lvl_tiles = nullptr;
     int n_tiles = 0, tail_level = 0;
+    int tail_cluster = 1, ctail_level = 0;   // CTAs of the sweep tail's cluster, its first level
     SweepCtl *ctl = nullptr;
     DevState *st = nullptr;
     DevParams *params = nullptr;

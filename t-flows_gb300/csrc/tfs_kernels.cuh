@@ -11,6 +11,7 @@
 // a solve is bitwise reproducible from run to run.
 #pragma once
 #include <cfloat>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "tfs_internal.h"
@@ -132,16 +133,58 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sm)[TFS_TPB 
     }
 }
 
-// Single-pass grid reduction: every block publishes one partial per value,
-// the last block to arrive sums the partials in block order.  Returns true
-// in thread 0 of that last block, with the totals in v.
-template <int NV>
-__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict__ part,
-                                            unsigned int *counter)
+// Sum over a warp of binary32 values, returned in binary64 by lane 0.  The
+// running sum is a binary32 pair (hi, lo) updated with Knuth's TwoSum, so it
+// carries about 48 significant bits without any binary64 instruction per
+// lane (GB300's binary64 pipe is narrow: a binary64 shuffle reduction of
+// every thread's partial kept it half busy in the binary32 vector kernels).
+__device__ __forceinline__ double warp_sum_f(float v)
 {
-    __shared__ double sm[NV][TFS_TPB / 32];
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(FULL, hi, o), l2 = __shfl_down_sync(FULL, lo, o);
+        const float s = hi + h2;
+        const float bp = s - hi;
+        const float e = (hi - (s - bp)) + (h2 - bp);
+        hi = s;
+        lo = (lo + l2) + e;
+    }
+    return (double)hi + (double)lo;
+}
+
+// Block sum of NV binary32 values; the binary64 result is valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[NV],
+                                            double (*sm)[TFS_TPB / 32])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const double w = warp_sum_f(v[k]);
+        if (lane == 0) sm[k][warp] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = sm[k][0];
+#pragma unroll
+            for (int w = 1; w < TFS_TPB / 32; w++) s = s + sm[k][w];
+            out[k] = s;
+        }
+    }
+}
+
+// Second half of a single-pass grid reduction: thread 0 of every block
+// publishes its block totals v, the last block to arrive sums the partials
+// in block order.  Returns true in thread 0 of that last block, with the
+// totals in v.
+template <int NV>
+__device__ __forceinline__ bool grid_publish(double (&v)[NV], double *__restrict__ part,
+                                             unsigned int *counter, double (*sm)[TFS_TPB / 32])
+{
     __shared__ unsigned int is_last;
-    block_sum<NV>(v, sm);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NV; k++) part[k * gridDim.x + blockIdx.x] = v[k];
@@ -169,6 +212,28 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict_
     return false;
 }
 
+// Single-pass grid reduction of binary64 values (warp shuffles, then one
+// partial per block, then the last block sums the partials in block order).
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict__ part,
+                                            unsigned int *counter)
+{
+    __shared__ double sm[NV][TFS_TPB / 32];
+    block_sum<NV>(v, sm);
+    return grid_publish<NV>(v, part, counter, sm);
+}
+
+// The same for binary32 per-thread values (binary64 from the warp sums on).
+// Returns true in thread 0 of the last block, with the totals in out.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce_f(const float (&v)[NV], double (&out)[NV],
+                                              double *__restrict__ part, unsigned int *counter)
+{
+    __shared__ double sm[NV][TFS_TPB / 32];
+    block_sum_f<NV>(v, out, sm);
+    return grid_publish<NV>(out, part, counter, sm);
+}
+
 // Row loops of the vector kernels: four chunks per step, with every load of
 // the four rows issued before any of them is used (memory-level parallelism;
 // the stores of one row could otherwise alias the loads of the next).
@@ -189,6 +254,16 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *__restrict_
 __device__ __forceinline__ void set_cond(cudaGraphConditionalHandle cond, unsigned v)
 {
     if (cond) cudaGraphSetConditional(cond, v);
+}
+
+// beta = rho / rho_old for the coming p update, once per iteration (a
+// binary64 division is a long instruction sequence on GB300's narrow
+// binary64 pipe; every thread dividing cost several microseconds).
+__device__ __forceinline__ void publish_beta(DevState *st)
+{
+    const double b = st->rho / st->rho_old;
+    st->beta = b;
+    st->beta32 = (float)b;
 }
 
 // Convergence test and bookkeeping at the end of one iteration, run by one
@@ -213,7 +288,10 @@ __device__ __forceinline__ void finish_iteration(DevState *st, double e2, double
     } else {
         st->iter = it + 1;
         st->rho_old = st->rho;               // Cg.f90:176
-        if (fused_rho) st->rho = rho_next;
+        if (fused_rho) {
+            st->rho = rho_next;
+            publish_beta(st);
+        }
     }
     st->loops = st->loops + 1;
     if (!st->done && st->loops >= st->loop_limit) {
@@ -471,15 +549,18 @@ __device__ __noinline__ void wait_count(const unsigned long long *cnt, unsigned 
 
 // One row of a sweep.  MODE 0: forward y = (b - L y) * D; MODE 1: backward
 // z = (y/(D+TINY) - U z) * D; MODE 2: DIC form D_i = 1/(a_ii - sum D_k a^2).
-// The first NP entries may come prefetched in kk/aa.
+// The first NP entries may come prefetched in kk/aa.  With skip (a finished
+// solve) nothing is stored; the flag is tested only before the stores, so
+// reading it does not delay the row's loads.
 template <typename T, int NR, int MODE, int NP>
 __device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict__ val, T *d,
                                           const T *b1, const T *b2, T *o1, T *o2, const T *y1,
                                           const T *y2, int i, const RowGeom &g, const int *kk,
-                                          const T *aa)
+                                          const T *aa, bool skip = false)
 {
     const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
     if (g.len == 0) {
+        if (skip) return;
         if (MODE == 2) d[i] = (T)1;
         else { o1[i] = (T)0; if (NR == 2) o2[i] = (T)0; }
         return;
@@ -517,6 +598,7 @@ __device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict_
             if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
         }
     }
+    if (skip) return;
     if (MODE == 2) { d[i] = (T)1 / s1; return; }
     o1[i] = s1 * di;
     if (NR == 2) o2[i] = s2 * di;
@@ -645,9 +727,9 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     }
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
-    if (st->done) return;
+    const bool skip = st->done != 0;
     if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa);
+    if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
 }
 
 // Levels [l_begin, l_end) of a sweep in one block (descending for MODE 1);
@@ -711,14 +793,14 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
 {
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
-    if (st->done) return;
+    const bool skip = st->done != 0;
     const int nl = l_end - l_begin;
     for (int q = 0; q < nl; q++) {
         const int lev = l_begin + q;
         const int r1 = __ldg(lvl_begin + lev + 1);
         for (int i = __ldg(lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
             RowGeom g = row_geom(A, i);
-            sweep_row<T, NR, 0, 0>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, i, g, nullptr, nullptr);
+            sweep_row<T, NR, 0, 0>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, i, g, nullptr, nullptr, skip);
         }
         __syncthreads();
     }
@@ -727,9 +809,44 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
         const int r1 = __ldg(lvl_begin + lev + 1);
         for (int i = __ldg(lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
             RowGeom g = row_geom(A, i);
-            sweep_row<T, NR, 1, 0>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, i, g, nullptr, nullptr);
+            sweep_row<T, NR, 1, 0>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, i, g, nullptr, nullptr, skip);
         }
         __syncthreads();
+    }
+}
+
+// Both tails by one thread-block cluster of C CTAs (C x TFS_SWEEP_TPB
+// threads): levels [l_begin, l_end) forward, then backward, one row per
+// thread and pass, the hardware cluster barrier between levels (release /
+// acquire at cluster scope: every CTA sees the rows the others wrote).  With
+// C CTAs the tail can take levels of up to C x 1024 rows, so fewer levels
+// need a launch of their own.
+template <typename T, int NR>
+__global__ void __launch_bounds__(TFS_SWEEP_TPB)
+k_sweep_tailc(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
+              T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
+{
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    if (st->done) return;
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    const int t = (int)cl.block_rank() * TFS_SWEEP_TPB + (int)threadIdx.x;
+    const int stride = (int)cl.num_blocks() * TFS_SWEEP_TPB;
+    for (int lev = l_begin; lev < l_end; lev++) {
+        const int r1 = __ldg(lvl_begin + lev + 1);
+        for (int i = __ldg(lvl_begin + lev) + t; i < r1; i += stride) {
+            RowGeom g = row_geom(A, i);
+            sweep_row<T, NR, 0, 0>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, i, g, nullptr, nullptr);
+        }
+        cl.sync();
+    }
+    for (int lev = l_end - 1; lev >= l_begin; lev--) {
+        const int r1 = __ldg(lvl_begin + lev + 1);
+        for (int i = __ldg(lvl_begin + lev) + t; i < r1; i += stride) {
+            RowGeom g = row_geom(A, i);
+            sweep_row<T, NR, 1, 0>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, i, g, nullptr, nullptr);
+        }
+        if (lev > l_begin) cl.sync();
     }
 }
 
@@ -738,20 +855,25 @@ template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)
 k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
 {
-    if (st->done) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->sweep_ns += gtimer() - st->t_sweep0;
-        st->sweep_n += 1;
-    }
+    const bool stop = st->done != 0;
     double acc = 0.0;
     TFS_QUAD_BEGIN(n_chunks)
         double a[4], b[4];
         TFS_QLOAD(a, METHOD == 0 ? V.r : V.z);
         TFS_QLOAD(b, METHOD == 0 ? V.z : V.r2);
+        if (stop) return;
         TFS_QUAD_FOR acc = fma(a[_q], b[_q], acc);
     TFS_QUAD_END
+    if (stop) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
+    }
     double v[1] = {acc};
-    if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
+    if (grid_reduce<1>(v, part, &st->counter)) {
+        st->rho = v[0];
+        if (st->iter > 1) publish_beta(st);
+    }
 }
 
 // ---------------------------------------------------------------- CG body
@@ -761,14 +883,15 @@ k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
 template <bool FROMZ>
 __global__ void __launch_bounds__(TFS_TPB) k_cg_p(int n_chunks, Vec64 V, const DevState *st)
 {
-    if (st->done) return;
+    const bool stop = st->done != 0;
     const int it = st->iter;
-    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    const double beta = st->beta;            // rho / rho_old, published once
     TFS_QUAD_BEGIN(n_chunks)
         double z[4], p[4];
         if (FROMZ) { TFS_QLOAD(z, V.z); }
         else { double r[4], d[4]; TFS_QLOAD(r, V.r); TFS_QLOAD(d, V.d); TFS_QUAD_FOR z[_q] = r[_q] / d[_q]; }
         TFS_QLOAD(p, V.p);
+        if (stop) return;
         TFS_QUAD_FOR V.p[_i[_q]] = it == 1 ? z[_q] : z[_q] + beta * p[_q];
     TFS_QUAD_END
 }
@@ -779,16 +902,21 @@ __global__ void __launch_bounds__(TFS_TPB)
 k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ p,
           double *__restrict__ q, DevState *st, double *part)
 {
-    if (st->done) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    // The finished-solve flag is tested after the first row's loads are
+    // issued (here and in the other per-iteration kernels), so that its
+    // load does not delay them.
+    const bool stop = st->done != 0;
+    if (!stop && blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
     double acc = 0.0;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
         double s = row_accum<false, double, double, double, TFS_SPMV_NC>(0.0, A.col, val, p, g.off, 0, g.len);
+        if (stop) return;
         q[i] = s;
         acc = fma(p[i], s, acc);
     }
+    if (stop) return;
     double v[1] = {acc};
     if (grid_reduce<1>(v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
@@ -803,16 +931,14 @@ template <bool FUSED>
 __global__ void __launch_bounds__(TFS_TPB)
 k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond)
 {
-    if (st->done) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
-        return;
-    }
+    const bool stop = st->done != 0;
     const double alfa = st->alpha;
     double e2 = 0.0, rz = 0.0;
     TFS_QUAD_BEGIN(n_chunks)
         double x[4], p[4], r[4], q[4], d[4];
         TFS_QLOAD(x, V.x); TFS_QLOAD(p, V.p); TFS_QLOAD(r, V.r); TFS_QLOAD(q, V.q);
         if (FUSED) { TFS_QLOAD(d, V.d); }
+        if (stop) break;
         TFS_QUAD_FOR {
             const int i = _i[_q];
             V.x[i] = x[_q] + alfa * p[_q];
@@ -822,6 +948,10 @@ k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditio
             if (FUSED) { double z = rn / d[_q]; V.z[i] = z; rz = fma(rn, z, rz); }
         }
     TFS_QUAD_END
+    if (stop) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
+        return;
+    }
     double v[2] = {e2, rz};
     if (grid_reduce<2>(v, part, &st->counter)) finish_iteration(st, v[0], v[1], FUSED, cond);
 }
@@ -833,7 +963,7 @@ __global__ void __launch_bounds__(TFS_TPB) k_bicg_p(int n_chunks, Vec64 V, const
 {
     if (st->done) return;
     const int it = st->iter;
-    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    const double beta = it == 1 ? 0.0 : st->beta;
     TFS_QUAD_BEGIN(n_chunks)
         double z1[4], z2[4], p1[4], p2[4];
         if (FROMZ) { TFS_QLOAD(z1, V.z); TFS_QLOAD(z2, V.z2); }
@@ -922,7 +1052,7 @@ __global__ void __launch_bounds__(TFS_TPB) k_cgs_u(int n_chunks, Vec64 V, const 
 {
     if (st->done) return;
     const int it = st->iter;
-    const double beta = it == 1 ? 0.0 : st->rho / st->rho_old;
+    const double beta = it == 1 ? 0.0 : st->beta;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         double u1, u2;

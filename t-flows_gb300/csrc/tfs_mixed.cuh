@@ -3,10 +3,12 @@
 // The Krylov recurrences run on binary32 matrix values and binary32 vectors
 // (r, p, q, z, ...), which cuts the bytes per iteration by about a third.
 // Binary64 is kept where the accuracy is decided:
-//   - every dot product (rho, (p,q), ||r||) is reduced in binary64 across
-//     threads and blocks; a thread first sums its own few rows (about 7 for
-//     a 2M-row system) in binary32 -- GB300's binary64 pipe is narrow, and
-//     per-element conversions to binary64 made these kernels FP64-bound;
+//   - every dot product (rho, (p,q), ||r||) is summed in binary32 over a
+//     thread's own few rows (about 7 for a 2M-row system), over the 32 lanes
+//     of a warp as a compensated binary32 pair (TwoSum, about 48 bits), and
+//     in binary64 across warps and blocks -- GB300's binary64 pipe is narrow,
+//     and binary64 conversions and shuffles per thread made these kernels
+//     FP64-bound;
 //   - alpha and beta are binary64 scalars;
 //   - the solution x is binary64: the binary32 corrections alpha * p are
 //     summed in a binary32 vector e, which is added to x in binary64 (and
@@ -152,8 +154,12 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho(int n_chunks, Vec32 F, D
         TFS_QLOAD(b, METHOD == 0 ? F.z : F.r2);
         TFS_QUAD_FOR acc = fmaf(a[_q], b[_q], acc);
     TFS_QUAD_END
-    double v[1] = {(double)acc};
-    if (grid_reduce<1>(v, part, &st->counter)) st->rho = v[0];
+    const float av[1] = {acc};
+    double v[1];
+    if (grid_reduce_f<1>(av, v, part, &st->counter)) {
+        st->rho = v[0];
+        if (st->iter > 1) publish_beta(st);
+    }
 }
 
 // ---------------------------------------------------------------- CG
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p(int n_chunks, Vec32 F, cons
 {
     if (st->done || st->need_true) return;
     const int it = st->iter;
-    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    const float beta = it == 1 ? 0.f : st->beta32;
     TFS_QUAD_BEGIN(n_chunks)
         float z[4], p[4];
         if (FROMZ) { TFS_QLOAD(z, F.z); }
@@ -178,18 +184,24 @@ __global__ void __launch_bounds__(TFS_TPB)
 k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__ p,
              float *__restrict__ q, DevState *st, double *part)
 {
-    if (st->done || st->need_true) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
+    // The skip flags are tested after the first row's loads are issued (here
+    // and in the other per-iteration kernels), so that reading them does not
+    // delay those loads.
+    const bool stop = (st->done | st->need_true) != 0;
+    if (!stop && blockIdx.x == 0 && threadIdx.x == 0) st->t_spmv0 = gtimer();
     float acc = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         RowGeom g = row_geom(A, i);
         float s = row_accum<false, float, float, float, TFS_SPMV_NC>(0.f, A.col, val, p, g.off, 0, g.len);
+        if (stop) return;
         q[i] = s;
         acc = fmaf(p[i], s, acc);
     }
-    double v[1] = {(double)acc};
-    if (grid_reduce<1>(v, part, &st->counter)) {
+    if (stop) return;
+    const float a1[1] = {acc};
+    double v[1];
+    if (grid_reduce_f<1>(a1, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
@@ -217,8 +229,9 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
             if (FUSED) { float z = rn / d[_q]; F.z[i] = z; rz = fmaf(rn, z, rz); }
         }
     TFS_QUAD_END
-    double v[2] = {(double)e2, (double)rz};
-    if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
+    const float av[2] = {e2, rz};
+    double v[2];
+    if (grid_reduce_f<2>(av, v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
 
 // ---------------------------------------------------- CG, four rows per thread
@@ -232,13 +245,14 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p4(int n4, Vec32 F, const DevState *st)
 {
-    if (st->done || st->need_true) return;
+    const bool stop = (st->done | st->need_true) != 0;
     const int it = st->iter;
-    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    const float beta = st->beta32;           // (float)(rho / rho_old), published once
     const float4 *z4 = (const float4 *)F.z;
     float4 *p4 = (float4 *)F.p;
     for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
         float4 z = z4[v], p = p4[v];
+        if (stop) return;
         if (it == 1) p4[v] = z;
         else p4[v] = make_float4(fmaf(beta, p.x, z.x), fmaf(beta, p.y, z.y), fmaf(beta, p.z, z.z), fmaf(beta, p.w, z.w));
     }
@@ -246,32 +260,40 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p4(int n4, Vec32 F, const Dev
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho4(int n4, Vec32 F, DevState *st, double *part)
 {
-    if (st->done || st->need_true) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->sweep_ns += gtimer() - st->t_sweep0;
-        st->sweep_n += 1;
-    }
+    const bool stop = (st->done | st->need_true) != 0;
     const float4 *r4 = (const float4 *)F.r, *z4 = (const float4 *)F.z;
     float acc = 0.f;
     for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
         float4 r = r4[v], z = z4[v];
+        if (stop) return;
         acc = fmaf(r.x, z.x, acc); acc = fmaf(r.y, z.y, acc); acc = fmaf(r.z, z.z, acc); acc = fmaf(r.w, z.w, acc);
     }
-    double v1[1] = {(double)acc};
-    if (grid_reduce<1>(v1, part, &st->counter)) st->rho = v1[0];
+    if (stop) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
+    }
+    const float a1[1] = {acc};
+    double v1[1];
+    if (grid_reduce_f<1>(a1, v1, part, &st->counter)) {
+        st->rho = v1[0];
+        if (st->iter > 1) publish_beta(st);
+    }
 }
 
 template <bool FUSED>
 __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part)
 {
-    if (st->done || st->need_true) return;
-    const float a = (float)st->alpha;
+    const bool stop = (st->done | st->need_true) != 0;
+    const double alpha = st->alpha;
     const float4 *p4 = (const float4 *)F.p, *q4 = (const float4 *)F.q, *d4 = (const float4 *)F.d;
     float4 *e4 = (float4 *)F.e, *r4 = (float4 *)F.r, *zz4 = (float4 *)F.z;
     float e2 = 0.f, rz = 0.f;
     for (int v = blockIdx.x * TFS_TPB + threadIdx.x; v < n4; v += gridDim.x * TFS_TPB) {
         float4 p = p4[v], q = q4[v], r = r4[v], e = e4[v], d;
         if (FUSED) d = d4[v];
+        if (stop) return;
+        const float a = (float)alpha;
         e4[v] = make_float4(fmaf(a, p.x, e.x), fmaf(a, p.y, e.y), fmaf(a, p.z, e.z), fmaf(a, p.w, e.w));
         r = make_float4(fmaf(-a, q.x, r.x), fmaf(-a, q.y, r.y), fmaf(-a, q.z, r.z), fmaf(-a, q.w, r.w));
         r4[v] = r;
@@ -282,8 +304,10 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevS
             rz = fmaf(r.x, z.x, rz); rz = fmaf(r.y, z.y, rz); rz = fmaf(r.z, z.z, rz); rz = fmaf(r.w, z.w, rz);
         }
     }
-    double v2[2] = {(double)e2, (double)rz};
-    if (grid_reduce<2>(v2, part, &st->counter)) mx_end_iteration(st, v2[0], v2[1], FUSED);
+    if (stop) return;
+    const float a2[2] = {e2, rz};
+    double v2[2];
+    if (grid_reduce_f<2>(a2, v2, part, &st->counter)) mx_end_iteration(st, v2[0], v2[1], FUSED);
 }
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_fold4(int n4, Vec64 V, Vec32 F, const DevState *st)
@@ -308,7 +332,7 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_bicg_p(int n_chunks, Vec32 F, co
 {
     if (st->done || st->need_true) return;
     const int it = st->iter;
-    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    const float beta = it == 1 ? 0.f : st->beta32;
     TFS_QUAD_BEGIN(n_chunks)
         float z1[4], z2[4], p1[4], p2[4];
         if (FROMZ) { TFS_QLOAD(z1, F.z); TFS_QLOAD(z2, F.z2); }
@@ -341,8 +365,9 @@ k_mx_spmv2_pq(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, d
         F.q2[i] = s2;
         acc = fmaf(F.p2[i], s1, acc);
     }
-    double v[1] = {(double)acc};
-    if (grid_reduce<1>(v, part, &st->counter)) {
+    const float av[1] = {acc};
+    double v[1];
+    if (grid_reduce_f<1>(av, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
@@ -378,8 +403,9 @@ k_mx_bicg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
             }
         }
     TFS_QUAD_END
-    double v[2] = {(double)e2, (double)rz};
-    if (grid_reduce<2>(v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
+    const float av[2] = {e2, rz};
+    double v[2];
+    if (grid_reduce_f<2>(av, v, part, &st->counter)) mx_end_iteration(st, v[0], v[1], FUSED);
 }
 
 // --------------------------------------------------------------- CGS
@@ -389,7 +415,7 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cgs_u(int n_chunks, Vec32 F, con
 {
     if (st->done || st->need_true) return;
     const int it = st->iter;
-    const float beta = it == 1 ? 0.f : (float)(st->rho / st->rho_old);
+    const float beta = it == 1 ? 0.f : st->beta32;
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
         float u1, u2;
@@ -418,8 +444,9 @@ k_mx_spmv_v(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, dou
         F.v2[i] = s;
         acc = fmaf(F.r2[i], s, acc);
     }
-    double v[1] = {(double)acc};
-    if (grid_reduce<1>(v, part, &st->counter)) {
+    const float av[1] = {acc};
+    double v[1];
+    if (grid_reduce_f<1>(av, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
@@ -461,8 +488,9 @@ k_mx_cgs_spmv_r(SellDev A, const float *__restrict__ val, Vec64 V, Vec32 F, DevS
         e2 = fmaf(r1, r1, e2);
         rr = fmaf(r1, F.r2[i], rr);
     }
-    double v[2] = {(double)e2, (double)rr};
-    if (grid_reduce<2>(v, part, &st->counter)) {
+    const float av[2] = {e2, rr};
+    double v[2];
+    if (grid_reduce_f<2>(av, v, part, &st->counter)) {
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
         mx_end_iteration(st, v[0], v[1], true);

@@ -298,22 +298,35 @@ def test_matrix_mod_example_nonsymmetric_pattern(gpu):
             assert iter_ok(res.niter, it) and rel_l2(x, xo) <= 1e-12
 
 
-@pytest.mark.parametrize("mode", ["levels", "dataflow"])
+@pytest.mark.parametrize("mode", ["levels", "levels-c1", "levels-c16", "coop", "single"])
 def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
-    """The single-launch dataflow sweep and the one-launch-per-level sweep do
-    the same per-row arithmetic: identical DIC results and solves."""
-    if mode == "levels":
-        monkeypatch.setenv("TFS_SWEEP", "levels")
-    s = system(CONVDIFF, 10, 9, 8)
-    b = np.random.default_rng(9).uniform(-1, 1, s.n)
-    with Solver(s.matrix()) as sol:
-        assert np.array_equal(sol.prec_form(s.val, 2), O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
-        assert np.array_equal(sol.prec_solve(s.val, 2, b),
-                              O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
-        ref = oracle_solve(s, TFS_BICG, 2)
-        x, r = np.zeros(s.n), s.b.copy()
-        res = sol.solve(TFS_BICG, s.val, x, r, 2, 2000, ref["tol"])
-        assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+    """The DIC schedules -- one launch per level with the small levels in one
+    8-CTA cluster (default), in one block (c1) or in a 16-CTA cluster (c16),
+    one cooperative launch with grid barriers, and the single-launch dataflow
+    sweep -- do the same per-row arithmetic: Prec_Form and Prec_Solve bitwise
+    equal to the oracle, and solves within the parity gates.  The 40^3 system
+    has levels of more than 8192 rows, so the grid-wide part of each schedule
+    runs, not only the tail."""
+    monkeypatch.setenv("TFS_SWEEP", mode.split("-")[0])
+    if "-c" in mode:
+        monkeypatch.setenv("TFS_TAIL_CLUSTER", mode.split("-c")[1])
+    for s, method in ((system(CONVDIFF, 10, 9, 8), TFS_BICG), (system(POISSON, 40, 40, 40), TFS_CG)):
+        b = np.random.default_rng(9).uniform(-1, 1, s.n)
+        with Solver(s.matrix()) as sol:
+            assert np.array_equal(sol.prec_form(s.val, 2), O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
+            assert np.array_equal(sol.prec_solve(s.val, 2, b),
+                                  O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+            ref = oracle_solve(s, method, 2)
+            x, r = np.zeros(s.n), s.b.copy()
+            res = sol.solve(method, s.val, x, r, 2, 2000, ref["tol"])
+            assert res.status == 0
+            assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+        if s.n > 60000:
+            with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+                x, r = np.zeros(s.n), s.b.copy()
+                res = sol.solve(method, s.val, x, r, 2, 2000, ref["tol"])
+                assert res.status == 0 and res.fin_res < ref["tol"]
+                assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) < 1e-6
 
 
 @pytest.mark.parametrize("mode", [TFS_FP64, TFS_MIXED])
