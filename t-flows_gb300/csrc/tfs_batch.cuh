@@ -183,7 +183,7 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         rz = 0.0;
         for (int i = gtid; i < n_int; i += stride) {
             RowGeom g = row_geom(A, i);
-            double r = row_accum<true, double, double, double>(V.u1[i], A.col, S.val, V.x, g.off, 0, g.len);
+            double r = row_accum<true, double, double, double, false, 4>(V.u1[i], A.col, S.val, V.x, g.off, 0, g.len);
             V.r[i] = r;
             e2 = fma(r, r, e2);
             VT rT = (VT)r, dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
@@ -257,7 +257,7 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                     sv[q] = (VT)0;
                     if (ii[q] < n_int) {
                         RowGeom g = row_geom(A, ii[q]);
-                        sv[q] = row_accum<false, VT, VT, VT>((VT)0, A.col, valT, W.p, g.off, 0, g.len);
+                        sv[q] = row_accum<false, VT, VT, VT, false, 4>((VT)0, A.col, valT, W.p, g.off, 0, g.len);
                     }
                 }
 #pragma unroll

@@ -59,27 +59,43 @@ __device__ __forceinline__ T gather(const T *p)
     else return __ldcg(p);
 }
 
-// Sequential sum s - sum_{j0<=j<j1} a_j x_col(j) (SUB) or s + ... (ADD),
-// loads of four entries issued before their products are summed in order.
-template <bool SUB, typename VT, typename XT, typename AT, bool NC = false>
+// Sequential sum s - sum_{j0<=j<j1} a_j x_col(j) (SUB) or s + ... (ADD).
+// Up to BW entries per pass: every column index and value of the pass is
+// loaded, then every gather issued, and only then are the products summed in
+// column order, so a row of up to BW entries costs three dependent memory
+// round trips (geometry, entries, gathers) whatever its length.
+// Four entries per pass: eight (one pass for the 7-entry rows of a hex
+// mesh) raised the SpMV's registers from 32 to 40 and made it slower on the
+// 128^3 system (43.8 against 40.1 us).
+#ifndef TFS_ROW_BATCH
+#define TFS_ROW_BATCH 4
+#endif
+template <bool SUB, typename VT, typename XT, typename AT, bool NC = false, int BW = TFS_ROW_BATCH>
 __device__ __forceinline__ AT row_accum(AT s, const int *__restrict__ col,
                                         const VT *__restrict__ val,
                                         const XT *__restrict__ x, int off, int j0, int j1)
 {
-    int j = j0;
-    for (; j + 4 <= j1; j += 4) {
-        int e0 = off + (j << 5), e1 = e0 + 32, e2 = e0 + 64, e3 = e0 + 96;
-        int k0 = __ldg(col + e0), k1 = __ldg(col + e1), k2 = __ldg(col + e2), k3 = __ldg(col + e3);
-        AT a0 = (AT)__ldg(val + e0), a1 = (AT)__ldg(val + e1), a2 = (AT)__ldg(val + e2), a3 = (AT)__ldg(val + e3);
-        AT x0 = (AT)gather<NC>(x + k0), x1 = (AT)gather<NC>(x + k1), x2 = (AT)gather<NC>(x + k2),
-           x3 = (AT)gather<NC>(x + k3);
-        if (SUB) { s = s - a0 * x0; s = s - a1 * x1; s = s - a2 * x2; s = s - a3 * x3; }
-        else     { s = s + a0 * x0; s = s + a1 * x1; s = s + a2 * x2; s = s + a3 * x3; }
-    }
-    for (; j < j1; j++) {
-        int e = off + (j << 5);
-        AT a = (AT)__ldg(val + e), xv = (AT)gather<NC>(x + __ldg(col + e));
-        if (SUB) s = s - a * xv; else s = s + a * xv;
+    for (int j = j0; j < j1; j += BW) {
+        int k[BW];
+        AT a[BW], xv[BW];
+#pragma unroll
+        for (int q = 0; q < BW; q++) {
+            k[q] = 0;
+            a[q] = (AT)0;
+            if (j + q < j1) {
+                const int e = off + ((j + q) << 5);
+                k[q] = __ldg(col + e);
+                a[q] = (AT)__ldg(val + e);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < BW; q++) xv[q] = (j + q < j1) ? (AT)gather<NC>(x + k[q]) : (AT)0;
+#pragma unroll
+        for (int q = 0; q < BW; q++)
+            if (j + q < j1) {
+                if (SUB) s = s - a[q] * xv[q];
+                else s = s + a[q] * xv[q];
+            }
     }
     return s;
 }
