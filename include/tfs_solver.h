@@ -321,6 +321,36 @@ int tfs_residual_norm_noalloc(int32_t n, const int32_t *d_row1,
                               const double *d_x, double *d_r1, double *d_norm,
                               void *stream);
 
+/* ---- device-side assembly through the face -> entry map ---------------- */
+
+/* Attach the mesh faces to a handle: faces_c (2*n_faces, 1-based cells c1,
+ * c2; c2 <= 0 marks a boundary face) and pos1 (2*n_faces, the 1-based CSR
+ * positions of the entries (c1,c2) and (c2,c1) of an interior face) as
+ * tfs_topology_build returns them.  Checked against the registered topology;
+ * builds on the device, once per mesh, every cell's faces in ascending face
+ * order.  Replaces: the face loops' use of Matrix_Type%pos and %dia
+ * (Matrix_Mod.f90:44-46, filled by Topology.f90:106-121). */
+int tfs_faces_register(tfs_handle *h, int32_t n_faces, const int32_t *faces_c,
+                       const int32_t *pos1);
+
+/* Assemble matrix values on the device from per-face coefficients, as the
+ * reference's face loops do (NewUVW.f90:366-384 followed by the cell loop
+ * NewUVW.f90:500-505; Compute_Pressure_Simple.f90:100-113 is the case
+ * off12 = off21 = dia12 = dia21 = A12 on a zeroed matrix):
+ *   interior face s:  val(pos(1,s)) -= off12(s); val(dia(c1)) += dia12(s);
+ *                     val(pos(2,s)) -= off21(s); val(dia(c2)) += dia21(s)
+ *   boundary face s:  val(dia(c1)) += dia12(s), skipped when dia12(s) == 0
+ *                     (a boundary type that adds nothing)
+ *   then every cell:  val(dia(c)) += cell(c)          (d_cell may be NULL)
+ * Every diagonal receives its additions in face order, so the values are
+ * bitwise those of the sequential loops.  d_val (nnz, CSR order) holds the
+ * starting values (normally zero) and receives the result; all arrays are
+ * device pointers (off21, dia21 of boundary faces are not read).  Runs on the
+ * handle's stream, before any solve issued after it; no synchronisation. */
+int tfs_assemble_faces_device(tfs_handle *h, const double *d_off12, const double *d_off21,
+                              const double *d_dia12, const double *d_dia21,
+                              const double *d_cell, double *d_val);
+
 /* ---- host-side mesh utilities ------------------------------------------ */
 
 /* Count of stored entries of the face-connectivity matrix (one per cell plus

@@ -413,3 +413,34 @@ void tfo_solve(int method, int n, const int *row, const int *col, const int *dia
     else
         tfo_cg(n, row, col, dia, val, x, r1, prec, niter, tol, ini_res, fin_res);
 }
+
+/* Matrix values from per-face coefficients through the face -> entry map,
+ * as the face loops of the reference assemble them: NewUVW.f90:366-384 (the
+ * interior face updates the two off-diagonal entries through pos(1,s) and
+ * pos(2,s) and the two diagonals through dia; a boundary face of a
+ * contributing type adds to the diagonal of c1) followed by the cell loop
+ * NewUVW.f90:500-505 (the inertial term on every diagonal).  Compute_Pressure_
+ * Simple.f90:100-113 is the same loop with off12 = off21 = dia12 = dia21 =
+ * A12 (its "= -A12" equals "0 - A12" on a zeroed matrix).  A boundary face
+ * whose dia12 is exactly zero stands for a type that adds nothing.
+ * faces_c(1:2, 1:n_faces), pos(1:2, 1:n_faces), dia(1:n_cells), val(1:nnz);
+ * cell may be NULL. */
+void tfo_assemble_faces(int n_cells, int n_faces, const int *faces_c, const int *pos,
+                        const int *dia, const double *off12, const double *off21,
+                        const double *dia12, const double *dia21, const double *cell,
+                        double *val)
+{
+    for (int s = 1; s <= n_faces; s++) {
+        const int c1 = faces_c[2 * (s - 1)], c2 = faces_c[2 * (s - 1) + 1];
+        if (c2 > 0) {
+            A1(val, pos[2 * (s - 1)]) = A1(val, pos[2 * (s - 1)]) - A1(off12, s);
+            A1(val, A1(dia, c1)) = A1(val, A1(dia, c1)) + A1(dia12, s);
+            A1(val, pos[2 * (s - 1) + 1]) = A1(val, pos[2 * (s - 1) + 1]) - A1(off21, s);
+            A1(val, A1(dia, c2)) = A1(val, A1(dia, c2)) + A1(dia21, s);
+        } else if (A1(dia12, s) != 0.0) {
+            A1(val, A1(dia, c1)) = A1(val, A1(dia, c1)) + A1(dia12, s);
+        }
+    }
+    if (cell)
+        for (int c = 1; c <= n_cells; c++) A1(val, A1(dia, c)) = A1(val, A1(dia, c)) + A1(cell, c);
+}

@@ -44,6 +44,8 @@ def lib() -> C.CDLL:
         for name in ("tfo_cg", "tfo_bicg", "tfo_cgs"):
             getattr(L, name).argtypes = [C.c_int, _i, _i, _i, _d, _d, _d, C.c_int, _i, C.c_double, _d, _d]
         L.tfo_solve.argtypes = [C.c_int, C.c_int, _i, _i, _i, _d, _d, _d, C.c_int, _i, C.c_double, _d, _d]
+        L.tfo_assemble_faces.restype = None
+        L.tfo_assemble_faces.argtypes = [C.c_int, C.c_int, _i, _i, _i, _d, _d, _d, _d, _d, _d]
         _lib = L
     return _lib
 
@@ -103,3 +105,19 @@ def solve(method, n, row, col, dia, val, x, r1, prec, niter, tol, ini_res=0.0):
     lib().tfo_solve(method, n, _pi(row), _pi(col), _pi(dia), _pd(val), _pd(x), _pd(r1), prec,
                     C.byref(it), tol, C.byref(ini), C.byref(fin))
     return it.value, ini.value, fin.value
+
+
+def assemble_faces(n_cells, faces_c, pos, dia, off12, off21, dia12, dia21, cell, val0):
+    """Values from per-face coefficients (the reference's face loops);
+    returns a new array starting from val0."""
+    val = np.array(val0, dtype=np.float64)
+    n_faces = len(faces_c) // 2
+    cellp = _pd(np.ascontiguousarray(cell, dtype=np.float64)) if cell is not None else None
+    lib().tfo_assemble_faces(n_cells, n_faces, _pi(np.ascontiguousarray(faces_c, dtype=np.int32)),
+                             _pi(np.ascontiguousarray(pos, dtype=np.int32)),
+                             _pi(np.ascontiguousarray(dia, dtype=np.int32)),
+                             _pd(np.ascontiguousarray(off12, dtype=np.float64)),
+                             _pd(np.ascontiguousarray(off21, dtype=np.float64)),
+                             _pd(np.ascontiguousarray(dia12, dtype=np.float64)),
+                             _pd(np.ascontiguousarray(dia21, dtype=np.float64)), cellp, _pd(val))
+    return val

@@ -79,6 +79,7 @@ static SellDev sell_of(const tfs_handle *h)
     A.rowinfo = h->rowinfo;
     A.slice_off = h->slice_off;
     A.col = h->col;
+    A.width = h->sell_width;
     return A;
 }
 
@@ -126,8 +127,17 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
     for (int q = 0; q < tail; q++) {
         const int l = MODE == 1 ? tail - 1 - q : q;
         const int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
-        cudaError_t e = launch_ex(pdl, k_sweep_level<T, NR, MODE>, (r1 - r0 + TFS_TPB - 1) / TFS_TPB, TFS_TPB, s,
-                                  A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        const int bs = h->level_tpb;
+        const int nb = (r1 - r0 + bs - 1) / bs;
+        cudaError_t e;
+        if (bs == 1024)
+            e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 1024>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        else if (bs == 512)
+            e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 512>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        else if (bs == 128)
+            e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 128>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        else
+            e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 256>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         if (e != cudaSuccess) return tfs_engine_error(e, "level launch");
         first = 0;
         (*count)++;
@@ -434,17 +444,35 @@ static int build_layout(tfs_handle *h, int kind)
         if (o >= 0) rowinfo[p] = (uint32_t)(row0[o + 1] - row0[o]) | ((uint32_t)(dia0[o] - row0[o]) << 16);
     }
     int64_t off = 0;
+    int wmax = 0;
     for (int s = 0; s < n_slices; s++) {
         int w = 0;
         for (int t = 0; t < 32; t++) {
             int len = (int)(rowinfo[32 * s + t] & 0xffffu);
             if (len > w) w = len;
         }
+        if (w > wmax) wmax = w;
         slice_off[s] = (int)off;
         off += 32 * (int64_t)w;
         if (off > INT32_MAX) { tfs_set_error_text("padded matrix exceeds 2^31 entries"); return TFS_ERR_ARG; }
     }
     slice_off[n_slices] = (int)off;
+    // One width for every slice (the slice offset computed instead of
+    // loaded) when rows have at most 8 entries and it costs at most 5% more
+    // slots: the 7-entry rows of a hex mesh.  Measured equal to per-slice
+    // widths on the 128^3 system (binary32 SpMV 39.3 against 39.5 us);
+    // TFS_SELL_UNIFORM=0 keeps per-slice widths.
+    h->sell_width = 0;
+    {
+        const int64_t uni = 32 * (int64_t)wmax * n_slices;
+        const char *env = getenv("TFS_SELL_UNIFORM");
+        const bool allow = !(env && strcmp(env, "0") == 0);
+        if (allow && wmax > 0 && wmax <= 8 && uni <= off + off / 20 && uni <= INT32_MAX) {
+            h->sell_width = wmax;
+            for (int s = 0; s <= n_slices; s++) slice_off[s] = 32 * wmax * s;
+            off = uni;
+        }
+    }
     const int nnz_pad = (int)off;
     std::vector<int> colx((size_t)nnz_pad, 0), vmap((size_t)nnz_pad, -1);
     for (int p = 0; p < n_int; p++) {
@@ -617,6 +645,7 @@ static void free_handle(tfs_handle *h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_layout(h);
+    tfs_faces_free(h);
     void *ptrs[] = {h->stage_val, h->stage_b, h->stage_x, h->st, h->params, h->ctl};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -678,6 +707,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
+    env = getenv("TFS_LEVEL_TPB");
+    if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
     env = getenv("TFS_PDL");
     if (env && strcmp(env, "0") == 0) h->use_pdl = 0;
     env = getenv("TFS_GRAPH");

@@ -85,6 +85,7 @@ struct SellDev {
     const uint32_t *rowinfo;
     const int *slice_off;
     const int *col;
+    int width;    // > 0: every slice has this width (slice s starts at 32*width*s)
 };
 
 // Work vectors (binary64).
@@ -96,6 +97,8 @@ struct Vec32 {
     float *r, *r2, *p, *p2, *q, *q2, *u1, *u2, *v2, *w, *d, *y, *y2, *z, *z2;
     float *e;   // solution correction since the last binary64 true residual
 };
+
+struct FaceMap;   // tfs_assemble.cu
 
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
@@ -111,6 +114,7 @@ struct tfs_handle {
     const struct GraphEntry *last_graph = nullptr;
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
+    int sell_width = 0;                // uniform slice width (0: per-slice widths)
     int grid = 0;                      // blocks of the vector kernels (grid-stride)
     int grid_spmv = 0;                 // blocks of the SpMV-type kernels
     int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels
@@ -118,6 +122,8 @@ struct tfs_handle {
     int sweep_grid = 0;                // blocks of the dataflow sweeps
     int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative
     int use_pdl = 1;                   // programmatic dependent launch between level kernels
+    int level_tpb = TFS_TPB;           // threads per block of the level-sweep kernels (TFS_LEVEL_TPB;
+                                       // 128/256/512/1024 measured 147.7/146.4/147.4/150.1 us per DIC application)
     int dic_r = 0;                     // rows per thread of the cooperative sweep (0: not chosen yet)
     int eager = 0;                     // 1: launch kernels directly, no CUDA graph
     int bicg_literal = 0;              // 1: BiCG runs its shadow sequence explicitly
@@ -154,6 +160,7 @@ struct tfs_handle {
     std::map<int, GraphEntry> graphs;  // key: method | prec << 4 | precision << 8
     tfs_stats stats{};
     int64_t device_bytes = 0;
+    FaceMap *faces = nullptr;          // tfs_faces_register
 };
 
 // tfs_engine.cu
@@ -167,3 +174,5 @@ int tfs_solve_launch(int method, tfs_handle *h, const double *val, double *x, do
 int tfs_solve_collect(tfs_handle *h, int32_t *niter, double *ini_res, double *fin_res);
 // Device bytes a topology will hold once its layout is built (estimate).
 int64_t tfs_estimate_bytes(int32_t n, int32_t nnz);
+// tfs_assemble.cu
+void tfs_faces_free(tfs_handle *h);

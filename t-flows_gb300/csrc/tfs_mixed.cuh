@@ -192,8 +192,7 @@ k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__
     float acc = 0.f;
     for (int c = blockIdx.x; c < A.n_chunks; c += gridDim.x) {
         int i = c * TFS_TPB + threadIdx.x;
-        RowGeom g = row_geom(A, i);
-        float s = row_accum<false, float, float, float, TFS_SPMV_NC>(0.f, A.col, val, p, g.off, 0, g.len);
+        float s = row_spmv<false, float, float, float, TFS_SPMV_NC>(0.f, A, val, p, i);
         if (stop) return;
         q[i] = s;
         acc = fmaf(p[i], s, acc);

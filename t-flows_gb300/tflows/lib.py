@@ -65,6 +65,8 @@ SIGNATURES = {
     "tfs_get_levels": (C.c_int, [P_void, P_i32]),
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_time_prec": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
+    "tfs_faces_register": (C.c_int, [P_void, C.c_int32, P_i32, P_i32]),
+    "tfs_assemble_faces_device": (C.c_int, [P_void, P_void, P_void, P_void, P_void, P_void, P_void]),
     "tfs_status_string": (C.c_char_p, [C.c_int]),
     "tfs_last_error": (C.c_char_p, []),
     "tfs_batch_create": (C.c_int, [C.c_int, C.POINTER(P_void), C.POINTER(P_void)]),

@@ -134,6 +134,49 @@ class Solver:
                                      C.byref(ms)), "tfs_time_spmv")
         return ms.value
 
+    def faces_register(self, faces_c: np.ndarray, pos: np.ndarray) -> None:
+        """Attach the mesh faces (n_faces x 2 cells, 1-based, c2 <= 0 on the
+        boundary) and Matrix_Type%pos (n_faces x 2) for device assembly."""
+        fc = np.ascontiguousarray(faces_c, dtype=np.int32).reshape(-1)
+        ps = np.ascontiguousarray(pos, dtype=np.int32).reshape(-1)
+        if fc.size != ps.size or fc.size % 2:
+            raise ValueError("faces_c and pos must both be n_faces x 2")
+        check(self.lib.tfs_faces_register(self.h, fc.size // 2, ptr(fc, _i32), ptr(ps, _i32)),
+              "tfs_faces_register")
+        self.n_faces = fc.size // 2
+
+    def assemble(self, off12: np.ndarray, off21: np.ndarray, dia12: np.ndarray, dia21: np.ndarray,
+                 cell: np.ndarray | None = None, val0: np.ndarray | None = None) -> np.ndarray:
+        """Matrix values from per-face coefficients, assembled on the device
+        (tfs_assemble_faces_device); host arrays in, CSR values out."""
+        nf = getattr(self, "n_faces", None)
+        if nf is None:   # no faces registered: the library reports it
+            check(self.lib.tfs_assemble_faces_device(self.h, None, None, None, None, None, None),
+                  "tfs_assemble_faces_device")
+        arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in (off12, off21, dia12, dia21)]
+        if any(a.shape != (nf,) for a in arrays):
+            raise ValueError(f"face coefficients must have length {nf}")
+        val = np.zeros(self.nnz) if val0 is None else np.array(val0, dtype=np.float64)
+        host = arrays + ([np.ascontiguousarray(cell, dtype=np.float64)] if cell is not None else []) + [val]
+        dev = []
+        try:
+            for a in host:
+                q = C.c_void_p()
+                check(self.lib.tfs_device_alloc(max(a.nbytes, 8), C.byref(q)), "tfs_device_alloc")
+                dev.append(q.value)
+                check(self.lib.tfs_copy(self.h, C.c_void_p(q.value), a.ctypes.data_as(C.c_void_p), a.nbytes),
+                      "tfs_copy")
+            d_cell = C.c_void_p(dev[4]) if cell is not None else None
+            check(self.lib.tfs_assemble_faces_device(self.h, *(C.c_void_p(d) for d in dev[:4]), d_cell,
+                                                     C.c_void_p(dev[-1])), "tfs_assemble_faces_device")
+            check(self.lib.tfs_copy(self.h, val.ctypes.data_as(C.c_void_p), C.c_void_p(dev[-1]), val.nbytes),
+                  "tfs_copy")
+            check(self.lib.tfs_sync(self.h), "tfs_sync")
+        finally:
+            for d in dev:
+                self.lib.tfs_device_free(C.c_void_p(d))
+        return val
+
     def time_prec(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
         """Milliseconds per DIC preconditioner application (both sweeps)."""
         ms = _dbl(0.0)

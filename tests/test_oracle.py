@@ -220,3 +220,25 @@ def test_golden_topology():
         assert np.array_equal(mir[mir - 1] , np.arange(1, col.size + 1))
         f = g["faces_c"]
         assert np.array_equal(col[pos[:, 0] - 1], f[:, 1]) and np.array_equal(col[pos[:, 1] - 1], f[:, 0])
+
+
+def test_assemble_faces_known_answer():
+    """Face-loop assembly (NewUVW.f90:366-384, :500-505) on a three-cell
+    chain with two boundary faces, against the matrix written out by hand."""
+    faces = np.array([[1, 2], [2, 3], [1, -1], [3, -2]], np.int32)
+    row, col, dia, mir, pos = O.topology(3, faces)
+    off12 = np.array([1.5, 2.0, 0.0, 0.0])
+    off21 = np.array([1.25, 2.5, 0.0, 0.0])
+    dia12 = np.array([1.5, 2.0, 0.75, 0.0])     # face 4: a boundary type that adds nothing
+    dia21 = np.array([1.25, 2.5, 0.0, 0.0])
+    cell = np.array([0.125, 0.25, 0.5])
+    val = O.assemble_faces(3, faces.reshape(-1), pos.reshape(-1), dia, off12, off21, dia12, dia21,
+                           cell, np.zeros(len(col)))
+    dense = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(row[i] - 1, row[i + 1] - 1):
+            dense[i, col[j] - 1] = val[j]
+    want = np.array([[1.5 + 0.75 + 0.125, -1.5, 0.0],
+                     [-1.25, 1.25 + 2.0 + 0.25, -2.0],
+                     [0.0, -2.5, 2.5 + 0.5]])
+    assert np.array_equal(dense, want)
