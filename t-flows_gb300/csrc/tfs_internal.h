@@ -53,7 +53,7 @@ struct DevState {
     // and its binary32 rounding, computed once by the thread that finalises
     // rho instead of by every thread
     float beta32;
-    int pad3;
+    float alpha32;       // (float) alpha, published with alpha
     // grid barrier of the cooperative DIC kernel (zeroed with the state)
     unsigned int bar_count, bar_gen, bar_abort, pad2;
 };

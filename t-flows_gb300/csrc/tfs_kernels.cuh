@@ -167,9 +167,10 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sm)[TFS_TPB 
 // carries about 48 significant bits without any binary64 instruction per
 // lane (GB300's binary64 pipe is narrow: a binary64 shuffle reduction of
 // every thread's partial kept it half busy in the binary32 vector kernels).
-__device__ __forceinline__ double warp_sum_f(float v)
+__device__ __forceinline__ void warp_sum_f2(float v, float &hi, float &lo)
 {
-    float hi = v, lo = 0.f;
+    hi = v;
+    lo = 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float h2 = __shfl_down_sync(FULL, hi, o), l2 = __shfl_down_sync(FULL, lo, o);
@@ -179,6 +180,12 @@ __device__ __forceinline__ double warp_sum_f(float v)
         hi = s;
         lo = (lo + l2) + e;
     }
+}
+
+__device__ __forceinline__ double warp_sum_f(float v)
+{
+    float hi, lo;
+    warp_sum_f2(v, hi, lo);
     return (double)hi + (double)lo;
 }
 
@@ -190,8 +197,9 @@ __device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        const double w = warp_sum_f(v[k]);
-        if (lane == 0) sm[k][warp] = w;
+        float hi, lo;
+        warp_sum_f2(v[k], hi, lo);
+        if (lane == 0) sm[k][warp] = (double)hi + (double)lo;   // binary64 in lane 0 only
     }
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -202,6 +202,7 @@ k_mx_spmv_pq(SellDev A, const float *__restrict__ val, const float *__restrict__
     double v[1];
     if (grid_reduce_f<1>(a1, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
+        st->alpha32 = (float)st->alpha;
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
     }
@@ -284,7 +285,7 @@ template <bool FUSED>
 __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part)
 {
     const bool stop = (st->done | st->need_true) != 0;
-    const double alpha = st->alpha;
+    const float a = st->alpha32;             // (float) alpha, published once
     const float4 *p4 = (const float4 *)F.p, *q4 = (const float4 *)F.q, *d4 = (const float4 *)F.d;
     float4 *e4 = (float4 *)F.e, *r4 = (float4 *)F.r, *zz4 = (float4 *)F.z;
     float e2 = 0.f, rz = 0.f;
@@ -292,7 +293,6 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevS
         float4 p = p4[v], q = q4[v], r = r4[v], e = e4[v], d;
         if (FUSED) d = d4[v];
         if (stop) return;
-        const float a = (float)alpha;
         e4[v] = make_float4(fmaf(a, p.x, e.x), fmaf(a, p.y, e.y), fmaf(a, p.z, e.z), fmaf(a, p.w, e.w));
         r = make_float4(fmaf(-a, q.x, r.x), fmaf(-a, q.y, r.y), fmaf(-a, q.z, r.z), fmaf(-a, q.w, r.w));
         r4[v] = r;
@@ -368,6 +368,7 @@ k_mx_spmv2_pq(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, d
     double v[1];
     if (grid_reduce_f<1>(av, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
+        st->alpha32 = (float)st->alpha;
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
     }
@@ -447,6 +448,7 @@ k_mx_spmv_v(SellDev A, const float *__restrict__ val, Vec32 F, DevState *st, dou
     double v[1];
     if (grid_reduce_f<1>(av, v, part, &st->counter)) {
         st->alpha = st->rho / v[0];
+        st->alpha32 = (float)st->alpha;
         st->spmv_ns += gtimer() - st->t_spmv0;
         st->spmv_n += 1;
     }
