@@ -316,6 +316,13 @@ def run_ours(args, dist: Dist) -> dict | None:
                "timing": "host wall clock around each tfs_solve call (copies included)"}
         for p in (p_val, p_x, p_r):
             lib.tfs_host_free(C.c_void_p(p))
+
+    # The rows after the solve path, on the same mesh (outside the timed
+    # region): Matrix_Mod_Topology built on the device against the host
+    # builder, and the face-loop assembly on the device against the oracle.
+    next_rows = None
+    if dist.rank == 0 and not args.no_next_rows:
+        next_rows = measure_next_rows(lib, sol, s, dalloc)
     for p in (d_val, d_b, d_x, d_r, d_zero):
         lib.tfs_device_free(C.c_void_p(p))
 
@@ -378,13 +385,74 @@ def run_ours(args, dist: Dist) -> dict | None:
         "spmv": {"fp64_us": round(spmv64_ms * 1e3, 2), "fp32_us": round(spmv32_ms * 1e3, 2),
                  "fp64_gbs": round(bytes64 / (spmv64_ms * 1e-3) / 1e9, 1),
                  "fp32_gbs": round(achieved, 1), "timing": "CUDA events, back-to-back launches"},
-        "roofline": roof, "roofline_spmv": roof_spmv, "e2e": e2e, "gpu_launches": int(timed_launches),
+        "roofline": roof, "roofline_spmv": roof_spmv, "next_rows": next_rows,
+        "e2e": e2e, "gpu_launches": int(timed_launches),
         "clocks": clock_info,
     }
     if cpu:
         line["cpu_baseline"] = cpu
     sol.close()
     return line if dist.rank == 0 else None
+
+
+def measure_next_rows(lib, sol, s, dalloc) -> dict:
+    """Device topology build and device face assembly of the workload's mesh
+    (interior faces), each checked bit for bit against its CPU counterpart
+    and timed beside it."""
+    import numpy as np
+    from oracle import tfs_oracle as O
+    from tflows.lib import check
+    from tflows.matrix_mod import Matrix_Mod_Topology, Matrix_Mod_Topology_Device
+
+    faces = s.faces_c
+    Matrix_Mod_Topology_Device(64, np.zeros((0, 2), np.int32))      # warm-up
+    t = time.perf_counter()
+    dev = Matrix_Mod_Topology_Device(s.n, faces)
+    topo_dev_ms = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    host = Matrix_Mod_Topology(s.n, faces)
+    topo_host_ms = (time.perf_counter() - t) * 1e3
+    topo_same = bool(np.array_equal(dev.col, host.col) and np.array_equal(dev.pos, host.pos)
+                     and np.array_equal(dev.mir, host.mir) and np.array_equal(dev.row, host.row)
+                     and np.array_equal(dev.dia, host.dia))
+    # Assembly: pressure-like coefficients per face, an inertial cell term.
+    rng = np.random.default_rng(BASE_SEED)
+    nf = len(faces)
+    a = rng.uniform(0.5, 1.5, nf)
+    cell = rng.uniform(0.0, 1e-3, s.n)
+    sol.faces_register(faces, dev.pos)
+    d_a, d_c, d_v = dalloc(8 * nf), dalloc(8 * s.n), dalloc(8 * s.nnz)
+    zeros = np.zeros(s.nnz)
+    h = sol.h
+    check(lib.tfs_copy(h, C.c_void_p(d_a), a.ctypes.data_as(C.c_void_p), 8 * nf), "copy")
+    check(lib.tfs_copy(h, C.c_void_p(d_c), cell.ctypes.data_as(C.c_void_p), 8 * s.n), "copy")
+    times = []
+    for rep in range(4):
+        check(lib.tfs_copy(h, C.c_void_p(d_v), zeros.ctypes.data_as(C.c_void_p), 8 * s.nnz), "copy")
+        check(lib.tfs_timer_start(h), "timer")
+        check(lib.tfs_assemble_faces_device(h, C.c_void_p(d_a), C.c_void_p(d_a), C.c_void_p(d_a),
+                                            C.c_void_p(d_a), C.c_void_p(d_c), C.c_void_p(d_v)), "assemble")
+        ms = C.c_double()
+        check(lib.tfs_timer_stop(h, C.byref(ms)), "timer")
+        if rep:
+            times.append(ms.value)
+    val = np.empty(s.nnz)
+    check(lib.tfs_copy(h, val.ctypes.data_as(C.c_void_p), C.c_void_p(d_v), 8 * s.nnz), "copy")
+    check(lib.tfs_sync(h), "sync")
+    for p in (d_a, d_c, d_v):
+        lib.tfs_device_free(C.c_void_p(p))
+    t = time.perf_counter()
+    want = O.assemble_faces(s.n, faces.reshape(-1), dev.pos.reshape(-1), dev.dia, a, a, a, a, cell, zeros)
+    asm_cpu_ms = (time.perf_counter() - t) * 1e3
+    return {
+        "topology_device_ms": round(topo_dev_ms, 2), "topology_host_ms": round(topo_host_ms, 2),
+        "topology_identical": topo_same,
+        "assemble_device_ms": round(statistics.median(times), 4), "assemble_oracle_ms": round(asm_cpu_ms, 2),
+        "assemble_identical": bool(np.array_equal(val, want)),
+        "timing": "topology: host wall clock around the synchronous calls (the device build includes "
+                  "its scratch allocation and the copies of faces in and arrays out); assembly: CUDA "
+                  "events on the handle's stream, median of 3 after a warm-up",
+    }
 
 
 # ---------------------------------------------------------------- serving arm
@@ -892,6 +960,8 @@ def main(argv=None) -> int:
     ap.add_argument("--ref-sample-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="skip the device topology / assembly measurements")
     ap.add_argument("--modes", default="fp64,mixed",
                     help="arithmetic legs to run (profiling runs may pick one)")
     args = ap.parse_args(argv)

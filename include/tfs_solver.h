@@ -243,6 +243,9 @@ int tfs_host_free(void *ptr);
  * handle's stream (asynchronous for device and page-locked memory). */
 int tfs_copy(tfs_handle *h, void *dst, const void *src, size_t bytes);
 
+/* Synchronous copy in any direction on the current device (no handle). */
+int tfs_memcpy(void *dst, const void *src, size_t bytes);
+
 /* Wait for all work queued on the handle's stream. */
 int tfs_sync(tfs_handle *h);
 
@@ -365,6 +368,19 @@ int32_t tfs_topology_count(int32_t n_cells, int32_t n_faces,
 int tfs_topology_build(int32_t n_cells, int32_t n_faces, const int32_t *faces_c,
                        int32_t *row1, int32_t *col1, int32_t *dia1,
                        int32_t *mir1, int32_t *pos1);
+
+/* Matrix_Mod_Topology on the device: the same row/col/dia/mir/pos as
+ * tfs_topology_build, bit for bit, from device-resident faces_c (2*n_faces,
+ * 1-based; c2 <= 0 marks a boundary face).  d_col1 and d_mir1 must hold
+ * n_cells + 2*n_faces entries (an upper bound of nnz); d_row1 n_cells+1,
+ * d_dia1 n_cells, d_pos1 2*n_faces (0 for boundary faces).  *nnz_out
+ * receives nnz.  Faces must join distinct pairs of distinct cells (checked:
+ * cell numbers in range and c1 != c2; TFS_ERR_TOPOLOGY otherwise).  Runs on
+ * the current device's default stream and returns when done.
+ * Replaces Matrix_Mod/Topology.f90:2-127 for meshes held on the GPU. */
+int tfs_topology_build_device(int32_t n_cells, int32_t n_faces, const int32_t *d_faces_c,
+                              int32_t *d_row1, int32_t *d_col1, int32_t *d_dia1,
+                              int32_t *d_mir1, int32_t *d_pos1, int32_t *nnz_out);
 
 #ifdef __cplusplus
 }

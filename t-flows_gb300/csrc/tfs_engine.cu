@@ -1581,6 +1581,13 @@ extern "C" int tfs_device_free(void *ptr)
     return TFS_OK;
 }
 
+extern "C" int tfs_memcpy(void *dst, const void *src, size_t bytes)
+{
+    if ((!dst || !src) && bytes) return TFS_ERR_ARG;
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
+    return TFS_OK;
+}
+
 extern "C" int tfs_host_alloc(size_t bytes, void **ptr)
 {
     if (!ptr) return TFS_ERR_ARG;

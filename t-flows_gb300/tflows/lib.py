@@ -95,6 +95,9 @@ SIGNATURES = {
     "tfs_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P_void)]),
     "tfs_host_free": (C.c_int, [P_void]),
     "tfs_copy": (C.c_int, [P_void, P_void, P_void, C.c_size_t]),
+    "tfs_memcpy": (C.c_int, [P_void, P_void, C.c_size_t]),
+    "tfs_topology_build_device": (C.c_int, [C.c_int32, C.c_int32, P_void, P_void, P_void, P_void, P_void,
+                                            P_void, P_i32]),
     "tfs_sync": (C.c_int, [P_void]),
     "tfs_timer_start": (C.c_int, [P_void]),
     "tfs_timer_stop": (C.c_int, [P_void, P_dbl]),

@@ -78,3 +78,36 @@ def Matrix_Mod_Topology(n_cells: int, faces_c: np.ndarray) -> Matrix_Type:
                                  ptr(col, C.c_int32), ptr(dia, C.c_int32), ptr(mir, C.c_int32),
                                  ptr(pos, C.c_int32)), "tfs_topology_build")
     return Matrix_Type(n_cells, row, col, dia, np.zeros(nnz), mir=mir, pos=pos.reshape(-1, 2))
+
+
+def Matrix_Mod_Topology_Device(n_cells: int, faces_c: np.ndarray) -> Matrix_Type:
+    """Matrix_Mod_Topology built on the GPU (tfs_topology_build_device): the
+    same row/col/dia/mir/pos as Matrix_Mod_Topology, bit for bit."""
+    lib = load_library()
+    fc = np.ascontiguousarray(faces_c, dtype=np.int32).reshape(-1)
+    n_faces = fc.size // 2
+    cap = n_cells + 2 * n_faces
+    sizes = {"fc": max(fc.nbytes, 4), "row": 4 * (n_cells + 1), "col": 4 * cap, "dia": 4 * n_cells,
+             "mir": 4 * cap, "pos": 4 * max(2 * n_faces, 1)}
+    dev = {}
+    try:
+        for k, nb in sizes.items():
+            q = C.c_void_p()
+            check(lib.tfs_device_alloc(nb, C.byref(q)), "tfs_device_alloc")
+            dev[k] = q.value
+        check(lib.tfs_memcpy(C.c_void_p(dev["fc"]), fc.ctypes.data_as(C.c_void_p), fc.nbytes), "tfs_memcpy")
+        nnz = C.c_int32()
+        check(lib.tfs_topology_build_device(n_cells, n_faces, *(C.c_void_p(dev[k]) for k in
+                                                               ("fc", "row", "col", "dia", "mir", "pos")),
+                                            C.byref(nnz)), "tfs_topology_build_device")
+        nnz = nnz.value
+        out = {"row": np.zeros(n_cells + 1, np.int32), "col": np.zeros(nnz, np.int32),
+               "dia": np.zeros(n_cells, np.int32), "mir": np.zeros(nnz, np.int32),
+               "pos": np.zeros(2 * n_faces, np.int32)}
+        for k, a in out.items():
+            check(lib.tfs_memcpy(a.ctypes.data_as(C.c_void_p), C.c_void_p(dev[k]), a.nbytes), "tfs_memcpy")
+    finally:
+        for d in dev.values():
+            lib.tfs_device_free(C.c_void_p(d))
+    return Matrix_Type(n_cells, out["row"], out["col"], out["dia"], np.zeros(nnz), mir=out["mir"],
+                       pos=out["pos"].reshape(-1, 2))
