@@ -51,6 +51,9 @@ struct BatchCtl {
 };
 
 #define TFS_BATCH_MAX_TPB 512
+#ifndef TFS_BATCH_MIN_BLOCKS
+#define TFS_BATCH_MIN_BLOCKS 2   // at most 64 registers: 4 CTAs of 256 threads per SM
+#endif
 
 // Sum of NV values over the cluster: block sum, one partial per CTA in
 // shared memory, cluster barrier, every thread adds the C partials in rank
@@ -373,7 +376,8 @@ __global__ void k_batch_gather(BatchSys *sys, BatchCtl *ctl, int mixed)
 }
 
 template <int METHOD, typename VT>
-__global__ void k_batch(BatchSys *sys, const int *order, int n_sys, BatchCtl *ctl)
+__global__ void __launch_bounds__(TFS_BATCH_MAX_TPB, TFS_BATCH_MIN_BLOCKS)
+k_batch(BatchSys *sys, const int *order, int n_sys, BatchCtl *ctl)
 {
     cg::cluster_group cl = cg::this_cluster();
     __shared__ double s_part[2][4];
