@@ -51,8 +51,13 @@ struct BatchCtl {
 };
 
 #define TFS_BATCH_MAX_TPB 512
+// Resident CTAs of 512 threads per SM the kernel is compiled for (at most
+// 65536 / (512 * 3) = 42 registers, with some spilling).  Measured on the
+// 256-system batch (mixed, best cluster shape each): 1 -> 422, 2 -> 499,
+// 3 -> 584, 4 -> 545 solves/s; the latency-bound solves gain more from
+// resident warps than they lose to the spills.
 #ifndef TFS_BATCH_MIN_BLOCKS
-#define TFS_BATCH_MIN_BLOCKS 2   // at most 64 registers: 4 CTAs of 256 threads per SM
+#define TFS_BATCH_MIN_BLOCKS 3
 #endif
 
 // Sum of NV values over the cluster: block sum, one partial per CTA in
