@@ -369,24 +369,4 @@ k_dic_apply(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, 
     }
 }
 
-// One level of a sweep with two rows per thread whose gathers are issued
-// together (the level-kernel schedule of tfs_engine.cu, TFS_LEVEL_R2=1):
-// half the threads of k_sweep_level, so the next level's blocks can become
-// resident, load their rows' geometry and wait in the dependency
-// synchronisation while this level runs.
-template <typename T, int MODE>
-__global__ void __launch_bounds__(TFS_TPB)
-k_sweep_level_r2(SellDev A, const T *__restrict__ val, const T *d, const T *b1, T *o1, const T *y1,
-                 int row0, int row1, DevState *st, int first)
-{
-    DicRows<T, 2> cur;
-    cur.template fetch<MODE>(A, val, row0 + blockIdx.x * (2 * TFS_TPB) + threadIdx.x, row1, TFS_TPB);
-    cudaTriggerProgrammaticLaunchCompletion();
-    cudaGridDependencySynchronize();
-    if (st->done) return;
-    if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    T acc = (T)0;
-    cur.template run<MODE, false>(A, val, d, b1, y1, o1, nullptr, acc);
-}
-
 }  // namespace tfs

@@ -130,17 +130,6 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
         const int bs = h->level_tpb;
         const int nb = (r1 - r0 + bs - 1) / bs;
         cudaError_t e;
-        if constexpr (NR == 1 && MODE != 2) {
-            if (h->level_r2) {
-                const int nb2 = (r1 - r0 + 2 * TFS_TPB - 1) / (2 * TFS_TPB);
-                e = launch_ex(pdl, k_sweep_level_r2<T, MODE>, nb2, TFS_TPB, s, A, val, (const T *)d, b1, o1, y1,
-                              r0, r1, h->st, first);
-                if (e != cudaSuccess) return tfs_engine_error(e, "level launch");
-                first = 0;
-                (*count)++;
-                continue;
-            }
-        }
         if (bs == 1024)
             e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 1024>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         else if (bs == 512)
@@ -718,8 +707,6 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
-    env = getenv("TFS_LEVEL_R2");
-    if (env && strcmp(env, "1") == 0) h->level_r2 = 1;
     env = getenv("TFS_LEVEL_TPB");
     if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
     env = getenv("TFS_PDL");
