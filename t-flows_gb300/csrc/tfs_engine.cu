@@ -106,7 +106,7 @@ static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int b
 template <typename T, int NR, int MODE>
 static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, const T *b1, const T *b2,
                          T *o1, T *o2, const T *y1, const T *y2, int *count, bool with_tail = true,
-                         int tail_at = -1)
+                         int tail_at = -1, int lvl_from = 0)
 {
     SellDev A = sell_of(h);
     const int L = h->n_levels, tail = tail_at >= 0 ? tail_at : h->tail_level;
@@ -126,6 +126,7 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
     }
     for (int q = 0; q < tail; q++) {
         const int l = MODE == 1 ? tail - 1 - q : q;
+        if (l < lvl_from) continue;
         const int r0 = h->lvl_begin[l], r1 = h->lvl_begin[l + 1];
         const int bs = h->level_tpb;
         const int nb = (r1 - r0 + bs - 1) / bs;
@@ -707,6 +708,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
+    env = getenv("TFS_FUSE_L0");
+    if (env && strcmp(env, "0") == 0) h->fuse_l0 = 0;
     env = getenv("TFS_LEVEL_TPB");
     if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
     env = getenv("TFS_PDL");
@@ -843,7 +846,7 @@ static int launch_dic(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *
 
 template <typename T>
 static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, const T *b2,
-                         T *y1, T *y2, T *z1, T *z2, int *count)
+                         T *y1, T *y2, T *z1, T *z2, int *count, bool fuse_l0 = false)
 {
     SellDev A = sell_of(h);
     if (h->sweep_mode == 2 && nr == 1) return launch_dic<T, false>(h, s, b1, y1, z1, nullptr, count);
@@ -898,9 +901,22 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
     };
     if (nr == 1) {
-        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
+        // fuse_l0 (binary32 CG): the forward sweep of level 0 is done by the
+        // update / true-residual kernels, and the backward sweep of level 0
+        // by k_mx_sweep0_rho together with rho.
+        const int from = fuse_l0 ? 1 : 0;
+        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
-        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at))) return rc;
+        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from))) return rc;
+        if constexpr (sizeof(T) == 4) {
+            if (fuse_l0) {
+                const int l0 = h->lvl_begin[1];
+                cudaError_t e = launch_ex(h->use_pdl != 0, k_mx_sweep0_rho, (l0 + T_ - 1) / T_, T_, s, A, val,
+                                          (const float *)d, b1, z1, (const float *)y1, l0, h->n_int, h->st, h->part);
+                (*count)++;
+                if (e != cudaSuccess) return tfs_engine_error(e, "level-0 sweep launch");
+            }
+        }
     } else {
         if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 2>, k_sweep_tailc<T, 2>))) return rc;
@@ -911,6 +927,18 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 
 // ------------------------------------------------ mixed-precision graphs
 
+// Rows of DIC level 0 whose forward sweep the binary32 CG kernels take over
+// (k_mx_true, k_mx_cg_update4: y = r D) and whose backward sweep runs with
+// rho in k_mx_sweep0_rho, or 0 when the plain level schedule runs.  Level 0
+// must be one of the per-level kernels (not part of a tail).
+static int mixed_l0_rows(const tfs_handle *h, int method, int prec)
+{
+    if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0 || !h->vec4) return 0;
+    const int tail_at = h->tail_cluster > 1 ? h->ctail_level : h->tail_level;
+    if (tail_at < 1 || h->lvl_begin.size() < 2) return 0;
+    return h->lvl_begin[1];
+}
+
 // After the binary64 preconditioner is formed: d32 = (float) d, then the
 // binary64 initial residual (k_mx_true<INIT>).
 static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
@@ -919,7 +947,8 @@ static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int pre
     SellDev A = sell_of(h);
     const int G = h->grid, T = TFS_TPB;
     k_mx_cast<<<G, T, 0, s>>>(h->n_int, h->v.d, h->f.d);
-    if (method == TFS_CG) k_mx_true<0, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
+    if (method == TFS_CG) k_mx_true<0, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond,
+                                                             mixed_l0_rows(h, method, prec));
     else if (method == TFS_BICG) k_mx_true<1, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
     else k_mx_true<2, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
     CKL("mixed prologue");
@@ -960,6 +989,15 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            *count += 5;
+        } else if (prec == 2 && mixed_l0_rows(h, method, prec) > 0) {
+            const int l0 = mixed_l0_rows(h, method, prec);
+            if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count, true))) return rc;
+            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
+            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part, l0 / 4);
+            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
+            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond, l0);
             *count += 5;
         } else if (prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;

@@ -38,7 +38,7 @@ __global__ void k_mx_cast(int n_int, const double *__restrict__ src, float *__re
 template <int METHOD, bool INIT>
 __global__ void __launch_bounds__(TFS_TPB)
 k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState *st,
-          double *part, int prec, cudaGraphConditionalHandle cond)
+          double *part, int prec, cudaGraphConditionalHandle cond, int l0_rows = 0)
 {
     if (st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
@@ -60,6 +60,9 @@ k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState 
         V.r[i] = r;
         float r32 = (float)r;
         F.r[i] = r32;
+        // DIC level 0 has no lower neighbours: its forward sweep is y = r D,
+        // done here (and in k_mx_cg_update4) instead of in a level kernel.
+        if (i < l0_rows) F.y[i] = r32 * F.d[i];
         // The shadow residual of the reference's BiCG equals r1 at every step
         // (it starts as r1 and is driven by A, not A^T), so a reliable update
         // resets it together with r1; CGS keeps its initial shadow.
@@ -282,7 +285,8 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho4(int n4, Vec32 F, DevSta
 }
 
 template <bool FUSED>
-__global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part)
+__global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part,
+                                                           int l0_rows4 = 0)
 {
     const bool stop = (st->done | st->need_true) != 0;
     const float a = st->alpha32;             // (float) alpha, published once
@@ -296,6 +300,10 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevS
         e4[v] = make_float4(fmaf(a, p.x, e.x), fmaf(a, p.y, e.y), fmaf(a, p.z, e.z), fmaf(a, p.w, e.w));
         r = make_float4(fmaf(-a, q.x, r.x), fmaf(-a, q.y, r.y), fmaf(-a, q.z, r.z), fmaf(-a, q.w, r.w));
         r4[v] = r;
+        if (v < l0_rows4) {   // forward sweep of DIC level 0: y = r D (no lower neighbours)
+            const float4 dd = d4[v];
+            ((float4 *)F.y)[v] = make_float4(r.x * dd.x, r.y * dd.y, r.z * dd.z, r.w * dd.w);
+        }
         e2 = fmaf(r.x, r.x, e2); e2 = fmaf(r.y, r.y, e2); e2 = fmaf(r.z, r.z, e2); e2 = fmaf(r.w, r.w, e2);
         if (FUSED) {
             float4 z = make_float4(r.x / d.x, r.y / d.y, r.z / d.z, r.w / d.w);
@@ -321,6 +329,51 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_fold4(int n4, Vec64 V, Vec32 F, 
         x2[2 * v] = xa;
         x2[2 * v + 1] = xb;
         e4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// The last kernel of the binary32 DIC application for CG: the backward
+// sweep of level 0 (rows [0, l0_rows), as k_sweep_level) fused with
+// rho = (r, z) over all rows (k_mx_dot_rho4's job): a thread adds r_i z_i of
+// its own level-0 row from the value it just computed, and of the rows above
+// level 0 (final since the earlier level kernels) over a grid-stride loop.
+__global__ void __launch_bounds__(TFS_TPB)
+k_mx_sweep0_rho(SellDev A, const float *__restrict__ val, const float *d, const float *r, float *z,
+                const float *y, int l0_rows, int n_int, DevState *st, double *part)
+{
+    const int i = blockIdx.x * TFS_TPB + threadIdx.x;
+    const bool active = i < l0_rows;
+    RowGeom g{0, 0, 0};
+    int kk[4] = {0, 0, 0, 0};
+    float aa[4] = {0.f, 0.f, 0.f, 0.f};
+    if (active) {
+        g = row_geom(A, i);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (g.dpos + 1 + q < g.len) {
+                const int ee = g.off + ((g.dpos + 1 + q) << 5);
+                kk[q] = __ldg(A.col + ee);
+                aa[q] = __ldg(val + ee);
+            }
+    }
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    const bool stop = (st->done | st->need_true) != 0;
+    float acc = 0.f;
+    if (active) {
+        sweep_row<float, 1, 1, 4>(A, val, (float *)d, nullptr, nullptr, z, nullptr, y, nullptr, i, g, kk, aa, stop);
+        if (!stop) acc = fmaf(r[i], z[i], acc);
+    }
+    for (int k = l0_rows + blockIdx.x * TFS_TPB + threadIdx.x; k < n_int; k += gridDim.x * TFS_TPB)
+        acc = fmaf(r[k], __ldcg(z + k), acc);
+    if (stop) return;
+    const float av[1] = {acc};
+    double v[1];
+    if (grid_reduce_f<1>(av, v, part, &st->counter)) {
+        st->rho = v[0];
+        if (st->iter > 1) publish_beta(st);
+        st->sweep_ns += gtimer() - st->t_sweep0;
+        st->sweep_n += 1;
     }
 }
 
