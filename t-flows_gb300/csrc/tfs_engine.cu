@@ -399,7 +399,7 @@ static void free_layout(tfs_handle *h)
 // RCM position inside a level) which every preconditioner can use.
 static int build_layout(tfs_handle *h, int kind)
 {
-    const int n = h->n, nnz = h->nnz;
+    const int n = h->n;
     const std::vector<int> &row0 = h->row0, &col0 = h->col0, &dia0 = h->dia0;
     CK(cudaStreamSynchronize(h->stream));
     free_layout(h);
@@ -745,7 +745,6 @@ extern "C" int tfs_set_precision(tfs_handle *h, int mode)
 static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
     SellDev A = sell_of(h);
-    const int T = TFS_TPB;
     if (h->sweep_mode == 1) {
         k_sweep_lv<double, 1, 2><<<h->sweep_grid, TFS_SWEEP_TPB, 0, s>>>(A, h->val, h->v.d, nullptr, nullptr, nullptr,
                                                              nullptr, nullptr, nullptr, tile_table(h), h->ctl,

@@ -98,14 +98,12 @@ static bool make_room(tfs_server *S, int64_t need, int64_t keep)
 {
     while (S->resident + need > S->budget) {
         System *victim = nullptr;
-        int64_t vid = 0;
         for (auto &kv : S->systems) {
             System &sy = kv.second;
             if (!sy.h || sy.busy || kv.first == keep) continue;
-            if (!victim || sy.last_used < victim->last_used) { victim = &sy; vid = kv.first; }
+            if (!victim || sy.last_used < victim->last_used) victim = &sy;
         }
         if (!victim) return false;
-        (void)vid;
         release_system(S, *victim);
     }
     return true;
