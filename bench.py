@@ -209,6 +209,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     t0 = time.perf_counter()
     sol = tflows.Solver(s.matrix())
     log(f"[bench] registered: {sol.stats()['n_levels']} levels ({time.perf_counter() - t0:.1f}s)")
+    # Launch shapes of the single-solve kernels, picked on this system
+    # (tfs_autotune) before anything is timed.
+    tune = None
+    if not args.no_autotune:
+        tune = sol.autotune(s.val, TFS_MIXED, prec, 5)
+        log(f"[bench] autotune: {tune}")
     n, nnz = s.n, s.nnz
     tol = REL_TOL * float(np.linalg.norm(s.b))
     h = sol.h
@@ -385,7 +391,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         "spmv": {"fp64_us": round(spmv64_ms * 1e3, 2), "fp32_us": round(spmv32_ms * 1e3, 2),
                  "fp64_gbs": round(bytes64 / (spmv64_ms * 1e-3) / 1e9, 1),
                  "fp32_gbs": round(achieved, 1), "timing": "CUDA events, back-to-back launches"},
-        "roofline": roof, "roofline_spmv": roof_spmv, "next_rows": next_rows,
+        "roofline": roof, "roofline_spmv": roof_spmv, "autotune": tune, "next_rows": next_rows,
         "e2e": e2e, "gpu_launches": int(timed_launches),
         "clocks": clock_info,
     }
@@ -960,6 +966,8 @@ def main(argv=None) -> int:
     ap.add_argument("--ref-sample-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes of the single-solve kernels")
     ap.add_argument("--no-next-rows", action="store_true",
                     help="skip the device topology / assembly measurements")
     ap.add_argument("--modes", default="fp64,mixed",

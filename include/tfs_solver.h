@@ -177,6 +177,28 @@ int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int reps,
 int tfs_time_prec(tfs_handle *h, const double *val, int mode, int reps,
                   double *ms_per_application);
 
+/* Launch shapes picked for one handle by tfs_autotune, with the timings
+ * they were picked from (0 where a candidate was not timed). */
+typedef struct tfs_tuning {
+    int32_t level_tpb;        /* threads per block of the DIC level kernels  */
+    int32_t spmv_chunks;      /* 1: one 256-row chunk per SpMV block,
+                                 0: 8 blocks per SM, grid-stride            */
+    double  prec_ms[4];       /* DIC application, level_tpb 128/256/512/1024 */
+    double  spmv_ms[2];       /* SpMV, spmv_chunks 0 / 1                     */
+} tfs_tuning;
+
+/* Time the candidate launch shapes of the single-solve kernels on this
+ * handle's own system (values val, host, nnz) in the given arithmetic and
+ * keep the fastest: the SpMV grid always, the DIC level-kernel block size
+ * when prec == 2 (this builds the level layout if the handle has none).
+ * Graphs built earlier for the handle are dropped and rebuilt on the next
+ * solve.  Results do not depend on the shapes (per-row arithmetic and
+ * reductions are shape-independent except for the order of the block
+ * partial sums).  No reference counterpart: the reference has no launch
+ * shapes. */
+int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec, int reps,
+                 tfs_tuning *out);
+
 /* Human-readable text for a status code. */
 const char *tfs_status_string(int status);
 

@@ -1597,6 +1597,59 @@ extern "C" int tfs_time_prec(tfs_handle *h, const double *val, int mode, int rep
     return TFS_OK;
 }
 
+// Autotuner of the single-solve launch shapes: every candidate is timed on
+// the handle's own system with the same timers as tfs_time_spmv /
+// tfs_time_prec, the fastest is kept, and the cached graphs (which hold the
+// launch shapes) are dropped.
+extern "C" int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec, int reps,
+                            tfs_tuning *out)
+{
+    if (!h || !val || !out || reps < 1 || (mode != TFS_FP64 && mode != TFS_MIXED) || prec < 0 || prec > 2)
+        return TFS_ERR_ARG;
+    memset(out, 0, sizeof(*out));
+    int rc;
+    if (prec == 2) {
+        static const int cand[4] = {128, 256, 512, 1024};
+        const int keep = h->level_tpb;
+        int best = keep;
+        double best_ms = 0.0;
+        for (int k = 0; k < 4; k++) {
+            h->level_tpb = cand[k];
+            double ms = 0.0;
+            if ((rc = tfs_time_prec(h, val, mode, reps, &ms))) { h->level_tpb = keep; return rc; }
+            out->prec_ms[k] = ms;
+            if (k == 0 || ms < best_ms) { best_ms = ms; best = cand[k]; }
+        }
+        h->level_tpb = best;
+    } else if ((rc = ensure_layout(h, prec))) {
+        return rc;
+    }
+    {
+        const int keep = h->grid_spmv;
+        const int cand[2] = {h->grid, h->n_chunks};
+        int best = keep;
+        double best_ms = 0.0;
+        for (int k = 0; k < 2; k++) {
+            h->grid_spmv = cand[k];
+            double ms = 0.0;
+            if ((rc = tfs_time_spmv(h, val, mode, reps, &ms))) { h->grid_spmv = keep; return rc; }
+            out->spmv_ms[k] = ms;
+            if (k == 0 || ms < best_ms) { best_ms = ms; best = cand[k]; }
+        }
+        h->grid_spmv = best;
+    }
+    // The part buffer holds TFS_NPART partials per chunk: both grids fit.
+    for (auto &kv : h->graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    h->graphs.clear();
+    h->last_graph = nullptr;
+    out->level_tpb = h->level_tpb;
+    out->spmv_chunks = h->grid_spmv == h->n_chunks && h->grid_spmv != h->grid ? 1 : 0;
+    return TFS_OK;
+}
+
 // ------------------------------------------------------ device helpers
 
 extern "C" int tfs_use_device(int device)

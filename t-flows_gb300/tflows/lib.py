@@ -23,6 +23,11 @@ i32, i64, u64, dbl = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 P_i32, P_dbl, P_void = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p
 
 
+class tfs_tuning(C.Structure):
+    _fields_ = [("level_tpb", C.c_int32), ("spmv_chunks", C.c_int32),
+                ("prec_ms", C.c_double * 4), ("spmv_ms", C.c_double * 2)]
+
+
 class tfs_stats(C.Structure):
     _fields_ = [("iterations", i32), ("true_residuals", i32), ("n_levels", i32), ("status", i32),
                 ("solve_ms", dbl), ("spmv_ns_total", dbl), ("spmv_launches", i64),
@@ -65,6 +70,7 @@ SIGNATURES = {
     "tfs_get_levels": (C.c_int, [P_void, P_i32]),
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_time_prec": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
+    "tfs_autotune": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "tfs_faces_register": (C.c_int, [P_void, C.c_int32, P_i32, P_i32]),
     "tfs_assemble_faces_device": (C.c_int, [P_void, P_void, P_void, P_void, P_void, P_void, P_void]),
     "tfs_status_string": (C.c_char_p, [C.c_int]),

@@ -177,6 +177,17 @@ class Solver:
                 self.lib.tfs_device_free(C.c_void_p(d))
         return val
 
+    def autotune(self, val: np.ndarray, mode: int = TFS_FP64, prec: int = 2, reps: int = 10) -> dict:
+        """Time the candidate launch shapes on this system and keep the
+        fastest (tfs_autotune); returns the choice and the timings."""
+        from .lib import tfs_tuning
+        t = tfs_tuning()
+        check(self.lib.tfs_autotune(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), mode, prec, reps,
+                                    C.byref(t)), "tfs_autotune")
+        return {"level_tpb": t.level_tpb, "spmv_chunks": t.spmv_chunks,
+                "prec_ms": {c: t.prec_ms[k] for k, c in enumerate((128, 256, 512, 1024))},
+                "spmv_ms": {"sm8": t.spmv_ms[0], "chunks": t.spmv_ms[1]}}
+
     def time_prec(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
         """Milliseconds per DIC preconditioner application (both sweeps)."""
         ms = _dbl(0.0)

@@ -395,3 +395,23 @@ def test_bicg_nonconvergence_matches_reference(convdiff12):
     res = sol.solve(TFS_BICG, s.val, x, r, 1, 300, ref["tol"])
     assert ref["niter"] == 301 and res.niter == 301
     assert res.fin_res == pytest.approx(ref["fin"], rel=1e-6)
+
+
+@pytest.mark.parametrize("mode", [TFS_FP64, TFS_MIXED])
+def test_autotune_keeps_parity(mode, gpu):
+    """tfs_autotune times the launch-shape candidates on the handle's own
+    system, keeps the fastest and drops the cached graphs; solves after it
+    still meet the parity gates."""
+    s = system(POISSON, 40, 40, 40)
+    ref = oracle_solve(s, TFS_CG, 2)
+    with Solver(s.matrix(), precision=mode) as sol:
+        x, r = np.zeros(s.n), s.b.copy()
+        sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])      # a graph exists before tuning
+        t = sol.autotune(s.val, mode, 2, 3)
+        assert t["level_tpb"] in (128, 256, 512, 1024) and t["spmv_chunks"] in (0, 1)
+        assert all(v > 0 for v in t["prec_ms"].values()) and all(v > 0 for v in t["spmv_ms"].values())
+        assert t["prec_ms"][t["level_tpb"]] == min(t["prec_ms"].values())
+        x, r = np.zeros(s.n), s.b.copy()
+        res = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
+        assert res.status == 0 and res.fin_res < ref["tol"] and iter_ok(res.niter, ref["niter"])
+        assert rel_l2(x, ref["x"]) <= (SOL_REL if mode == TFS_FP64 else 1e-6)
