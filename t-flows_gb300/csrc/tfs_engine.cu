@@ -709,7 +709,7 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
     env = getenv("TFS_FUSE_L0");
-    if (env && strcmp(env, "0") == 0) h->fuse_l0 = 0;
+    if (env && (strcmp(env, "0") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
     env = getenv("TFS_LEVEL_TPB");
     if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
     env = getenv("TFS_PDL");
@@ -759,6 +759,7 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 }
 
 static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int prec, cudaGraphConditionalHandle cond);
+static int dic_l0_rows(const tfs_handle *h, int method, int prec);
 static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec, cudaGraphConditionalHandle cond, int *count);
 static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst);
 static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s);
@@ -780,7 +781,8 @@ static int launch_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
         tfs_mixed_prologue(h, s, method, prec, cond);
         *count += 2;
     } else {
-        if (method == TFS_CG) k_residual<0><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
+        if (method == TFS_CG) k_residual<0><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond,
+                                                            dic_l0_rows(h, method, prec));
         else if (method == TFS_BICG) k_residual<1><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
         else k_residual<2><<<G, T, 0, s>>>(A, h->val, h->v, h->st, h->part, prec, cond);
         *count += 1;
@@ -900,21 +902,19 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
     };
     if (nr == 1) {
-        // fuse_l0 (binary32 CG): the forward sweep of level 0 is done by the
-        // update / true-residual kernels, and the backward sweep of level 0
-        // by k_mx_sweep0_rho together with rho.
+        // fuse_l0 (CG): the forward sweep of level 0 is done by the update /
+        // true-residual kernels, and the backward sweep of level 0 by
+        // k_sweep0_rho together with rho.
         const int from = fuse_l0 ? 1 : 0;
         if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
         if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from))) return rc;
-        if constexpr (sizeof(T) == 4) {
-            if (fuse_l0) {
-                const int l0 = h->lvl_begin[1];
-                cudaError_t e = launch_ex(h->use_pdl != 0, k_mx_sweep0_rho, (l0 + T_ - 1) / T_, T_, s, A, val,
-                                          (const float *)d, b1, z1, (const float *)y1, l0, h->n_int, h->st, h->part);
-                (*count)++;
-                if (e != cudaSuccess) return tfs_engine_error(e, "level-0 sweep launch");
-            }
+        if (fuse_l0) {
+            const int l0 = h->lvl_begin[1];
+            cudaError_t e = launch_ex(h->use_pdl != 0, k_sweep0_rho<T>, (l0 + T_ - 1) / T_, T_, s, A, val,
+                                      (const T *)d, b1, z1, (const T *)y1, l0, h->n_int, h->st, h->part);
+            (*count)++;
+            if (e != cudaSuccess) return tfs_engine_error(e, "level-0 sweep launch");
         }
     } else {
         if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
@@ -926,13 +926,18 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 
 // ------------------------------------------------ mixed-precision graphs
 
-// Rows of DIC level 0 whose forward sweep the binary32 CG kernels take over
-// (k_mx_true, k_mx_cg_update4: y = r D) and whose backward sweep runs with
-// rho in k_mx_sweep0_rho, or 0 when the plain level schedule runs.  Level 0
-// must be one of the per-level kernels (not part of a tail).
-static int mixed_l0_rows(const tfs_handle *h, int method, int prec)
+// Rows of DIC level 0 whose forward sweep the CG kernels take over
+// (k_mx_true, k_mx_cg_update4, k_residual, k_cg_update: y = r D) and whose
+// backward sweep runs with rho in k_sweep0_rho, or 0 when the plain level
+// schedule runs.  Level 0 must be one of the per-level kernels (not part of
+// a tail).  fuse_l0 = 1 fuses the binary32 iteration only: in binary64 the
+// fused body measured slower on the 128^3 Poisson system (5.98 against 6.11
+// solves/s), so it runs there only with fuse_l0 = 2.
+static int dic_l0_rows(const tfs_handle *h, int method, int prec)
 {
-    if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0 || !h->vec4) return 0;
+    if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0) return 0;
+    if (h->precision == TFS_MIXED && !h->vec4) return 0;
+    if (h->precision != TFS_MIXED && h->fuse_l0 != 2) return 0;
     const int tail_at = h->tail_cluster > 1 ? h->ctail_level : h->tail_level;
     if (tail_at < 1 || h->lvl_begin.size() < 2) return 0;
     return h->lvl_begin[1];
@@ -947,7 +952,7 @@ static int tfs_mixed_prologue(tfs_handle *h, cudaStream_t s, int method, int pre
     const int G = h->grid, T = TFS_TPB;
     k_mx_cast<<<G, T, 0, s>>>(h->n_int, h->v.d, h->f.d);
     if (method == TFS_CG) k_mx_true<0, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond,
-                                                             mixed_l0_rows(h, method, prec));
+                                                             dic_l0_rows(h, method, prec));
     else if (method == TFS_BICG) k_mx_true<1, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
     else k_mx_true<2, true><<<G, T, 0, s>>>(A, h->val, h->v, h->f, h->st, h->part, prec, cond);
     CKL("mixed prologue");
@@ -989,8 +994,8 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 5;
-        } else if (prec == 2 && mixed_l0_rows(h, method, prec) > 0) {
-            const int l0 = mixed_l0_rows(h, method, prec);
+        } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
+            const int l0 = dic_l0_rows(h, method, prec);
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count, true))) return rc;
             k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
             k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
@@ -1082,6 +1087,13 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 2;
+        } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
+            const int l0 = dic_l0_rows(h, method, prec);
+            if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count, true))) return rc;
+            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
+            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond, l0);
+            *count += 3;
         } else if (prec == 2) {
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
             k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);

@@ -428,7 +428,7 @@ k_dic_form(SellDev A, const double *__restrict__ val, double *d, int row0, int r
 template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)
 k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, double *part,
-           int prec, cudaGraphConditionalHandle cond)
+           int prec, cudaGraphConditionalHandle cond, int l0_rows = 0)
 {
     if (st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
@@ -441,6 +441,7 @@ k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
         RowGeom g = row_geom(A, i);
         double r = row_accum<true, double, double, double, TFS_SPMV_NC>(V.r[i], A.col, val, V.x, g.off, 0, g.len);
         V.r[i] = r;
+        if (i < l0_rows) V.y[i] = r * V.d[i];   // forward sweep of DIC level 0
         if (METHOD != 0) V.r2[i] = r;
         e2 = fma(r, r, e2);
         if (METHOD == 2) rz = fma(r, r, rz);            // Cgs.f90:105-109, r2 = r1
@@ -965,7 +966,8 @@ k_spmv_pq(SellDev A, const double *__restrict__ val, const double *__restrict__ 
 // FUSED also rho of the next iteration, (r, r/d).
 template <bool FUSED>
 __global__ void __launch_bounds__(TFS_TPB)
-k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond)
+k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond,
+            int l0_rows = 0)
 {
     const bool stop = st->done != 0;
     const double alfa = st->alpha;
@@ -980,6 +982,8 @@ k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditio
             V.x[i] = x[_q] + alfa * p[_q];
             double rn = r[_q] - alfa * q[_q];
             V.r[i] = rn;
+            // DIC level 0 has no lower neighbours: its forward sweep y = r D.
+            if (i < l0_rows) V.y[i] = rn * V.d[i];
             e2 = fma(rn, rn, e2);
             if (FUSED) { double z = rn / d[_q]; V.z[i] = z; rz = fma(rn, z, rz); }
         }

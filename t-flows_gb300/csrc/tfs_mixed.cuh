@@ -332,20 +332,22 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_fold4(int n4, Vec64 V, Vec32 F, 
     }
 }
 
-// The last kernel of the binary32 DIC application for CG: the backward
-// sweep of level 0 (rows [0, l0_rows), as k_sweep_level) fused with
-// rho = (r, z) over all rows (k_mx_dot_rho4's job): a thread adds r_i z_i of
+// The last kernel of the DIC application of CG: the backward sweep of
+// level 0 (rows [0, l0_rows), as k_sweep_level) fused with rho = (r, z) over
+// all rows (the job of k_dot_rho / k_mx_dot_rho4): a thread adds r_i z_i of
 // its own level-0 row from the value it just computed, and of the rows above
 // level 0 (final since the earlier level kernels) over a grid-stride loop.
+// Binary32 (T = float, compensated warp sums) or binary64 (fma partials).
+template <typename T>
 __global__ void __launch_bounds__(TFS_TPB)
-k_mx_sweep0_rho(SellDev A, const float *__restrict__ val, const float *d, const float *r, float *z,
-                const float *y, int l0_rows, int n_int, DevState *st, double *part)
+k_sweep0_rho(SellDev A, const T *__restrict__ val, const T *d, const T *r, T *z, const T *y, int l0_rows,
+             int n_int, DevState *st, double *part)
 {
     const int i = blockIdx.x * TFS_TPB + threadIdx.x;
     const bool active = i < l0_rows;
     RowGeom g{0, 0, 0};
     int kk[4] = {0, 0, 0, 0};
-    float aa[4] = {0.f, 0.f, 0.f, 0.f};
+    T aa[4] = {(T)0, (T)0, (T)0, (T)0};
     if (active) {
         g = row_geom(A, i);
 #pragma unroll
@@ -359,17 +361,29 @@ k_mx_sweep0_rho(SellDev A, const float *__restrict__ val, const float *d, const 
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
     const bool stop = (st->done | st->need_true) != 0;
-    float acc = 0.f;
+    T acc = (T)0;
     if (active) {
-        sweep_row<float, 1, 1, 4>(A, val, (float *)d, nullptr, nullptr, z, nullptr, y, nullptr, i, g, kk, aa, stop);
-        if (!stop) acc = fmaf(r[i], z[i], acc);
+        sweep_row<T, 1, 1, 4>(A, val, (T *)d, nullptr, nullptr, z, nullptr, y, nullptr, i, g, kk, aa, stop);
+        if (!stop) {
+            if constexpr (sizeof(T) == 4) acc = fmaf(r[i], z[i], acc);
+            else acc = fma(r[i], z[i], acc);
+        }
     }
-    for (int k = l0_rows + blockIdx.x * TFS_TPB + threadIdx.x; k < n_int; k += gridDim.x * TFS_TPB)
-        acc = fmaf(r[k], __ldcg(z + k), acc);
+    for (int k = l0_rows + blockIdx.x * TFS_TPB + threadIdx.x; k < n_int; k += gridDim.x * TFS_TPB) {
+        if constexpr (sizeof(T) == 4) acc = fmaf(r[k], __ldcg(z + k), acc);
+        else acc = fma(r[k], __ldcg(z + k), acc);
+    }
     if (stop) return;
-    const float av[1] = {acc};
     double v[1];
-    if (grid_reduce_f<1>(av, v, part, &st->counter)) {
+    bool last;
+    if constexpr (sizeof(T) == 4) {
+        const float av[1] = {acc};
+        last = grid_reduce_f<1>(av, v, part, &st->counter);
+    } else {
+        v[0] = acc;
+        last = grid_reduce<1>(v, part, &st->counter);
+    }
+    if (last) {
         st->rho = v[0];
         if (st->iter > 1) publish_beta(st);
         st->sweep_ns += gtimer() - st->t_sweep0;

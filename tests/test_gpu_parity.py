@@ -329,6 +329,22 @@ def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
                 assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) < 1e-6
 
 
+@pytest.mark.parametrize("fuse", ["0", "1", "2"])
+def test_level0_fusion_parity(fuse, monkeypatch, gpu):
+    """DIC-CG with level 0 swept inside the residual, update and rho kernels
+    (TFS_FUSE_L0: 0 off, 1 binary32 iteration, 2 binary64 too) stays within
+    the parity gates of the oracle in both precisions on the 40^3 system."""
+    monkeypatch.setenv("TFS_FUSE_L0", fuse)
+    s = system(POISSON, 40, 40, 40)
+    ref = oracle_solve(s, TFS_CG, 2)
+    for mode, sol_tol in ((TFS_FP64, SOL_REL), (TFS_MIXED, 1e-6)):
+        with Solver(s.matrix(), precision=mode) as sol:
+            x, r = np.zeros(s.n), s.b.copy()
+            res = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
+            assert res.status == 0 and res.fin_res < ref["tol"]
+            assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= sol_tol
+
+
 @pytest.mark.parametrize("mode", [TFS_FP64, TFS_MIXED])
 @pytest.mark.parametrize("prec", [1, 2])
 def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
@@ -344,6 +360,9 @@ def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
     non-symmetric system)."""
     s = system(CONVDIFF, 9, 8, 8)
     tol = 1e-8 * np.linalg.norm(s.b)
+    # Both runs reduce rho with the same kernel: the CG body's fusion of rho
+    # into the level-0 backward sweep sums the partials in another order.
+    monkeypatch.setenv("TFS_FUSE_L0", "0")
     out = {}
     for tag in ("cg", "literal"):
         if tag == "literal":
