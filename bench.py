@@ -173,6 +173,15 @@ def measured_peak_gbs() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+# Binary32 CG SpMV kernels by tfs_stats.spmv_kernel (W: the slice width).
+SPMV_KERNEL_NAMES = {
+    0: ("k_mx_spmv_pq", "direct: per-row dependent loads"),
+    1: ("k_spmv_pq_pipe<float,true,W>", "software-pipelined: next row's columns loaded during the gathers"),
+    2: ("k_spmv_pq_bulk<float,true>", "matrix tiles staged in shared memory by cp.async.bulk"),
+    3: ("k_spmv_pq_async<float,true,S>", "matrix tiles staged in shared memory by cp.async"),
+}
+
+
 def ncu_traffic(workload: str, kernel: str) -> float | None:
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
     p = REPO / "profiles" / "traffic.json"
@@ -353,11 +362,14 @@ def run_ours(args, dist: Dist) -> dict | None:
 
     peak, peak_src = measured_peak_gbs()
     achieved = bytes32 / (spmv32_ms * 1e-3) / 1e9
-    roof_spmv = {"kernel": "k_mx_spmv_pq (binary32 SELL-32 SpMV + (p,q))", "bound": "hbm",
+    st_k = sol.stats()
+    kname, kdesc = SPMV_KERNEL_NAMES.get(st_k["spmv_kernel"], ("k_mx_spmv_pq", "direct"))
+    kname = kname.replace("W", str(st_k["sell_width"]))
+    roof_spmv = {"kernel": f"{kname} (binary32 SELL-32 SpMV + (p,q), {kdesc})", "bound": "hbm",
                  "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                  "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
                  "algorithmic_bytes_per_launch": bytes32,
-                 "traffic": ncu_traffic(args.workload, "k_mx_spmv_pq"),
+                 "traffic": ncu_traffic(args.workload, kname.split("<")[0]),
                  "timing": "CUDA events, back-to-back launches on the handle's stream"}
     roof = roof_spmv
     if prec32_ms is not None:

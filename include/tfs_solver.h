@@ -87,6 +87,10 @@ typedef struct tfs_stats {
     int64_t  sweep_launches;
     int64_t  kernel_launches;   /* kernels launched by the last solve            */
     int64_t  device_bytes;      /* device memory held by the handle             */
+    int32_t  spmv_kernel;       /* SpMV kernel of the CG iterations: 0 direct,
+                                   1 software-pipelined, 2 bulk-copy,
+                                   3 cp.async-staged                          */
+    int32_t  sell_width;        /* uniform SELL-32 slice width, 0 if per slice  */
 } tfs_stats;
 
 /* ---- topology ----------------------------------------------------------- */
@@ -184,12 +188,17 @@ typedef struct tfs_tuning {
     int32_t spmv_chunks;      /* 1: one 256-row chunk per SpMV block,
                                  0: 8 blocks per SM, grid-stride            */
     double  prec_ms[4];       /* DIC application, level_tpb 128/256/512/1024 */
-    double  spmv_ms[2];       /* SpMV, spmv_chunks 0 / 1                     */
+    double  spmv_ms[2];       /* direct SpMV kernel, spmv_chunks 0 / 1       */
+    int32_t spmv_kernel;      /* SpMV kernel kept: 0 direct, 1 software-
+                                 pipelined, 2 bulk-copy, 3 cp.async-staged  */
+    int32_t pad;
+    double  spmv_pipe_ms[2];  /* software-pipelined SpMV, spmv_chunks 0 / 1
+                                 (0: matrix not of uniform slice width)     */
 } tfs_tuning;
 
 /* Time the candidate launch shapes of the single-solve kernels on this
  * handle's own system (values val, host, nnz) in the given arithmetic and
- * keep the fastest: the SpMV grid always, the DIC level-kernel block size
+ * keep the fastest: the SpMV kernel and grid always, the DIC level-kernel block size
  * when prec == 2 (this builds the level layout if the handle has none).
  * Graphs built earlier for the handle are dropped and rebuilt on the next
  * solve.  Results do not depend on the shapes (per-row arithmetic and

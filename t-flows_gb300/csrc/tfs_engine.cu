@@ -23,6 +23,7 @@
 #include "tfs_kernels.cuh"
 #include "tfs_mixed.cuh"
 #include "tfs_dic.cuh"
+#include "tfs_spmv.cuh"
 
 using namespace tfs;
 
@@ -170,6 +171,127 @@ static int dalloc(tfs_handle *h, T **p, size_t count)
     CK(cudaMalloc((void **)p, bytes));
     h->device_bytes += (int64_t)bytes;
     return TFS_OK;
+}
+
+// The SpMV kernel of the CG iterations: for uniform-width matrices the
+// software-pipelined kernel (default), the cp.async-staged kernel
+// (TFS_SPMV=async) or the bulk-copy kernel (TFS_SPMV=bulk) -- the staged
+// kernels with TFS_BULK_STAGES stages per block, resident blocks per SM from
+// the occupancy calculator, 16-byte aligned tile bases -- else (per-slice
+// widths or TFS_SPMV=direct) the direct kernels.  All give bitwise the same
+// results.
+template <typename K>
+static bool staged_occupancy(K kernel, int smem, int *occ)
+{
+    *occ = 0;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kernel, TFS_TPB, smem) != cudaSuccess || *occ < 1) {
+        cudaGetLastError();
+        *occ = 0;
+        return false;
+    }
+    return true;
+}
+
+static void spmv_kind_setup(tfs_handle *h)
+{
+    h->spmv_kind = TFS_SPMV_DIRECT;
+    h->bulk_occ32 = h->bulk_occ64 = 0;
+    if (h->sell_width <= 0 || h->sell_width > 8) return;
+    const char *env = getenv("TFS_SPMV");
+    if (env && strcmp(env, "direct") == 0) return;
+    h->spmv_kind = TFS_SPMV_PIPE;
+    const bool bulk = env && strcmp(env, "bulk") == 0, async = env && strcmp(env, "async") == 0;
+    if (!bulk && !async) return;
+    auto aligned = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+    if (!aligned(h->col) || !aligned(h->rowinfo) || !aligned(h->val) || !aligned(h->val32)) return;
+    int stages = 3;
+    env = getenv("TFS_BULK_STAGES");
+    if (env && atoi(env) >= 2 && atoi(env) <= TFS_BULK_MAX_STAGES) stages = atoi(env);
+    h->bulk_stages = stages;
+    h->bulk_smem32 = stages * bulk_stage_bytes<float>(h->sell_width);
+    h->bulk_smem64 = stages * bulk_stage_bytes<double>(h->sell_width);
+    bool ok;
+    if (bulk) {
+        ok = staged_occupancy(k_spmv_pq_bulk<float, true>, h->bulk_smem32, &h->bulk_occ32) &&
+             staged_occupancy(k_spmv_pq_bulk<double, false>, h->bulk_smem64, &h->bulk_occ64);
+    } else if (stages == 2) {
+        ok = staged_occupancy(k_spmv_pq_async<float, true, 2>, h->bulk_smem32, &h->bulk_occ32) &&
+             staged_occupancy(k_spmv_pq_async<double, false, 2>, h->bulk_smem64, &h->bulk_occ64);
+    } else if (stages == 3) {
+        ok = staged_occupancy(k_spmv_pq_async<float, true, 3>, h->bulk_smem32, &h->bulk_occ32) &&
+             staged_occupancy(k_spmv_pq_async<double, false, 3>, h->bulk_smem64, &h->bulk_occ64);
+    } else {
+        ok = staged_occupancy(k_spmv_pq_async<float, true, 4>, h->bulk_smem32, &h->bulk_occ32) &&
+             staged_occupancy(k_spmv_pq_async<double, false, 4>, h->bulk_smem64, &h->bulk_occ64);
+    }
+    if (!ok) {
+        h->bulk_occ32 = h->bulk_occ64 = 0;
+        return;
+    }
+    h->spmv_kind = bulk ? TFS_SPMV_BULK : TFS_SPMV_ASYNC;
+}
+
+template <typename VT, bool MIXED>
+static void launch_spmv_async(const tfs_handle *h, cudaStream_t s, int G, int smem, const VT *val, const VT *p,
+                              VT *q)
+{
+    const SellDev A = sell_of(h);
+    const int VG = h->grid_spmv;
+    if (h->bulk_stages == 2)
+        k_spmv_pq_async<VT, MIXED, 2><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
+    else if (h->bulk_stages == 3)
+        k_spmv_pq_async<VT, MIXED, 3><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
+    else
+        k_spmv_pq_async<VT, MIXED, 4><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
+}
+
+template <typename VT, bool MIXED>
+static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q)
+{
+    const SellDev A = sell_of(h);
+    const int G = h->grid_spmv;
+    switch (h->sell_width) {
+    case 1: k_spmv_pq_pipe<VT, MIXED, 1><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 2: k_spmv_pq_pipe<VT, MIXED, 2><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 3: k_spmv_pq_pipe<VT, MIXED, 3><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 4: k_spmv_pq_pipe<VT, MIXED, 4><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 5: k_spmv_pq_pipe<VT, MIXED, 5><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 6: k_spmv_pq_pipe<VT, MIXED, 6><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 7: k_spmv_pq_pipe<VT, MIXED, 7><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    default: k_spmv_pq_pipe<VT, MIXED, 8><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    }
+}
+
+// q = A p, (p, q) and alpha of a CG iteration on stream s, binary32 (mixed)
+// or binary64, with the handle's SpMV kernel over grid_spmv (virtual)
+// blocks.
+static void launch_spmv_pq(tfs_handle *h, cudaStream_t s, bool mixed)
+{
+    const SellDev A = sell_of(h);
+    const int VG = h->grid_spmv;
+    if (h->spmv_kind == TFS_SPMV_PIPE) {
+        if (mixed) launch_spmv_pipe<float, true>(h, s, h->val32, h->f.p, h->f.q);
+        else launch_spmv_pipe<double, false>(h, s, h->val, h->v.p, h->v.q);
+    } else if (h->spmv_kind == TFS_SPMV_ASYNC && mixed) {
+        launch_spmv_async<float, true>(h, s, std::min(VG, h->sm_count * h->bulk_occ32), h->bulk_smem32, h->val32,
+                                       h->f.p, h->f.q);
+    } else if (h->spmv_kind == TFS_SPMV_ASYNC) {
+        launch_spmv_async<double, false>(h, s, std::min(VG, h->sm_count * h->bulk_occ64), h->bulk_smem64, h->val,
+                                         h->v.p, h->v.q);
+    } else if (h->spmv_kind == TFS_SPMV_BULK && mixed) {
+        const int G = std::min(VG, h->sm_count * h->bulk_occ32);
+        k_spmv_pq_bulk<float, true><<<G, TFS_TPB, h->bulk_smem32, s>>>(A, h->val32, h->f.p, h->f.q, h->st,
+                                                                      h->part, VG, h->bulk_stages);
+    } else if (h->spmv_kind == TFS_SPMV_BULK) {
+        const int G = std::min(VG, h->sm_count * h->bulk_occ64);
+        k_spmv_pq_bulk<double, false><<<G, TFS_TPB, h->bulk_smem64, s>>>(A, h->val, h->v.p, h->v.q, h->st,
+                                                                        h->part, VG, h->bulk_stages);
+    } else if (mixed) {
+        k_mx_spmv_pq<<<VG, TFS_TPB, 0, s>>>(A, h->val32, h->f.p, h->f.q, h->st, h->part);
+    } else {
+        k_spmv_pq<<<VG, TFS_TPB, 0, s>>>(A, h->val, h->v.p, h->v.q, h->st, h->part);
+    }
 }
 
 static uint64_t fingerprint(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
@@ -597,6 +719,7 @@ static int build_layout(tfs_handle *h, int kind)
         h->sweep_grid = h->n_tiles < gs ? h->n_tiles : gs;
         if (h->sweep_grid < 1) h->sweep_grid = 1;
     }
+    spmv_kind_setup(h);
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->rowinfo, rowinfo.data(), sizeof(uint32_t) * n_int, cudaMemcpyHostToDevice, h->stream));
@@ -973,7 +1096,7 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
         const int n4 = h->n_int / 4, G4 = h->grid_vec4;
         if (h->sweep_mode == 2 && prec == 2) {
             if ((rc = launch_dic<float, true>(h, s, F.r, F.y, F.z, F.p, count))) return rc;
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
             k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
@@ -982,14 +1105,14 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
             k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
             k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update<false><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 6;
         } else if (!h->vec4) {
             k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update<true><<<G, T, 0, s>>>(nc, V, F, h->st, h->part);
             k_mx_fold<<<G, T, 0, s>>>(nc, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
@@ -998,7 +1121,7 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             const int l0 = dic_l0_rows(h, method, prec);
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count, true))) return rc;
             k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part, l0 / 4);
             k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond, l0);
@@ -1007,14 +1130,14 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
             k_mx_dot_rho4<<<G4, T, 0, s>>>(n4, F, h->st, h->part);
             k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
             k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 6;
         } else {
             k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            k_mx_spmv_pq<<<GS, T, 0, s>>>(A, v32, F.p, F.q, h->st, h->part);
+            launch_spmv_pq(h, s, true);
             k_mx_cg_update4<true><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
             k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
@@ -1070,7 +1193,7 @@ static void tfs_mixed_fill32(tfs_handle *h, const double *src, float *dst)
 
 static void tfs_mixed_spmv_only(tfs_handle *h, cudaStream_t s)
 {
-    k_mx_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, s>>>(sell_of(h), h->val32, h->f.p, h->f.q, h->st, h->part);
+    launch_spmv_pq(h, s, true);
 }
 
 static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
@@ -1084,26 +1207,26 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     if (method == TFS_CG) {
         if (prec == 2 && h->sweep_mode == 2) {
             if ((rc = launch_dic<double, true>(h, s, V.r, V.y, V.z, V.p, count))) return rc;
-            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            launch_spmv_pq(h, s, false);
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 2;
         } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
             const int l0 = dic_l0_rows(h, method, prec);
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count, true))) return rc;
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            launch_spmv_pq(h, s, false);
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond, l0);
             *count += 3;
         } else if (prec == 2) {
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
             k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            launch_spmv_pq(h, s, false);
             k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 4;
         } else {
             k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            k_spmv_pq<<<GS, T, 0, s>>>(A, h->val, V.p, V.q, h->st, h->part);
+            launch_spmv_pq(h, s, false);
             k_cg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
             *count += 3;
         }
@@ -1486,7 +1609,7 @@ extern "C" int tfs_spmv(tfs_handle *h, const double *val, const double *p, doubl
     CK(cudaSetDevice(h->device));
     int rc;
     if ((rc = prepare_values(h, val)) || (rc = vec_in(h, p, h->v.p))) return rc;
-    k_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, h->stream>>>(sell_of(h), h->val, h->v.p, h->v.q, h->st, h->part);
+    launch_spmv_pq(h, h->stream, false);
     CKL("spmv");
     return vec_out(h, h->v.q, q);
 }
@@ -1532,6 +1655,8 @@ extern "C" int tfs_get_stats(const tfs_handle *h, tfs_stats *out)
 {
     if (!h || !out) return TFS_ERR_ARG;
     *out = h->stats;
+    out->spmv_kernel = h->spmv_kind;
+    out->sell_width = h->sell_width;
     return TFS_OK;
 }
 
@@ -1557,7 +1682,7 @@ extern "C" int tfs_time_spmv(tfs_handle *h, const double *val, int mode, int rep
     k_diag_form<<<(h->n_int + 255) / 256, 256, 0, s>>>(A, h->val, h->v.p, 0);
     tfs_mixed_fill32(h, h->v.p, h->f.p);
     auto launch = [&]() {
-        if (mode == TFS_FP64) k_spmv_pq<<<h->grid_spmv, TFS_TPB, 0, s>>>(A, h->val, h->v.p, h->v.q, h->st, h->part);
+        if (mode == TFS_FP64) launch_spmv_pq(h, s, false);
         else tfs_mixed_spmv_only(h, s);
     };
     for (int w = 0; w < 3; w++) launch();
@@ -1637,18 +1762,37 @@ extern "C" int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec
         return rc;
     }
     {
-        const int keep = h->grid_spmv;
-        const int cand[2] = {h->grid, h->n_chunks};
-        int best = keep;
+        // SpMV kernel x grid: the direct kernel, the software-pipelined one
+        // (uniform-width matrices) and a staged kernel chosen by TFS_SPMV,
+        // each with 8 blocks per SM (grid-stride) or one block per chunk.
+        const int keep_grid = h->grid_spmv, keep_kind = h->spmv_kind;
+        const int grids[2] = {h->grid, h->n_chunks};
+        int kinds[3], nk = 0;
+        kinds[nk++] = TFS_SPMV_DIRECT;
+        if (h->sell_width > 0 && h->sell_width <= 8) kinds[nk++] = TFS_SPMV_PIPE;
+        if (keep_kind == TFS_SPMV_BULK || keep_kind == TFS_SPMV_ASYNC) kinds[nk++] = keep_kind;
+        int best_grid = keep_grid, best_kind = keep_kind;
         double best_ms = 0.0;
-        for (int k = 0; k < 2; k++) {
-            h->grid_spmv = cand[k];
-            double ms = 0.0;
-            if ((rc = tfs_time_spmv(h, val, mode, reps, &ms))) { h->grid_spmv = keep; return rc; }
-            out->spmv_ms[k] = ms;
-            if (k == 0 || ms < best_ms) { best_ms = ms; best = cand[k]; }
-        }
-        h->grid_spmv = best;
+        for (int a = 0; a < nk; a++)
+            for (int k = 0; k < 2; k++) {
+                h->spmv_kind = kinds[a];
+                h->grid_spmv = grids[k];
+                double ms = 0.0;
+                if ((rc = tfs_time_spmv(h, val, mode, reps, &ms))) {
+                    h->grid_spmv = keep_grid;
+                    h->spmv_kind = keep_kind;
+                    return rc;
+                }
+                if (kinds[a] == TFS_SPMV_DIRECT) out->spmv_ms[k] = ms;
+                if (kinds[a] == TFS_SPMV_PIPE) out->spmv_pipe_ms[k] = ms;
+                if ((a == 0 && k == 0) || ms < best_ms) {
+                    best_ms = ms;
+                    best_grid = grids[k];
+                    best_kind = kinds[a];
+                }
+            }
+        h->grid_spmv = best_grid;
+        h->spmv_kind = best_kind;
     }
     // The part buffer holds TFS_NPART partials per chunk: both grids fit.
     for (auto &kv : h->graphs) {
@@ -1659,6 +1803,7 @@ extern "C" int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec
     h->last_graph = nullptr;
     out->level_tpb = h->level_tpb;
     out->spmv_chunks = h->grid_spmv == h->n_chunks && h->grid_spmv != h->grid ? 1 : 0;
+    out->spmv_kernel = h->spmv_kind;
     return TFS_OK;
 }
 

@@ -29,6 +29,10 @@
 #define TFS_SWEEP_TPB 1024    // threads per block = rows per tile of the level sweeps
 #define TFS_TAIL_ROWS 1024    // levels after the last one above this size form the tail
 #define TFS_NPART 4           // values reduced at once, at most
+#define TFS_SPMV_DIRECT 0     // CG SpMV kernels: per-row dependent chain (any SELL-32 matrix)
+#define TFS_SPMV_PIPE 1       //   software-pipelined, uniform slice width
+#define TFS_SPMV_BULK 2       //   bulk copies into shared memory, uniform slice width
+#define TFS_SPMV_ASYNC 3      //   cp.async copies into shared memory, uniform slice width
 
 // Device-resident state of one solve.  Written by k_init from DevParams and
 // then only by the last block of each reducing kernel.
@@ -115,6 +119,11 @@ struct tfs_handle {
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int sell_width = 0;                // uniform slice width (0: per-slice widths)
+    int spmv_kind = 0;                 // TFS_SPMV_DIRECT / _PIPE / _BULK / _ASYNC: kernel of the CG SpMV
+    // bulk-copy SpMV: resident blocks per SM of the binary32 / binary64
+    // kernel, stages per block, dynamic shared memory per block
+    int bulk_occ32 = 0, bulk_occ64 = 0, bulk_stages = 3;
+    int bulk_smem32 = 0, bulk_smem64 = 0;
     int grid = 0;                      // blocks of the vector kernels (grid-stride)
     int grid_spmv = 0;                 // blocks of the SpMV-type kernels
     int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels

@@ -25,14 +25,15 @@ P_i32, P_dbl, P_void = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p
 
 class tfs_tuning(C.Structure):
     _fields_ = [("level_tpb", C.c_int32), ("spmv_chunks", C.c_int32),
-                ("prec_ms", C.c_double * 4), ("spmv_ms", C.c_double * 2)]
+                ("prec_ms", C.c_double * 4), ("spmv_ms", C.c_double * 2),
+                ("spmv_kernel", C.c_int32), ("pad", C.c_int32), ("spmv_pipe_ms", C.c_double * 2)]
 
 
 class tfs_stats(C.Structure):
     _fields_ = [("iterations", i32), ("true_residuals", i32), ("n_levels", i32), ("status", i32),
                 ("solve_ms", dbl), ("spmv_ns_total", dbl), ("spmv_launches", i64),
                 ("sweep_ns_total", dbl), ("sweep_launches", i64), ("kernel_launches", i64),
-                ("device_bytes", i64)]
+                ("device_bytes", i64), ("spmv_kernel", i32), ("sell_width", i32)]
 
 
 class tfs_result(C.Structure):

@@ -18,6 +18,9 @@ from .lib import (TFS_BICG, TFS_CG, TFS_CGS, TFS_ERR_NONFINITE, TFS_FP64, TFS_OK
                   check, last_error, load_library, tfs_stats)
 from .matrix_mod import Matrix_Type, ptr
 
+# SpMV kernels of the CG iterations (tfs_stats.spmv_kernel, tfs_tuning.spmv_kernel).
+SPMV_KERNELS = {0: "direct", 1: "pipe", 2: "bulk", 3: "async"}
+
 _dbl, _i32 = C.c_double, C.c_int32
 
 
@@ -185,8 +188,10 @@ class Solver:
         check(self.lib.tfs_autotune(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), mode, prec, reps,
                                     C.byref(t)), "tfs_autotune")
         return {"level_tpb": t.level_tpb, "spmv_chunks": t.spmv_chunks,
+                "spmv_kernel": SPMV_KERNELS.get(t.spmv_kernel, str(t.spmv_kernel)),
                 "prec_ms": {c: t.prec_ms[k] for k, c in enumerate((128, 256, 512, 1024))},
-                "spmv_ms": {"sm8": t.spmv_ms[0], "chunks": t.spmv_ms[1]}}
+                "spmv_ms": {"direct_sm8": t.spmv_ms[0], "direct_chunks": t.spmv_ms[1],
+                            "pipe_sm8": t.spmv_pipe_ms[0], "pipe_chunks": t.spmv_pipe_ms[1]}}
 
     def time_prec(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
         """Milliseconds per DIC preconditioner application (both sweeps)."""

@@ -329,6 +329,42 @@ def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
                 assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) < 1e-6
 
 
+@pytest.mark.parametrize("grid", ["sm8", "chunks"])
+@pytest.mark.parametrize("kind", ["pipe", "bulk-2", "bulk-4", "async-2", "async-3", "async-4"])
+def test_spmv_kernels_bitwise(grid, kind, monkeypatch, gpu):
+    """The CG SpMV kernels for uniform-width matrices -- software-pipelined
+    (the next row's column indices loaded while the current row's gathers
+    are in flight), bulk-copy (matrix tiles streamed into shared memory by
+    cp.async.bulk, 2 or 4 stages) and cp.async-staged (2 to 4 stages) -- take the direct kernel's rows,
+    dot-product order and reductions over the same (virtual) grid: q = A p
+    and whole CG solves (binary64 and mixed, diagonal and DIC) are bitwise
+    those of the direct kernel (TFS_SPMV=direct)."""
+    if grid == "chunks":
+        monkeypatch.setenv("TFS_SPMV_GRID", "chunks")
+    if "-" in kind:
+        monkeypatch.setenv("TFS_BULK_STAGES", kind.split("-")[1])
+    s = system(POISSON, 40, 40, 40)
+    ref = oracle_solve(s, TFS_CG, 2)
+    pv = np.random.default_rng(5).uniform(-1, 1, s.n)
+    out = {}
+    for k in (kind.split("-")[0], "direct"):
+        monkeypatch.setenv("TFS_SPMV", k)
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode) as sol:
+                if mode == TFS_FP64:
+                    res.append(sol.spmv(s.val, pv))
+                for prec in (1, 2):
+                    x, r = np.zeros(s.n), s.b.copy()
+                    st = sol.solve(TFS_CG, s.val, x, r, prec, 2000, ref["tol"])
+                    assert st.status == 0 and st.fin_res < ref["tol"]
+                    res += [x, r, st.niter, st.fin_res]
+        out[k] = res
+    assert np.array_equal(out["direct"][0], O.spmv(s.n, s.row, s.col, s.val, pv))
+    for a, b in zip(out[kind.split("-")[0]], out["direct"]):
+        assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("fuse", ["0", "1", "2"])
 def test_level0_fusion_parity(fuse, monkeypatch, gpu):
     """DIC-CG with level 0 swept inside the residual, update and rho kernels
