@@ -338,6 +338,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     next_rows = None
     if dist.rank == 0 and not args.no_next_rows:
         next_rows = measure_next_rows(lib, sol, s, dalloc)
+        next_rows["reference_meshes"] = measure_reference_meshes()
     for p in (d_val, d_b, d_x, d_r, d_zero):
         lib.tfs_device_free(C.c_void_p(p))
 
@@ -471,6 +472,43 @@ def measure_next_rows(lib, sol, s, dalloc) -> dict:
                   "its scratch allocation and the copies of faces in and arrays out); assembly: CUDA "
                   "events on the handle's stream, median of 3 after a warm-up",
     }
+
+
+def measure_reference_meshes() -> dict:
+    """DIC-CG on the reference's own test meshes (Gambit files of its Tests/
+    directory, committed as tests/golden/gambit_*.npz): binary64 and mixed
+    solves against the oracle, in the meshes' own cell numbering."""
+    import numpy as np
+    from oracle import tfs_oracle as O
+    from tflows import TFS_CG, TFS_FP64, TFS_MIXED, Solver
+    from tflows import gambit as G
+
+    out = {}
+    for name in ("chan", "plain50"):
+        s = G.system_from_fixture(REPO / "tests" / "golden" / f"gambit_{name}.npz")
+        tol = 1e-8 * float(np.linalg.norm(s.b))
+        xo, ro = np.zeros(s.n), s.b.copy()
+        t = time.perf_counter()
+        it, ini, fin = O.solve(0, s.n, s.row, s.col, s.dia, s.val, xo, ro, 2, 5000, tol)
+        cpu_ms = (time.perf_counter() - t) * 1e3
+        row = {"cells": s.n, "nnz": s.nnz, "oracle_iterations": it, "oracle_ms": round(cpu_ms, 2)}
+        for mode, tag in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
+            with Solver(s.matrix(), precision=mode) as sol:
+                ms = []
+                for rep in range(4):
+                    x, r = np.zeros(s.n), s.b.copy()
+                    res = sol.solve(TFS_CG, s.val, x, r, 2, 5000, tol)
+                    if rep:
+                        ms.append(sol.stats()["solve_ms"])
+                st = sol.stats()
+                row[tag] = {"iterations": res.niter, "status": res.status,
+                            "device_ms": round(statistics.median(ms), 3),
+                            "rel_err_vs_oracle": float(np.linalg.norm(x - xo) / np.linalg.norm(xo)),
+                            "dic_levels": st["n_levels"]}
+        out[name] = row
+    out["timing"] = ("device time of one tfs_solve (CUDA events inside the library, median of 3 "
+                     "after a warm-up); oracle: one binary64 solve on one host core")
+    return out
 
 
 # ---------------------------------------------------------------- serving arm
