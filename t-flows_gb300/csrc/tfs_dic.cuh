@@ -369,4 +369,100 @@ k_dic_apply(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, 
     }
 }
 
+// ------------------------------------------------ slabs with neighbour waits
+//
+// The same application as one cooperative launch without grid barriers.
+// Block b owns the rows whose reverse Cuthill-McKee position lies in slab b
+// of G equal slabs, in every level (a contiguous range of each level, whose
+// rows are in RCM order: seg[L * (G + 1) + b] .. seg[L * (G + 1) + b + 1]).
+// A row's neighbours lie within the RCM bandwidth, so the rows a block reads
+// belong to the blocks dep[b].x .. dep[b].y, a few slabs around its own.  A
+// block sweeps its rows level by level (forward 0..nl-1, then backward
+// nl-1..0: 2 nl steps) and after every step publishes the step number in its
+// progress word (release); before a step it waits until every block of its
+// range has published the step before (acquire) -- the level structure
+// guarantees that the rows it reads were written in earlier steps.  No block
+// waits for the whole grid.  Progress words only grow: step s of the e-th
+// application is published as e * (2 nl + 1) + s, e counted in ectl[0] by
+// the last block to finish (ectl[1] counts arrivals), so nothing is cleared
+// between applications.  Deadlock-free: all blocks are co-resident
+// (cooperative launch) and step 1 waits for nobody.  Every wait is bounded
+// (TFS_BAR_SPINS polls, abort flag, TFS_ERR_TIMEOUT); an aborted block still
+// arrives at the end, so the application counter stays consistent.
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" : : "l"(p), "l"(v) : "memory");
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(TFS_DIC_TPB, R == 1 ? 2 : 1)
+k_dic_slab(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, T *z,
+           const int *__restrict__ seg, const int2 *__restrict__ dep, int nl,
+           unsigned long long *prog, unsigned long long *ectl, DevState *st)
+{
+    using AT = typename std::conditional<sizeof(T) == 4, float, double>::type;
+    const int G = gridDim.x, blk = blockIdx.x;
+    const unsigned long long steps = 2ull * (unsigned long long)nl + 1ull;
+    const unsigned long long base = *(volatile unsigned long long *)ectl * steps;
+    const int2 rng = __ldg(dep + blk);
+    const bool active = st->done == 0;
+    if (active && blk == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
+    AT acc = (AT)0;
+    DicRows<T, R> cur;
+    for (int k = 0; active && k < 2 * nl; k++) {
+        const int mode = k < nl ? 0 : 1;
+        const int lev = k < nl ? k : 2 * nl - 1 - k;
+        const int r0 = __ldg(seg + lev * (G + 1) + blk), r1 = __ldg(seg + lev * (G + 1) + blk + 1);
+        // Loads that do not depend on other rows go ahead of the wait.
+        if (mode == 0) cur.template fetch<0>(A, val, r0 + threadIdx.x, r1, TFS_DIC_TPB);
+        else cur.template fetch<1>(A, val, r0 + threadIdx.x, r1, TFS_DIC_TPB);
+        // Steps 1 (forward level 0) and nl + 1 (backward top level) read no
+        // other block's rows of this application.
+        if (k != 0 && k != nl) {
+            const int j = rng.x + (int)threadIdx.x;
+            bool fail = false;
+            if (j <= rng.y && j != blk) {
+                const unsigned long long want = base + (unsigned long long)k;
+                unsigned spins = 0;
+                while (ld_acquire_u64(prog + j) < want) {
+                    if ((spins & 63u) == 63u && ld_relaxed_u32(&st->bar_abort)) { fail = true; break; }
+                    if (++spins > TFS_BAR_SPINS) { bar_abort(st); fail = true; break; }
+                }
+                __threadfence();
+            }
+            if (__syncthreads_or(fail)) break;
+        }
+        if (mode == 0) dic_level<T, R, 0, false>(cur, A, val, d, b, nullptr, y, nullptr, r0, r1, threadIdx.x,
+                                                 TFS_DIC_TPB, acc);
+        else dic_level<T, R, 1, false>(cur, A, val, d, nullptr, y, z, nullptr, r0, r1, threadIdx.x,
+                                       TFS_DIC_TPB, acc);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_u64(prog + blk, base + (unsigned long long)(k + 1));
+        }
+    }
+    // Every block arrives once; the last one advances the application count.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(ectl + 1, 1ull) == (unsigned long long)G - 1ull) {
+            if (active) {
+                st->sweep_ns += gtimer() - st->t_sweep0;
+                st->sweep_n += 1;
+            }
+            ectl[1] = 0ull;
+            __threadfence();
+            st_release_u64(ectl, ectl[0] + 1ull);
+        }
+    }
+}
+
 }  // namespace tfs

@@ -512,6 +512,13 @@ static void free_layout(tfs_handle *h)
     h->lvl_cnt = nullptr;
     h->vec_pool = h->vec32_pool = nullptr;
     h->part = nullptr;
+    void *slab[] = {h->d_slab_seg, h->d_slab_dep, h->d_slab_prog};
+    for (void *p : slab)
+        if (p) cudaFree(p);
+    h->d_slab_seg = nullptr;
+    h->d_slab_dep = nullptr;
+    h->d_slab_prog = nullptr;
+    h->slab_G = 0;
     h->device_bytes = h->fixed_bytes;
     h->layout = -1;
 }
@@ -831,6 +838,7 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
+    if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
     env = getenv("TFS_FUSE_L0");
     if (env && (strcmp(env, "0") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
     env = getenv("TFS_LEVEL_TPB");
@@ -968,12 +976,101 @@ static int launch_dic(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *
     return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "cooperative DIC launch");
 }
 
+// Slab schedule (k_dic_slab): block b owns the rows of RCM slab b of every
+// level; its neighbour range covers the slabs of every row it reads.  One
+// block per SM (TFS_SLAB_PER_SM=2: two, where they fit), at most 1024.
+static int slab_setup(tfs_handle *h)
+{
+    if (h->slab_G > 0) return TFS_OK;
+    int per_sm = 1;
+    const char *env = getenv("TFS_SLAB_PER_SM");
+    if (env && atoi(env) == 2) per_sm = 2;
+    int occ32 = 0, occ64 = 0;
+    if (per_sm == 2) {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_dic_slab<float, 1>, TFS_DIC_TPB, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_dic_slab<double, 1>, TFS_DIC_TPB, 0));
+    } else {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_dic_slab<float, 2>, TFS_DIC_TPB, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_dic_slab<double, 2>, TFS_DIC_TPB, 0));
+    }
+    const int occ = std::min(occ32, occ64);
+    if (occ < 1) {
+        tfs_set_error_text("slab DIC kernel cannot be resident");
+        return TFS_ERR_CUDA;
+    }
+    per_sm = std::min(per_sm, occ);
+    const int G = std::min(1024, h->sm_count * per_sm);
+    const int n = h->n, nl = h->n_levels;
+    if ((int)h->levels_nat.size() != n || (int)h->lvl_begin.size() != nl + 1) {
+        tfs_set_error_text("slab schedule needs the level layout");
+        return TFS_ERR_ARG;
+    }
+    auto slab = [&](int i) { return (int)((int64_t)h->rcm_pos[i] * G / n); };
+    std::vector<int> cnt((size_t)nl * G, 0), seg((size_t)nl * (G + 1));
+    for (int i = 0; i < n; i++) cnt[(size_t)h->levels_nat[i] * G + slab(i)]++;
+    for (int l = 0; l < nl; l++) {
+        int *sg = seg.data() + (size_t)l * (G + 1);
+        sg[0] = h->lvl_begin[l];
+        for (int b = 0; b < G; b++) sg[b + 1] = sg[b] + cnt[(size_t)l * G + b];
+        sg[G] = h->lvl_begin[l + 1];   // the level's padding rows go to the last block
+    }
+    std::vector<int2> dep(G);
+    for (int b = 0; b < G; b++) dep[b] = make_int2(b, b);
+    for (int i = 0; i < n; i++) {
+        const int sb = slab(i);
+        for (int j = h->row0[i]; j < h->row0[i + 1]; j++) {
+            const int sk = slab(h->col0[j]);
+            dep[sb].x = std::min(dep[sb].x, sk);
+            dep[sb].y = std::max(dep[sb].y, sk);
+        }
+    }
+    int rc;
+    if ((rc = dalloc(h, &h->d_slab_seg, seg.size())) || (rc = dalloc(h, &h->d_slab_dep, (size_t)G)) ||
+        (rc = dalloc(h, &h->d_slab_prog, (size_t)G + 2)))
+        return rc;
+    CK(cudaMemcpyAsync(h->d_slab_seg, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_slab_dep, dep.data(), sizeof(int2) * (size_t)G, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_slab_prog, 0, sizeof(unsigned long long) * ((size_t)G + 2), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->slab_G = G;
+    return TFS_OK;
+}
+
+template <typename T>
+static int launch_slab(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, int *count)
+{
+    int rc = slab_setup(h);
+    if (rc) return rc;
+    const T *val;
+    const T *d;
+    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
+    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
+    const int G = h->slab_G;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3((unsigned)G);
+    cfg.blockDim = dim3(TFS_DIC_TPB);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    // Two blocks per SM: one row per thread (32 registers); one: two rows.
+    auto kernel = G > h->sm_count ? k_dic_slab<T, 1> : k_dic_slab<T, 2>;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, sell_of(h), val, d, b, y, z,
+                                       (const int *)h->d_slab_seg, (const int2 *)h->d_slab_dep, h->n_levels,
+                                       h->d_slab_prog, h->d_slab_prog + G, h->st);
+    (*count)++;
+    return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "slab DIC launch");
+}
+
 template <typename T>
 static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, const T *b2,
                          T *y1, T *y2, T *z1, T *z2, int *count, bool fuse_l0 = false)
 {
     SellDev A = sell_of(h);
     if (h->sweep_mode == 2 && nr == 1) return launch_dic<T, false>(h, s, b1, y1, z1, nullptr, count);
+    if (h->sweep_mode == 3 && nr == 1) return launch_slab<T>(h, s, b1, y1, z1, count);
     const int T_ = TFS_TPB;
     const T *val;
     T *d;
@@ -1368,8 +1465,10 @@ static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
     auto it = h->graphs.find(key);
     if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
     GraphEntry ge;
-    int rc = build_graph(h, method, prec, ge);
-    if (rc && h->sweep_mode == 2 && prec == 2) {
+    int rc = TFS_OK;
+    if (h->sweep_mode == 3 && prec == 2 && (rc = slab_setup(h))) return rc;   // no copies during capture
+    rc = build_graph(h, method, prec, ge);
+    if (rc && (h->sweep_mode == 2 || h->sweep_mode == 3) && prec == 2) {
         // A driver that cannot capture a cooperative launch inside a
         // conditional body gets the per-level schedule instead.
         h->sweep_mode = 0;

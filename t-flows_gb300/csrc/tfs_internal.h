@@ -129,12 +129,19 @@ struct tfs_handle {
     int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels
     int vec4 = 1;                      // 1: binary32 CG vector kernels with 16-byte loads
     int sweep_grid = 0;                // blocks of the dataflow sweeps
-    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative
+    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative, 3: slabs
     int use_pdl = 1;                   // programmatic dependent launch between level kernels
     int fuse_l0 = 1;                   // DIC-CG level 0 swept inside the neighbouring kernels (1: binary32 iteration, 2: binary64 too)
     int level_tpb = TFS_TPB;           // threads per block of the level-sweep kernels (TFS_LEVEL_TPB;
                                        // 128/256/512/1024 measured 147.7/146.4/147.4/150.1 us per DIC application)
     int dic_r = 0;                     // rows per thread of the cooperative sweep (0: not chosen yet)
+    // slab schedule of the DIC sweeps (sweep_mode 3): blocks, per-level row
+    // ranges of every block, neighbour-block ranges, progress words (+2
+    // application counter words); built on first use for the level layout
+    int slab_G = 0;
+    int *d_slab_seg = nullptr;
+    int2 *d_slab_dep = nullptr;
+    unsigned long long *d_slab_prog = nullptr;
     int eager = 0;                     // 1: launch kernels directly, no CUDA graph
     int bicg_literal = 0;              // 1: BiCG runs its shadow sequence explicitly
     int precision = TFS_FP64;

@@ -298,18 +298,21 @@ def test_matrix_mod_example_nonsymmetric_pattern(gpu):
             assert iter_ok(res.niter, it) and rel_l2(x, xo) <= 1e-12
 
 
-@pytest.mark.parametrize("mode", ["levels", "levels-c1", "levels-c16", "coop", "single"])
+@pytest.mark.parametrize("mode", ["levels", "levels-c1", "levels-c16", "coop", "single", "slab", "slab-p2"])
 def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
     """The DIC schedules -- one launch per level with the small levels in one
     8-CTA cluster (default), in one block (c1) or in a 16-CTA cluster (c16),
-    one cooperative launch with grid barriers, and the single-launch dataflow
-    sweep -- do the same per-row arithmetic: Prec_Form and Prec_Solve bitwise
+    one cooperative launch with grid barriers, the single-launch dataflow
+    sweep, and RCM slabs per block with neighbour-only waits (one or two
+    blocks per SM) -- do the same per-row arithmetic: Prec_Form and Prec_Solve bitwise
     equal to the oracle, and solves within the parity gates.  The 40^3 system
     has levels of more than 8192 rows, so the grid-wide part of each schedule
     runs, not only the tail."""
     monkeypatch.setenv("TFS_SWEEP", mode.split("-")[0])
     if "-c" in mode:
         monkeypatch.setenv("TFS_TAIL_CLUSTER", mode.split("-c")[1])
+    if mode == "slab-p2":
+        monkeypatch.setenv("TFS_SLAB_PER_SM", "2")
     for s, method in ((system(CONVDIFF, 10, 9, 8), TFS_BICG), (system(POISSON, 40, 40, 40), TFS_CG)):
         b = np.random.default_rng(9).uniform(-1, 1, s.n)
         with Solver(s.matrix()) as sol:
