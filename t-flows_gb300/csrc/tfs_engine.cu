@@ -653,8 +653,11 @@ static int build_layout(tfs_handle *h, int kind)
         // Sweep work items: tiles of at most TFS_SWEEP_TPB rows inside one
         // level, then one item for the tail (the levels after the last level
         // with more than TFS_TAIL_ROWS rows).
+        int tail_rows = TFS_TAIL_ROWS;
+        const char *tenv = getenv("TFS_TAIL_ROWS");
+        if (tenv && atoi(tenv) >= 1 && atoi(tenv) <= 65536) tail_rows = atoi(tenv);
         int tail = nl;
-        while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= TFS_TAIL_ROWS) tail--;
+        while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= tail_rows) tail--;
         if (tail == 0) tail = nl > 1 ? 1 : nl;   // level 0 always runs as tiles
         h->tail_level = tail;
         // A cluster tail of the per-level sweeps takes levels of up to
