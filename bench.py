@@ -346,18 +346,40 @@ def run_ours(args, dist: Dist) -> dict | None:
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         from oracle import tfs_oracle as O
-        xo, ro = np.zeros(n), s.b.copy()
+        # A probe of a few iterations sizes the sample: one full solve (and
+        # the error of the GPU solutions against it) when that takes at most
+        # about a minute on one core, else a bounded run of iterations scaled
+        # to the binary64 GPU solve's iteration count.
+        probe = 8
+        xp, rp = np.zeros(n), s.b.copy()
         t = time.perf_counter()
-        it, ini, fin = O.solve(method, n, s.row, s.col, s.dia, s.val, xo, ro, prec, args.niter, tol)
-        cpu_s = time.perf_counter() - t
-        cpu = {"value": 1.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"one full binary64 solve ({it} iterations, {cpu_s:.1f} s) of the same "
-                         f"system on 1 host core; {os.cpu_count()} cores present",
-               "oracle_iterations": it}
-        for name in results:
-            x = results[name]["_x"]
-            results[name]["rel_err_vs_oracle"] = float(np.linalg.norm(x - xo) / np.linalg.norm(xo))
-            results[name]["iterations_vs_oracle"] = f"{results[name]['iterations']} vs {it}"
+        O.solve(method, n, s.row, s.col, s.dia, s.val, xp, rp, prec, probe, tol)
+        t_it = (time.perf_counter() - t) / probe
+        gpu_its = (results.get("fp64") or next(iter(results.values())))["iterations"]
+        if t_it * gpu_its <= 60.0:
+            xo, ro = np.zeros(n), s.b.copy()
+            t = time.perf_counter()
+            it, ini, fin = O.solve(method, n, s.row, s.col, s.dia, s.val, xo, ro, prec, args.niter, tol)
+            cpu_s = time.perf_counter() - t
+            cpu = {"value": 1.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"one full binary64 solve ({it} iterations, {cpu_s:.1f} s) of the same "
+                             f"system on 1 host core; {os.cpu_count()} cores present",
+                   "oracle_iterations": it}
+            for name in results:
+                x = results[name]["_x"]
+                results[name]["rel_err_vs_oracle"] = float(np.linalg.norm(x - xo) / np.linalg.norm(xo))
+                results[name]["iterations_vs_oracle"] = f"{results[name]['iterations']} vs {it}"
+        else:
+            k = max(probe, int(20.0 / max(t_it, 1e-9)))
+            xp, rp = np.zeros(n), s.b.copy()
+            t = time.perf_counter()
+            O.solve(method, n, s.row, s.col, s.dia, s.val, xp, rp, prec, k, tol)
+            per_it = (time.perf_counter() - t) / k
+            cpu_s = per_it * gpu_its
+            cpu = {"value": 1.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"{k} binary64 iterations ({per_it * k:.1f} s) of the same system on 1 host "
+                             f"core, scaled to the {gpu_its} iterations of the binary64 GPU solve (a full "
+                             f"oracle solve would take about {cpu_s:.0f} s); {os.cpu_count()} cores present"}
     for name in results:
         results[name].pop("_x", None)
 
