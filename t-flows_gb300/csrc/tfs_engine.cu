@@ -842,6 +842,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
     if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
+    env = getenv("TFS_TAIL_PF");
+    if (env && strcmp(env, "0") == 0) h->tail_pf = 0;
     env = getenv("TFS_FUSE_L0");
     if (env && (strcmp(env, "0") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
     env = getenv("TFS_LEVEL_TPB");
@@ -1117,6 +1119,10 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
             cfg.numAttrs = h->use_pdl ? 2 : 1;
             e = cudaLaunchKernelEx(&cfg, kernel_c, A, val, d, b1, b2, y1, y2, z1, z2,
                                    (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+        } else if (nr == 1 && h->tail_pf && h->sell_width > 0 && h->sell_width <= 8 &&
+                   h->lvl_begin[h->n_levels] - h->lvl_begin[tail_at] <= TFS_SWEEP_TPB) {
+            e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
+                          y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
         } else {
             e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
                           z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);

@@ -853,6 +853,75 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     }
 }
 
+// Both tails by one block when the tail has at most TFS_SWEEP_TPB rows in
+// all (one row per thread) and the matrix has uniform slice width W <= 8:
+// every thread loads its row's geometry, entries, right-hand side and
+// diagonal before cudaGridDependencySynchronize (none of them is written by
+// the level kernels this launch may overlap: b and D come from kernels that
+// completed before the first level kernel of the sweep started), so a level
+// step is only the gathers of the rows written in the steps before, the
+// row's arithmetic and a block barrier.  Per-row arithmetic as sweep_row.
+template <typename T>
+__global__ void __launch_bounds__(TFS_SWEEP_TPB)
+k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, T *z,
+              const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
+{
+    const int i = __ldg(lvl_begin + l_begin) + (int)threadIdx.x;
+    const bool mine = i < __ldg(lvl_begin + l_end);
+    int lev = -1;
+    RowGeom g{0, 0, 0};
+    int kk[8];
+    T aa[8];
+    T bi = (T)0, di = (T)0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) { kk[j] = 0; aa[j] = (T)0; }
+    if (mine) {
+        lev = l_begin;
+        while (__ldg(lvl_begin + lev + 1) <= i) lev++;
+        g = row_geom(A, i);
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (j < g.len) {
+                kk[j] = __ldg(A.col + g.off + (j << 5));
+                aa[j] = __ldg(val + g.off + (j << 5));
+            }
+        if (g.len > 0) { bi = b[i]; di = d[i]; }
+    }
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+    const bool skip = st->done != 0;
+    T yi = (T)0;
+    for (int l = l_begin; l < l_end; l++) {
+        if (lev == l) {
+            if (g.len == 0) {
+                if (!skip) y[i] = (T)0;
+            } else {
+                T s = bi;
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (j < g.dpos) s = s - aa[j] * __ldcg(y + kk[j]);
+                yi = s * di;
+                if (!skip) y[i] = yi;
+            }
+        }
+        __syncthreads();
+    }
+    for (int l = l_end - 1; l >= l_begin; l--) {
+        if (lev == l) {
+            if (g.len == 0) {
+                if (!skip) z[i] = (T)0;
+            } else {
+                T s = yi / (di + (T)TINY);
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (j > g.dpos && j < g.len) s = s - aa[j] * __ldcg(z + kk[j]);
+                if (!skip) z[i] = s * di;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Both tails by one thread-block cluster of C CTAs (C x TFS_SWEEP_TPB
 // threads): levels [l_begin, l_end) forward, then backward, one row per
 // thread and pass, the hardware cluster barrier between levels (release /

@@ -368,6 +368,33 @@ def test_spmv_kernels_bitwise(grid, kind, monkeypatch, gpu):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17), (9, 8, 8)])
+def test_tail_prefetch_bitwise(shape, monkeypatch, gpu):
+    """The one-row-per-thread tail (every row's entries, right-hand side and
+    diagonal loaded before the dependency wait) gives the DIC application
+    and whole DIC-CG solves bitwise equal to the level-by-level tail loop
+    (TFS_TAIL_PF=0), and Prec_Solve equal to the oracle."""
+    s = system(POISSON, *shape)
+    ref = oracle_solve(s, TFS_CG, 2)
+    b = np.random.default_rng(4).uniform(-1, 1, s.n)
+    out = {}
+    for pf in ("1", "0"):
+        monkeypatch.setenv("TFS_TAIL_PF", pf)
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode) as sol:
+                if mode == TFS_FP64:
+                    res.append(sol.prec_solve(s.val, 2, b))
+                x, r = np.zeros(s.n), s.b.copy()
+                st = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
+                assert st.status == 0 and st.fin_res < ref["tol"]
+                res += [x, r, st.niter]
+        out[pf] = res
+    assert np.array_equal(out["1"][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+    for a, c in zip(out["1"], out["0"]):
+        assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("fuse", ["0", "1", "2"])
 def test_level0_fusion_parity(fuse, monkeypatch, gpu):
     """DIC-CG with level 0 swept inside the residual, update and rho kernels
