@@ -702,6 +702,53 @@ static int build_layout(tfs_handle *h, int kind)
             while (ct > 0 && h->lvl_begin[ct] - h->lvl_begin[ct - 1] <= C * TFS_SWEEP_TPB) ct--;
             h->ctail_level = ct;
         }
+        {
+            // Prefetching tail (k_sweep_tail1): the longest suffix of levels
+            // (never level 0) whose rows fit one per thread of one block, or
+            // of a cluster of up to TFS_TAIL_PF_CLUSTER CTAs; used when it
+            // reaches at least as far down as the plain tail.  Clusters let
+            // the mid-sized levels join the tail, but measured no faster on
+            // the 128^3 system (one block 128.8 us per DIC application; 2, 8,
+            // 16 CTAs 131.8, 129.3, 126.3 us, binary32 solves/s 14.04 against
+            // 13.72, 13.84, 13.98), so the default is one block.
+            int cmax = 1;
+            const char *env = getenv("TFS_TAIL_PF_CLUSTER");
+            if (env && (atoi(env) == 1 || atoi(env) == 2 || atoi(env) == 4 || atoi(env) == 8 || atoi(env) == 16))
+                cmax = atoi(env);
+            int l = nl, rows = 0;
+            while (l > 1 && rows + (h->lvl_begin[l] - h->lvl_begin[l - 1]) <= cmax * TFS_SWEEP_TPB) {
+                rows += h->lvl_begin[l] - h->lvl_begin[l - 1];
+                l--;
+            }
+            int C = 1;
+            while (C * TFS_SWEEP_TPB < rows) C *= 2;
+            h->pf_tail_level = l;
+            h->pf_C = (l < nl && l <= h->tail_level) ? C : 0;
+            if (h->pf_C > 1) {
+                auto kc = k_sweep_tail1<float, true>;
+                auto kd = k_sweep_tail1<double, true>;
+                if (h->pf_C > 8) {
+                    cudaFuncSetAttribute(kc, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                    cudaFuncSetAttribute(kd, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                }
+                cudaLaunchConfig_t cfg = {};
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = (unsigned)h->pf_C;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.gridDim = dim3((unsigned)h->pf_C);
+                cfg.blockDim = dim3(TFS_SWEEP_TPB);
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int n32 = 0, n64 = 0;
+                if (cudaOccupancyMaxActiveClusters(&n32, kc, &cfg) != cudaSuccess ||
+                    cudaOccupancyMaxActiveClusters(&n64, kd, &cfg) != cudaSuccess || n32 < 1 || n64 < 1) {
+                    cudaGetLastError();
+                    h->pf_C = 0;
+                }
+            }
+        }
         std::vector<int2> tiles;
         std::vector<int> lvl_tiles(nl, 0);
         for (int l = 0; l < tail; l++)
@@ -1069,6 +1116,20 @@ static int launch_slab(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, in
     return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "slab DIC launch");
 }
 
+// The tail of the per-level schedule: the prefetching tail (k_sweep_tail1,
+// one block or one cluster) for one right-hand side on uniform-width
+// matrices when it was set up, else the single-block or cluster level loop.
+static bool pf_tail(const tfs_handle *h, int nr)
+{
+    return nr == 1 && h->tail_pf && h->pf_C > 0 && h->sell_width > 0 && h->sell_width <= 8;
+}
+
+static int sweep_tail_at(const tfs_handle *h, int nr)
+{
+    if (pf_tail(h, nr)) return h->pf_tail_level;
+    return h->tail_cluster > 1 ? h->ctail_level : h->tail_level;
+}
+
 template <typename T>
 static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, const T *b2,
                          T *y1, T *y2, T *z1, T *z2, int *count, bool fuse_l0 = false)
@@ -1098,12 +1159,31 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     // Forward levels, both tails in one block or one cluster, backward levels.
     int rc;
     const int C = h->tail_cluster;
-    const int tail_at = C > 1 ? h->ctail_level : h->tail_level;
+    const int tail_at = sweep_tail_at(h, nr);
     const bool tails = tail_at < h->n_levels;
     auto tail2 = [&](auto kernel, auto kernel_c) -> int {
         if (!tails) return TFS_OK;
         cudaError_t e;
-        if (C > 1) {
+        if (pf_tail(h, nr) && h->pf_C > 1) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[2];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)h->pf_C;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[1].val.programmaticStreamSerializationAllowed = 1;
+            cfg.gridDim = dim3((unsigned)h->pf_C);
+            cfg.blockDim = dim3(TFS_SWEEP_TPB);
+            cfg.stream = s;
+            cfg.attrs = attr;
+            cfg.numAttrs = h->use_pdl ? 2 : 1;
+            e = cudaLaunchKernelEx(&cfg, k_sweep_tail1<T, true>, A, val, (const T *)d, b1, y1, z1,
+                                   (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+        } else if (pf_tail(h, nr)) {
+            e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T, false>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
+                          y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+        } else if (C > 1) {
             cudaLaunchConfig_t cfg = {};
             cudaLaunchAttribute attr[2];
             attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1119,10 +1199,6 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
             cfg.numAttrs = h->use_pdl ? 2 : 1;
             e = cudaLaunchKernelEx(&cfg, kernel_c, A, val, d, b1, b2, y1, y2, z1, z2,
                                    (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
-        } else if (nr == 1 && h->tail_pf && h->sell_width > 0 && h->sell_width <= 8 &&
-                   h->lvl_begin[h->n_levels] - h->lvl_begin[tail_at] <= TFS_SWEEP_TPB) {
-            e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
-                          y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
         } else {
             e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
                           z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
@@ -1167,7 +1243,7 @@ static int dic_l0_rows(const tfs_handle *h, int method, int prec)
     if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0) return 0;
     if (h->precision == TFS_MIXED && !h->vec4) return 0;
     if (h->precision != TFS_MIXED && h->fuse_l0 != 2) return 0;
-    const int tail_at = h->tail_cluster > 1 ? h->ctail_level : h->tail_level;
+    const int tail_at = sweep_tail_at(h, 1);
     if (tail_at < 1 || h->lvl_begin.size() < 2) return 0;
     return h->lvl_begin[1];
 }

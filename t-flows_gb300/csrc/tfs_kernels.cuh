@@ -861,12 +861,18 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
 // completed before the first level kernel of the sweep started), so a level
 // step is only the gathers of the rows written in the steps before, the
 // row's arithmetic and a block barrier.  Per-row arithmetic as sweep_row.
-template <typename T>
+//
+// CLUSTER: the tail spread over the C CTAs of one thread-block cluster (one
+// row per thread of the cluster), the hardware cluster barrier (release /
+// acquire at cluster scope) between levels, so that levels of a few
+// thousand rows join the tail instead of taking a launch each.
+template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, T *z,
               const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
 {
-    const int i = __ldg(lvl_begin + l_begin) + (int)threadIdx.x;
+    const int rank = CLUSTER ? (int)cooperative_groups::this_cluster().block_rank() : 0;
+    const int i = __ldg(lvl_begin + l_begin) + rank * TFS_SWEEP_TPB + (int)threadIdx.x;
     const bool mine = i < __ldg(lvl_begin + l_end);
     int lev = -1;
     RowGeom g{0, 0, 0};
@@ -904,7 +910,8 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
                 if (!skip) y[i] = yi;
             }
         }
-        __syncthreads();
+        if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
+        else __syncthreads();
     }
     for (int l = l_end - 1; l >= l_begin; l--) {
         if (lev == l) {
@@ -918,7 +925,8 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
                 if (!skip) z[i] = s * di;
             }
         }
-        __syncthreads();
+        if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
+        else __syncthreads();
     }
 }
 

@@ -368,12 +368,16 @@ def test_spmv_kernels_bitwise(grid, kind, monkeypatch, gpu):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("cluster", ["1", "8", "16"])
 @pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17), (9, 8, 8)])
-def test_tail_prefetch_bitwise(shape, monkeypatch, gpu):
+def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
     """The one-row-per-thread tail (every row's entries, right-hand side and
-    diagonal loaded before the dependency wait) gives the DIC application
-    and whole DIC-CG solves bitwise equal to the level-by-level tail loop
-    (TFS_TAIL_PF=0), and Prec_Solve equal to the oracle."""
+    diagonal loaded before the dependency wait), in one block or spread over
+    a cluster of up to 8 or 16 CTAs (so that mid-sized levels join it), gives
+    the DIC application and whole DIC-CG solves bitwise equal to the
+    level-by-level tail loop (TFS_TAIL_PF=0), and Prec_Solve equal to the
+    oracle."""
+    monkeypatch.setenv("TFS_TAIL_PF_CLUSTER", cluster)
     s = system(POISSON, *shape)
     ref = oracle_solve(s, TFS_CG, 2)
     b = np.random.default_rng(4).uniform(-1, 1, s.n)
