@@ -399,7 +399,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         # The level sweeps are the dominant kernels of DIC-CG: one "launch" is
         # one preconditioner application (all level kernels of both sweeps).
         ach = prec_bytes32 / (prec32_ms * 1e-3) / 1e9
-        roof = {"kernel": "k_sweep_level + k_sweep_tail2 (one binary32 DIC application: "
+        roof = {"kernel": "k_sweep_level + k_sweep_tail1 (one binary32 DIC application: "
                           "forward levels, fused tails, backward levels)",
                 "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
