@@ -753,15 +753,29 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     int kk[4] = {0, 0, 0, 0};
     T aa[4] = {(T)0, (T)0, (T)0, (T)0};
     if (active) {
-        g = row_geom(A, i);
-        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+        if (MODE == 0 && A.width > 0) {
+            // Uniform slice width: the first four slots are where they are
+            // whatever the row's geometry says, so their loads do not wait
+            // for it (slots past the row's length hold column 0, value 0).
+            const int off = (i & ~31) * A.width + (i & 31);
+            g = row_geom(A, i);
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (j0 + q < j1) {
-                int ee = g.off + ((j0 + q) << 5);
-                kk[q] = __ldg(A.col + ee);
-                aa[q] = __ldg(val + ee);
-            }
+            for (int q = 0; q < 4; q++)
+                if (q < A.width) {
+                    kk[q] = __ldg(A.col + off + (q << 5));
+                    aa[q] = __ldg(val + off + (q << 5));
+                }
+        } else {
+            g = row_geom(A, i);
+            const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (j0 + q < j1) {
+                    int ee = g.off + ((j0 + q) << 5);
+                    kk[q] = __ldg(A.col + ee);
+                    aa[q] = __ldg(val + ee);
+                }
+        }
     }
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
