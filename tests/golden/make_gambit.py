@@ -12,7 +12,11 @@ reference tree is absent:
   gambit_chan.npz     Tests/Rans/Channel_Re_Tau_590/chan.neu.gz (480 bricks)
   gambit_plain50.npz  Tests/Rans/Flow_over_plain/plain_50.neu.gz (14,490 bricks)
 
-Each holds the face list faces_c (1-based, c2 = 0 on the boundary), the
+and the first also in the reference's own mesh format, as written by
+tflows.cns_geo (chan.cns, chan.geo: the record layout Process reads in
+Load_Cns.f90 / Load_Geo.f90).
+
+Each .npz holds the face list faces_c (1-based, c2 = 0 on the boundary), the
 pressure-Poisson face coefficients coef (a_f = |S_f|/|d_f| inside,
 |S_b|/|d_b| on the Dirichlet set's faces, 0 on the other boundary faces),
 the Dirichlet set, the right-hand-side seed and the SHA-256 of the source
@@ -53,13 +57,27 @@ def build(root: Path, name: str) -> dict:
             "sha256": np.array(hashlib.sha256(src.read_bytes()).hexdigest())}
 
 
+def write_reference_format(root: Path, name: str, out_dir: Path) -> None:
+    """The mesh in the reference's own .cns/.geo format (tflows.cns_geo)."""
+    from tflows import cns_geo
+    m = G.read_neu(root / MESHES[name])
+    f = G.mesh_faces(m)
+    g = G.geometry(m, f)
+    cns, geo = cns_geo.from_gambit(m, f, g)
+    cns_geo.write_cns(out_dir / f"{name}.cns", cns)
+    cns_geo.write_geo(out_dir / f"{name}.geo", geo)
+
+
 def main() -> None:
     root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    golden = REPO / "tests" / "golden"
     for name in MESHES:
         d = build(root, name)
-        out = REPO / "tests" / "golden" / f"gambit_{name}.npz"
+        out = golden / f"gambit_{name}.npz"
         np.savez_compressed(out, **d)
         print(f"{out.name}: {int(d['n_cells'])} cells, {len(d['faces_c'])} faces, {out.stat().st_size} bytes")
+    write_reference_format(root, "chan", golden)
+    print("chan.cns, chan.geo:", (golden / "chan.cns").stat().st_size, (golden / "chan.geo").stat().st_size, "bytes")
 
 
 if __name__ == "__main__":

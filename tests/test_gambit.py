@@ -83,3 +83,51 @@ def test_fixture_system_against_oracle(name):
     x, r = np.zeros(s.n), s.b.copy()
     it, ini, fin = O.solve(0, s.n, s.row, s.col, s.dia, s.val, x, r, 1, 5000, tol)
     assert it <= 5000 and fin < tol
+
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def test_cns_geo_fixture_matches_gambit_system():
+    """The chan mesh in the reference's .cns/.geo format (read as Process's
+    Load_Cns / Load_Geo read it) gives the same faces, coefficients, matrix
+    and values bit for bit as the Gambit-derived fixture."""
+    from tflows import cns_geo
+    a = cns_geo.pressure_system(GOLDEN / "chan.cns", GOLDEN / "chan.geo", dirichlet_bcs=(1,))
+    b = load("chan")
+    assert np.array_equal(a.faces_c, b.faces_c) and np.array_equal(a.coef, b.coef)
+    for k in ("row", "col", "dia", "pos", "val", "b"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+
+
+def test_cns_geo_roundtrip_and_errors(tmp_path):
+    """Reading and writing back reproduces the files byte for byte; a cut
+    file or a damaged record marker is refused."""
+    from tflows import cns_geo
+    c = cns_geo.read_cns(GOLDEN / "chan.cns")
+    g = cns_geo.read_geo(GOLDEN / "chan.geo", c)
+    assert c.n_cells == 480 and c.n_faces == 1711 and c.n_bnd_cells == 542
+    assert c.boundary_conditions[:2] == ["one", "two"]
+    assert (c.faces_c[:, 0] > 0).all() and (c.faces_c[c.faces_c[:, 1] < 0, 1] >= -c.n_bnd_cells).all()
+    cns_geo.write_cns(tmp_path / "x.cns", c)
+    cns_geo.write_geo(tmp_path / "x.geo", g)
+    assert (tmp_path / "x.cns").read_bytes() == (GOLDEN / "chan.cns").read_bytes()
+    assert (tmp_path / "x.geo").read_bytes() == (GOLDEN / "chan.geo").read_bytes()
+    raw = (GOLDEN / "chan.cns").read_bytes()
+    (tmp_path / "cut.cns").write_bytes(raw[:-6])
+    with pytest.raises(ValueError):
+        cns_geo.read_cns(tmp_path / "cut.cns")
+    bad = bytearray(raw)
+    bad[4 + 4] ^= 1          # tail marker of the first record
+    (tmp_path / "bad.cns").write_bytes(bytes(bad))
+    with pytest.raises(ValueError):
+        cns_geo.read_cns(tmp_path / "bad.cns")
+
+
+@needs_ref
+def test_cns_geo_fixture_is_reproduced(tmp_path):
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_gambit
+    make_gambit.write_reference_format(REF, "chan", tmp_path)
+    for ext in ("cns", "geo"):
+        assert (tmp_path / f"chan.{ext}").read_bytes() == (GOLDEN / f"chan.{ext}").read_bytes()

@@ -92,3 +92,22 @@ def test_device_topology_and_assembly(name, gpu):
         sol.faces_register(s.faces_c, s.pos)
         val = sol.assemble(off, off, s.coef, off)
     assert np.array_equal(val, s.val)
+
+
+def test_solve_from_reference_format_files(gpu):
+    """A mesh stored in the reference's own .cns/.geo format solves on the
+    GPU within the parity gates (binary64) and converges in mixed precision."""
+    from pathlib import Path
+    from tflows import cns_geo
+    golden = Path(__file__).resolve().parent / "golden"
+    s = cns_geo.pressure_system(golden / "chan.cns", golden / "chan.geo", dirichlet_bcs=(1,))
+    for prec in (1, 2):
+        ref = oracle(s, 0, prec)
+        with Solver(s.matrix()) as sol:
+            x, r = np.zeros(s.n), s.b.copy()
+            res = sol.solve(TFS_CG, s.val, x, r, prec, 5000, ref["tol"])
+            assert res.status == 0 and iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+        with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+            x, r = np.zeros(s.n), s.b.copy()
+            res = sol.solve(TFS_CG, s.val, x, r, prec, 5000, ref["tol"])
+            assert res.status == 0 and res.fin_res < ref["tol"] and rel_l2(x, ref["x"]) < 1e-6
