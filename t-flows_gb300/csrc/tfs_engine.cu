@@ -629,6 +629,9 @@ static int build_layout(tfs_handle *h, int kind)
     {
         const char *env = getenv("TFS_SPMV_GRID");
         if (env && strcmp(env, "chunks") == 0) h->grid_spmv = h->n_chunks;
+        // TFS_SPMV_GRID=<k>, 1 <= k <= 8: k blocks per SM.
+        if (env && atoi(env) >= 1 && atoi(env) <= 8)
+            h->grid_spmv = std::max(1, std::min(h->n_chunks, h->sm_count * atoi(env)));
     }
     // Binary32 CG vector kernels: 16-byte loads, grid-stride over the same
     // grid as the other vector kernels.  TFS_VEC=full gives every thread

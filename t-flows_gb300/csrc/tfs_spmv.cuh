@@ -386,11 +386,15 @@ k_spmv_pq_async(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p,
 // q = A p; (p, q); alpha, software-pipelined over the thread's rows c *
 // 256 + tid, c = blockIdx.x, blockIdx.x + gridDim.x, ... (the direct
 // kernels' rows and order).  W: the matrix's uniform slice width.
+// Minimum resident blocks per SM asked of the compiler (register cap).
+// Unconstrained (1) measured best on the 128^3 system: binary32 35.7 us at
+// 40 registers against 36.9 us capped to 32 (8 blocks, with spills);
+// binary64 74.6 against 75.4 us at 56.
 #ifndef TFS_PIPE_MINB32
-#define TFS_PIPE_MINB32 8
+#define TFS_PIPE_MINB32 1
 #endif
 #ifndef TFS_PIPE_MINB64
-#define TFS_PIPE_MINB64 4
+#define TFS_PIPE_MINB64 1
 #endif
 template <typename VT, bool MIXED, int W>
 __global__ void __launch_bounds__(TFS_TPB, sizeof(VT) == 4 ? TFS_PIPE_MINB32 : TFS_PIPE_MINB64)
