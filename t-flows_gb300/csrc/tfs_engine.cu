@@ -107,7 +107,7 @@ static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int b
 template <typename T, int NR, int MODE>
 static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, const T *b1, const T *b2,
                          T *o1, T *o2, const T *y1, const T *y2, int *count, bool with_tail = true,
-                         int tail_at = -1, int lvl_from = 0)
+                         int tail_at = -1, int lvl_from = 0, bool prey = false)
 {
     SellDev A = sell_of(h);
     const int L = h->n_levels, tail = tail_at >= 0 ? tail_at : h->tail_level;
@@ -132,7 +132,18 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
         const int bs = h->level_tpb;
         const int nb = (r1 - r0 + bs - 1) / bs;
         cudaError_t e;
-        if (bs == 1024)
+        if (MODE == 1 && prey) {
+            // Backward levels after a tail that releases them only past its
+            // own wait: start values computed before the dependency wait.
+            if (bs == 1024)
+                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 1024, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+            else if (bs == 512)
+                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 512, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+            else if (bs == 128)
+                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 128, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+            else
+                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 256, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+        } else if (bs == 1024)
             e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 1024>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         else if (bs == 512)
             e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 512>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
@@ -892,6 +903,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
     if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
+    env = getenv("TFS_BWD_PRE");
+    if (env && strcmp(env, "0") == 0) h->bwd_pre = 0;
     env = getenv("TFS_TAIL_PF");
     if (env && strcmp(env, "0") == 0) h->tail_pf = 0;
     env = getenv("TFS_FUSE_L0");
@@ -1216,7 +1229,8 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         const int from = fuse_l0 ? 1 : 0;
         if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
-        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from))) return rc;
+        if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from,
+                                         tails && h->bwd_pre))) return rc;
         if (fuse_l0) {
             const int l0 = h->lvl_begin[1];
             cudaError_t e = launch_ex(h->use_pdl != 0, k_sweep0_rho<T>, (l0 + T_ - 1) / T_, T_, s, A, val,
@@ -1227,7 +1241,8 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     } else {
         if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 2>, k_sweep_tailc<T, 2>))) return rc;
-        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at))) return rc;
+        if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, 0,
+                                         tails && h->bwd_pre))) return rc;
     }
     return TFS_OK;
 }

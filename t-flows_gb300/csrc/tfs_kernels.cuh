@@ -742,7 +742,47 @@ k_sweep_lv(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
 // level's blocks could become resident earlier) measured 1.4x and 2.3x
 // slower on the 128^3 system, since a thread's rows then run their dependent
 // gathers one after the other.
-template <typename T, int NR, int MODE, int BS = TFS_TPB>
+// Backward row (MODE 1 of sweep_row) whose start value s = y_i / (D_i +
+// TINY) and D_i were computed before the dependency wait.
+template <typename T, int NR, int NP>
+__device__ __forceinline__ void sweep_row_bwd_pre(const SellDev &A, const T *__restrict__ val, T *o1, T *o2,
+                                                  int i, const RowGeom &g, const int *kk, const T *aa, T s1,
+                                                  T s2, T di, bool skip)
+{
+    if (g.len == 0) {
+        if (skip) return;
+        o1[i] = (T)0;
+        if (NR == 2) o2[i] = (T)0;
+        return;
+    }
+    int j = g.dpos + 1;
+    const int j1 = g.len;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        if (j < j1) {
+            s1 = s1 - aa[q] * __ldcg(o1 + kk[q]);
+            if (NR == 2) s2 = s2 - aa[q] * __ldcg(o2 + kk[q]);
+            j++;
+        }
+    }
+    for (; j < j1; j++) {
+        const int ee = g.off + (j << 5);
+        const int k = __ldg(A.col + ee);
+        const T a = __ldg(val + ee);
+        s1 = s1 - a * __ldcg(o1 + k);
+        if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
+    }
+    if (skip) return;
+    o1[i] = s1 * di;
+    if (NR == 2) o2[i] = s2 * di;
+}
+
+//
+// PREY (backward sweep after a tail kernel, which releases its dependants
+// only once it has passed its own wait, so the forward sweep is complete
+// when this kernel starts): the row's start value y_i / (D_i + TINY) is
+// computed before the wait, taking the division off the dependent chain.
+template <typename T, int NR, int MODE, int BS = TFS_TPB, bool PREY = false>
 __global__ void __launch_bounds__(BS)
 k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
               T *o2, const T *y1, const T *y2, int row0, int row1, DevState *st, int first)
@@ -777,11 +817,21 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
                 }
         }
     }
+    T pdi = (T)0, ps1 = (T)0, ps2 = (T)0;
+    if (MODE == 1 && PREY && active && g.len > 0) {
+        pdi = d[i];
+        ps1 = y1[i] / (pdi + (T)TINY);
+        if (NR == 2) ps2 = y2[i] / (pdi + (T)TINY);
+    }
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
     const bool skip = st->done != 0;
     if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
+    if (MODE == 1 && PREY) {
+        if (active) sweep_row_bwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
+    } else if (active) {
+        sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
+    }
 }
 
 // Levels [l_begin, l_end) of a sweep in one block (descending for MODE 1);
@@ -843,8 +893,10 @@ __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
               T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
 {
-    cudaTriggerProgrammaticLaunchCompletion();
+    // The trigger follows the wait: the backward level kernels launched
+    // after a tail read the forward sweep's output before their own wait.
     cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool skip = st->done != 0;
     const int nl = l_end - l_begin;
     for (int q = 0; q < nl; q++) {
@@ -907,8 +959,8 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
             }
         if (g.len > 0) { bi = b[i]; di = d[i]; }
     }
-    cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();   // after the wait, as in k_sweep_tail2
     const bool skip = st->done != 0;
     T yi = (T)0;
     for (int l = l_begin; l < l_end; l++) {
@@ -955,8 +1007,8 @@ __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tailc(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
               T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
 {
-    cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();   // after the wait, as in k_sweep_tail2
     if (st->done) return;
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
     const int t = (int)cl.block_rank() * TFS_SWEEP_TPB + (int)threadIdx.x;

@@ -399,6 +399,40 @@ def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17)])
+def test_backward_precompute_bitwise(shape, monkeypatch, gpu):
+    """Backward level kernels that compute their rows' start values y_i /
+    (D_i + TINY) before the dependency wait (the tail releases them only
+    past its own wait) give the DIC application, DIC-CG solves in both
+    precisions and the literal two-sequence BiCG bitwise equal to the
+    in-chain division (TFS_BWD_PRE=0)."""
+    s = system(POISSON, *shape)
+    ref = oracle_solve(s, TFS_CG, 2)
+    b = np.random.default_rng(6).uniform(-1, 1, s.n)
+    out = {}
+    for pre in ("1", "0"):
+        monkeypatch.setenv("TFS_BWD_PRE", pre)
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode) as sol:
+                if mode == TFS_FP64:
+                    res.append(sol.prec_solve(s.val, 2, b))
+                x, r = np.zeros(s.n), s.b.copy()
+                st = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
+                assert st.status == 0 and st.fin_res < ref["tol"]
+                res += [x, r, st.niter]
+        monkeypatch.setenv("TFS_BICG", "literal")
+        with Solver(s.matrix()) as sol:
+            x, r = np.zeros(s.n), s.b.copy()
+            st = sol.solve(TFS_BICG, s.val, x, r, 2, 2000, ref["tol"])
+            res += [x, r, st.niter]
+        monkeypatch.delenv("TFS_BICG")
+        out[pre] = res
+    assert np.array_equal(out["1"][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+    for a, c in zip(out["1"], out["0"]):
+        assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("fuse", ["0", "1", "2"])
 def test_level0_fusion_parity(fuse, monkeypatch, gpu):
     """DIC-CG with level 0 swept inside the residual, update and rho kernels
