@@ -358,15 +358,42 @@ k_sweep0_rho(SellDev A, const T *__restrict__ val, const T *d, const T *r, T *z,
                 aa[q] = __ldg(val + ee);
             }
     }
+    // Level 0's forward values and r come from kernels that completed before
+    // the sweep's first level kernel started: the row's start value
+    // y_i / (D_i + TINY) and r_i are ready before the wait.
+    T di = (T)0, s0 = (T)0, ri = (T)0;
+    if (active && g.len > 0) {
+        di = d[i];
+        s0 = y[i] / (di + (T)TINY);
+        ri = r[i];
+    }
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
     const bool stop = (st->done | st->need_true) != 0;
     T acc = (T)0;
     if (active) {
-        sweep_row<T, 1, 1, 4>(A, val, (T *)d, nullptr, nullptr, z, nullptr, y, nullptr, i, g, kk, aa, stop);
-        if (!stop) {
-            if constexpr (sizeof(T) == 4) acc = fmaf(r[i], z[i], acc);
-            else acc = fma(r[i], z[i], acc);
+        if (g.len == 0) {
+            if (!stop) z[i] = (T)0;   // padding row: r_i z_i adds (r_i = 0) * 0
+            if (!stop) {
+                if constexpr (sizeof(T) == 4) acc = fmaf(r[i], (T)0, acc);
+                else acc = fma(r[i], (T)0, acc);
+            }
+        } else {
+            T sv = s0;
+            int j = g.dpos + 1;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (j < g.len) { sv = sv - aa[q] * __ldcg(z + kk[q]); j++; }
+            for (; j < g.len; j++) {
+                const int ee = g.off + (j << 5);
+                sv = sv - __ldg(val + ee) * __ldcg(z + __ldg(A.col + ee));
+            }
+            const T zi = sv * di;
+            if (!stop) {
+                z[i] = zi;
+                if constexpr (sizeof(T) == 4) acc = fmaf(ri, zi, acc);
+                else acc = fma(ri, zi, acc);
+            }
         }
     }
     for (int k = l0_rows + blockIdx.x * TFS_TPB + threadIdx.x; k < n_int; k += gridDim.x * TFS_TPB) {
