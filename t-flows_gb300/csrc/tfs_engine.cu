@@ -258,32 +258,32 @@ static void launch_spmv_async(const tfs_handle *h, cudaStream_t s, int G, int sm
 }
 
 template <typename VT, bool MIXED>
-static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q)
+static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
 {
     const SellDev A = sell_of(h);
     const int G = h->grid_spmv;
     switch (h->sell_width) {
-    case 1: k_spmv_pq_pipe<VT, MIXED, 1><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 2: k_spmv_pq_pipe<VT, MIXED, 2><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 3: k_spmv_pq_pipe<VT, MIXED, 3><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 4: k_spmv_pq_pipe<VT, MIXED, 4><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 5: k_spmv_pq_pipe<VT, MIXED, 5><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 6: k_spmv_pq_pipe<VT, MIXED, 6><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    case 7: k_spmv_pq_pipe<VT, MIXED, 7><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
-    default: k_spmv_pq_pipe<VT, MIXED, 8><<<G, TFS_TPB, 0, s>>>(A, val, p, q, h->st, h->part); break;
+    case 1: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 1>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 2: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 2>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 3: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 3>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 4: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 4>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 5: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 5>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 6: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 6>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 7: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 7>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    default: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 8>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
     }
 }
 
 // q = A p, (p, q) and alpha of a CG iteration on stream s, binary32 (mixed)
 // or binary64, with the handle's SpMV kernel over grid_spmv (virtual)
 // blocks.
-static void launch_spmv_pq(tfs_handle *h, cudaStream_t s, bool mixed)
+static void launch_spmv_pq(tfs_handle *h, cudaStream_t s, bool mixed, bool pdl = false)
 {
     const SellDev A = sell_of(h);
     const int VG = h->grid_spmv;
     if (h->spmv_kind == TFS_SPMV_PIPE) {
-        if (mixed) launch_spmv_pipe<float, true>(h, s, h->val32, h->f.p, h->f.q);
-        else launch_spmv_pipe<double, false>(h, s, h->val, h->v.p, h->v.q);
+        if (mixed) launch_spmv_pipe<float, true>(h, s, h->val32, h->f.p, h->f.q, pdl);
+        else launch_spmv_pipe<double, false>(h, s, h->val, h->v.p, h->v.q, pdl);
     } else if (h->spmv_kind == TFS_SPMV_ASYNC && mixed) {
         launch_spmv_async<float, true>(h, s, std::min(VG, h->sm_count * h->bulk_occ32), h->bulk_smem32, h->val32,
                                        h->f.p, h->f.q);
@@ -903,6 +903,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
     if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
     if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
+    env = getenv("TFS_PDL_VEC");
+    if (env && strcmp(env, "0") == 0) h->pdl_vec = 0;
     env = getenv("TFS_BWD_PRE");
     if (env && strcmp(env, "0") == 0) h->bwd_pre = 0;
     env = getenv("TFS_TAIL_PF");
@@ -1319,12 +1321,15 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             *count += 5;
         } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
             const int l0 = dic_l0_rows(h, method, prec);
+            // The vector kernels after the sweeps are PDL-chained as well
+            // (each waits for its predecessor before it reads anything).
+            const bool pv = h->use_pdl && h->pdl_vec;
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count, true))) return rc;
-            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            launch_spmv_pq(h, s, true);
-            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part, l0 / 4);
-            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
-            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond, l0);
+            launch_ex(pv, k_mx_cg_p4, G4, T, s, n4, F, (const DevState *)h->st);
+            launch_spmv_pq(h, s, true, pv);
+            launch_ex(pv, k_mx_cg_update4<false>, G4, T, s, n4, F, h->st, h->part, l0 / 4);
+            launch_ex(pv, k_mx_fold4, G4, T, s, n4, V, F, (const DevState *)h->st);
+            launch_ex(pv, k_mx_true<0, false>, G, T, s, A, (const double *)h->val, V, F, h->st, h->part, prec, cond, l0);
             *count += 5;
         } else if (prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
@@ -1336,11 +1341,13 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
             *count += 6;
         } else {
-            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            launch_spmv_pq(h, s, true);
-            k_mx_cg_update4<true><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
-            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
-            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            // Diagonal (or no) preconditioner: the whole body PDL-chained.
+            const bool pv = h->use_pdl && h->pdl_vec;
+            launch_ex(pv, k_mx_cg_p4, G4, T, s, n4, F, (const DevState *)h->st);
+            launch_spmv_pq(h, s, true, pv);
+            launch_ex(pv, k_mx_cg_update4<true>, G4, T, s, n4, F, h->st, h->part, 0);
+            launch_ex(pv, k_mx_fold4, G4, T, s, n4, V, F, (const DevState *)h->st);
+            launch_ex(pv, k_mx_true<0, false>, G, T, s, A, (const double *)h->val, V, F, h->st, h->part, prec, cond, 0);
             *count += 5;
         }
     } else if (method == TFS_BICG) {

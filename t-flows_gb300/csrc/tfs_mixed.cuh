@@ -40,6 +40,10 @@ __global__ void __launch_bounds__(TFS_TPB)
 k_mx_true(SellDev A, const double *__restrict__ val, Vec64 V, Vec32 F, DevState *st,
           double *part, int prec, cudaGraphConditionalHandle cond, int l0_rows = 0)
 {
+    // PDL secondary (a no-op when launched plainly).  No early trigger: a
+    // DIC level chain launched after this kernel reads r before its own
+    // waits, so it must start only once this kernel has completed.
+    cudaGridDependencySynchronize();
     if (st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0u);
         return;
@@ -248,6 +252,10 @@ k_mx_cg_update(int n_chunks, Vec64 V, Vec32 F, DevState *st, double *part)
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p4(int n4, Vec32 F, const DevState *st)
 {
+    // PDL secondary (a no-op when launched plainly): wait for the
+    // predecessor before reading anything, then let the successor launch.
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = (st->done | st->need_true) != 0;
     const int it = st->iter;
     const float beta = st->beta32;           // (float)(rho / rho_old), published once
@@ -288,6 +296,8 @@ template <bool FUSED>
 __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevState *st, double *part,
                                                            int l0_rows4 = 0)
 {
+    cudaGridDependencySynchronize();   // PDL secondary, as k_mx_cg_p4
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = (st->done | st->need_true) != 0;
     const float a = st->alpha32;             // (float) alpha, published once
     const float4 *p4 = (const float4 *)F.p, *q4 = (const float4 *)F.q, *d4 = (const float4 *)F.d;
@@ -319,6 +329,8 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_update4(int n4, Vec32 F, DevS
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_fold4(int n4, Vec64 V, Vec32 F, const DevState *st)
 {
+    cudaGridDependencySynchronize();   // PDL secondary, as k_mx_cg_p4
+    cudaTriggerProgrammaticLaunchCompletion();
     if (st->done || !st->need_true) return;
     float4 *e4 = (float4 *)F.e;
     double2 *x2 = (double2 *)V.x;

@@ -140,6 +140,11 @@ static bool try_start(tfs_server *S, Request *r)
             r->t_done = clk::now();
             return true;
         }
+        // Solves share the GPU here: PDL-chained vector kernels would park
+        // their blocks at the dependency wait while other requests' kernels
+        // could use the slots (measured 232 against 252 solves/s on the
+        // serving trace), so the server's handles launch them plainly.
+        sy.h->pdl_vec = 0;
         sy.bytes = need;
         S->resident += need;
         S->stats.registrations++;

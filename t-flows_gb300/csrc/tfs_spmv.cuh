@@ -413,6 +413,8 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
 #pragma unroll
         for (int j = 0; j < W; j++) nk[j] = __ldg(A.col + off + 32 * j);
     }
+    cudaGridDependencySynchronize();   // PDL secondary of the p update (a no-op when launched plainly)
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = MIXED ? (st->done | st->need_true) != 0 : st->done != 0;
     if (stop) return;
     if (blockIdx.x == 0 && tid == 0) st->t_spmv0 = gtimer();
