@@ -1419,22 +1419,25 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             *count += 2;
         } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
             const int l0 = dic_l0_rows(h, method, prec);
+            const bool pv = h->use_pdl && h->pdl_vec;   // vector kernels PDL-chained
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count, true))) return rc;
-            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            launch_spmv_pq(h, s, false);
-            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond, l0);
+            launch_ex(pv, k_cg_p<true>, G, T, s, nc, V, (const DevState *)h->st);
+            launch_spmv_pq(h, s, false, pv);
+            launch_ex(pv, k_cg_update<false>, G, T, s, nc, V, h->st, h->part, cond, l0);
             *count += 3;
         } else if (prec == 2) {
+            const bool pv = h->use_pdl && h->pdl_vec;
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count))) return rc;
-            k_dot_rho<0><<<G, T, 0, s>>>(nc, V, h->st, h->part);
-            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            launch_spmv_pq(h, s, false);
-            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            launch_ex(pv, k_dot_rho<0>, G, T, s, nc, V, h->st, h->part);
+            launch_ex(pv, k_cg_p<true>, G, T, s, nc, V, (const DevState *)h->st);
+            launch_spmv_pq(h, s, false, pv);
+            launch_ex(pv, k_cg_update<false>, G, T, s, nc, V, h->st, h->part, cond, 0);
             *count += 4;
         } else {
-            k_cg_p<true><<<G, T, 0, s>>>(nc, V, h->st);
-            launch_spmv_pq(h, s, false);
-            k_cg_update<true><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
+            const bool pv = h->use_pdl && h->pdl_vec;
+            launch_ex(pv, k_cg_p<true>, G, T, s, nc, V, (const DevState *)h->st);
+            launch_spmv_pq(h, s, false, pv);
+            launch_ex(pv, k_cg_update<true>, G, T, s, nc, V, h->st, h->part, cond, 0);
             *count += 3;
         }
     } else if (method == TFS_BICG) {

@@ -1036,6 +1036,10 @@ template <int METHOD>
 __global__ void __launch_bounds__(TFS_TPB)
 k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
 {
+    // PDL secondary (a no-op when launched plainly): wait for the
+    // predecessor before reading anything, then let the successor launch.
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = st->done != 0;
     double acc = 0.0;
     TFS_QUAD_BEGIN(n_chunks)
@@ -1064,6 +1068,8 @@ k_dot_rho(int n_chunks, Vec64 V, DevState *st, double *part)
 template <bool FROMZ>
 __global__ void __launch_bounds__(TFS_TPB) k_cg_p(int n_chunks, Vec64 V, const DevState *st)
 {
+    cudaGridDependencySynchronize();   // PDL secondary, as k_dot_rho
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = st->done != 0;
     const int it = st->iter;
     const double beta = st->beta;            // rho / rho_old, published once
@@ -1112,6 +1118,9 @@ __global__ void __launch_bounds__(TFS_TPB)
 k_cg_update(int n_chunks, Vec64 V, DevState *st, double *part, cudaGraphConditionalHandle cond,
             int l0_rows = 0)
 {
+    // PDL secondary; no early trigger: the DIC level chain of the next
+    // iteration reads r before its own waits.
+    cudaGridDependencySynchronize();
     const bool stop = st->done != 0;
     const double alfa = st->alpha;
     double e2 = 0.0, rz = 0.0;
