@@ -132,17 +132,18 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
         const int bs = h->level_tpb;
         const int nb = (r1 - r0 + bs - 1) / bs;
         cudaError_t e;
-        if (MODE == 1 && prey) {
+        if ((MODE == 1 || MODE == 0) && prey) {
             // Backward levels after a tail that releases them only past its
-            // own wait: start values computed before the dependency wait.
+            // own wait: start values computed before the dependency wait;
+            // forward levels: right-hand side and D loaded before it.
             if (bs == 1024)
-                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 1024, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+                e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 1024, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
             else if (bs == 512)
-                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 512, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+                e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 512, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
             else if (bs == 128)
-                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 128, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+                e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 128, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
             else
-                e = launch_ex(pdl, k_sweep_level<T, NR, 1, 256, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
+                e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 256, true>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         } else if (bs == 1024)
             e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 1024>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         else if (bs == 512)
@@ -905,6 +906,8 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
     env = getenv("TFS_PDL_VEC");
     if (env && strcmp(env, "0") == 0) h->pdl_vec = 0;
+    env = getenv("TFS_FWD_PRE");
+    if (env && strcmp(env, "0") == 0) h->fwd_pre = 0;
     env = getenv("TFS_BWD_PRE");
     if (env && strcmp(env, "0") == 0) h->bwd_pre = 0;
     env = getenv("TFS_TAIL_PF");
@@ -1229,7 +1232,8 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         // true-residual kernels, and the backward sweep of level 0 by
         // k_sweep0_rho together with rho.
         const int from = fuse_l0 ? 1 : 0;
-        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from))) return rc;
+        if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from,
+                                         h->fwd_pre != 0))) return rc;
         if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
         if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from,
                                          tails && h->bwd_pre))) return rc;

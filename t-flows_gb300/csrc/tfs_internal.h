@@ -132,6 +132,7 @@ struct tfs_handle {
     int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative, 3: slabs
     int use_pdl = 1;                   // programmatic dependent launch between level kernels
     int pdl_vec = 1;                   // binary32 CG vector kernels PDL-chained (TFS_PDL_VEC=0: plain launches)
+    int fwd_pre = 1;                   // forward level kernels: right-hand side and D before the wait
     int bwd_pre = 1;                   // backward level kernels after a tail: start values before the wait
     int tail_pf = 1;                   // prefetching tail (k_sweep_tail1): one row per thread, loads ahead
     int pf_tail_level = 0, pf_C = 0;   // its first level and cluster size (0: not usable)

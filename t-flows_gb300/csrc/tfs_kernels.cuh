@@ -777,6 +777,41 @@ __device__ __forceinline__ void sweep_row_bwd_pre(const SellDev &A, const T *__r
     if (NR == 2) o2[i] = s2 * di;
 }
 
+// Forward row (MODE 0 of sweep_row) whose right-hand side b_i and D_i were
+// loaded before the dependency wait.
+template <typename T, int NR, int NP>
+__device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__restrict__ val, T *o1, T *o2,
+                                                  int i, const RowGeom &g, const int *kk, const T *aa, T s1,
+                                                  T s2, T di, bool skip)
+{
+    if (g.len == 0) {
+        if (skip) return;
+        o1[i] = (T)0;
+        if (NR == 2) o2[i] = (T)0;
+        return;
+    }
+    int j = 0;
+    const int j1 = g.dpos;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        if (j < j1) {
+            s1 = s1 - aa[q] * __ldcg(o1 + kk[q]);
+            if (NR == 2) s2 = s2 - aa[q] * __ldcg(o2 + kk[q]);
+            j++;
+        }
+    }
+    for (; j < j1; j++) {
+        const int ee = g.off + (j << 5);
+        const int k = __ldg(A.col + ee);
+        const T a = __ldg(val + ee);
+        s1 = s1 - a * __ldcg(o1 + k);
+        if (NR == 2) s2 = s2 - a * __ldcg(o2 + k);
+    }
+    if (skip) return;
+    o1[i] = s1 * di;
+    if (NR == 2) o2[i] = s2 * di;
+}
+
 //
 // PREY (backward sweep after a tail kernel, which releases its dependants
 // only once it has passed its own wait, so the forward sweep is complete
@@ -823,12 +858,22 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
         ps1 = y1[i] / (pdi + (T)TINY);
         if (NR == 2) ps2 = y2[i] / (pdi + (T)TINY);
     }
+    // Forward sweep: the right-hand side and D come from kernels that
+    // completed before the level chain started, so they load before the
+    // wait as well (PREY = true for MODE 0).
+    if (MODE == 0 && PREY && active && g.len > 0) {
+        pdi = d[i];
+        ps1 = b1[i];
+        if (NR == 2) ps2 = b2[i];
+    }
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
     const bool skip = st->done != 0;
     if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
     if (MODE == 1 && PREY) {
         if (active) sweep_row_bwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
+    } else if (MODE == 0 && PREY) {
+        if (active) sweep_row_fwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
     } else if (active) {
         sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
     }

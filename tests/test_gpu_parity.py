@@ -399,19 +399,21 @@ def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("knob", ["TFS_BWD_PRE", "TFS_FWD_PRE"])
 @pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17)])
-def test_backward_precompute_bitwise(shape, monkeypatch, gpu):
-    """Backward level kernels that compute their rows' start values y_i /
-    (D_i + TINY) before the dependency wait (the tail releases them only
-    past its own wait) give the DIC application, DIC-CG solves in both
-    precisions and the literal two-sequence BiCG bitwise equal to the
-    in-chain division (TFS_BWD_PRE=0)."""
+def test_backward_precompute_bitwise(shape, knob, monkeypatch, gpu):
+    """Level kernels that load or compute their rows' start values before
+    the dependency wait -- backward: y_i / (D_i + TINY) (the tail releases
+    them only past its own wait); forward: b_i and D_i (written before the
+    level chain starts) -- give the DIC application, DIC-CG solves in both
+    precisions and the literal two-sequence BiCG bitwise equal to loading
+    them after the wait (TFS_BWD_PRE=0, TFS_FWD_PRE=0)."""
     s = system(POISSON, *shape)
     ref = oracle_solve(s, TFS_CG, 2)
     b = np.random.default_rng(6).uniform(-1, 1, s.n)
     out = {}
     for pre in ("1", "0"):
-        monkeypatch.setenv("TFS_BWD_PRE", pre)
+        monkeypatch.setenv(knob, pre)
         res = []
         for mode in (TFS_FP64, TFS_MIXED):
             with Solver(s.matrix(), precision=mode) as sol:
