@@ -131,3 +131,45 @@ def test_cns_geo_fixture_is_reproduced(tmp_path):
     make_gambit.write_reference_format(REF, "chan", tmp_path)
     for ext in ("cns", "geo"):
         assert (tmp_path / f"chan.{ext}").read_bytes() == (GOLDEN / f"chan.{ext}").read_bytes()
+
+
+def test_neu_reader_small_synthetic(tmp_path):
+    """A two-brick Gambit file written here: the shared face is found once,
+    boundary-set faces map to boundary faces, area vectors point out of c1,
+    and an unsupported element type is refused."""
+    nodes = [(x, y, z) for z in (0.0, 1.0) for y in (0.0, 1.0) for x in (0.0, 1.0, 2.0)]
+    # brick node order of Gambit: (0,0,0),(1,0,0),(0,1,0),(1,1,0),(0,0,1),(1,0,1),(0,1,1),(1,1,1)
+    def nid(ix, iy, iz):
+        return 1 + ix + 3 * iy + 6 * iz
+    cells = []
+    for c in range(2):
+        cells.append([nid(c + dx, dy, dz) for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)])
+    lines = ["        CONTROL INFO 2.3.16", "** GAMBIT NEUTRAL FILE", "t", "PROGRAM:  test", "date",
+             "     NUMNP     NELEM     NGRPS    NBSETS     NDFCD     NDFVL",
+             f"{len(nodes):10d}{len(cells):10d}         1         1         3         3", "ENDOFSECTION",
+             "   NODAL COORDINATES 2.3.16"]
+    for k, (x, y, z) in enumerate(nodes):
+        lines.append(f"{k + 1:10d}{x:20.11e}{y:20.11e}{z:20.11e}")
+    lines += ["ENDOFSECTION", "      ELEMENTS/CELLS 2.3.16"]
+    for k, c in enumerate(cells):
+        lines.append(f"{k + 1:8d} 4  8 " + " ".join(str(v) for v in c[:7]))
+        lines.append("               " + str(c[7]))
+    # face 4 of Gambit's brick is the x = 0 side: cell 1's left face
+    lines += ["ENDOFSECTION", " BOUNDARY CONDITIONS 2.3.16", "                            left       1       1       0       6",
+              "         1    4    4", "ENDOFSECTION"]
+    p = tmp_path / "two.neu"
+    p.write_text("\n".join(lines) + "\n")
+    m = G.read_neu(p)
+    f = G.mesh_faces(m)
+    g = G.geometry(m, f)
+    assert m.n_cells == 2 and len(f.faces_c) == 11
+    inner = f.faces_c[:, 1] > 0
+    assert inner.sum() == 1 and tuple(f.faces_c[inner][0]) == (1, 2)
+    assert np.allclose(g.face_area[inner][0], [1.0, 0.0, 0.0])
+    fid = f.face_of[m.bc[0].cells, m.bc[0].faces][0]
+    assert f.faces_c[fid, 1] == 0 and np.allclose(g.face_centre[fid], [0.0, 0.5, 0.5])
+    assert np.allclose(g.face_area[fid], [-1.0, 0.0, 0.0])
+    bad = p.read_text().replace("       1 4  8 ", "       1 9  8 ", 1)
+    (tmp_path / "bad.neu").write_text(bad)
+    with pytest.raises(ValueError):
+        G.read_neu(tmp_path / "bad.neu")
