@@ -157,3 +157,37 @@ def test_fortran_shim_binds_the_abi():
         assert f'bind(C, name="{name}")' in shim
     for sub in ("subroutine Cg(", "subroutine Bicg(", "subroutine Cgs("):
         assert sub in shim
+
+
+def test_abi_struct_layouts_match_ctypes(tmp_path):
+    """The structs of include/tfs_solver.h and their ctypes mirrors have the
+    same size and field offsets (compiled with the host C compiler)."""
+    import shutil
+    import subprocess
+    from tflows import lib as L
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    structs = {"tfs_stats": L.tfs_stats, "tfs_tuning": L.tfs_tuning, "tfs_result": L.tfs_result,
+               "tfs_server_stats": L.tfs_server_stats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "tfs_solver.h"', "int main(void) {"]
+    for name, py in structs.items():
+        lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{name} {fname} %zu\\n", offsetof({name}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    include = Path(__file__).resolve().parents[1] / "include"
+    subprocess.run([cc, "-std=c11", "-I", str(include), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            name, field, val = ln.split()
+            got[(name, field)] = int(val)
+    for name, py in structs.items():
+        assert got[(name, "size")] == C.sizeof(py), name
+        for fname, _ in py._fields_:
+            assert got[(name, fname)] == getattr(py, fname).offset, (name, fname)
