@@ -913,7 +913,7 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     env = getenv("TFS_TAIL_PF");
     if (env && strcmp(env, "0") == 0) h->tail_pf = 0;
     env = getenv("TFS_FUSE_L0");
-    if (env && (strcmp(env, "0") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
+    if (env && (strcmp(env, "0") == 0 || strcmp(env, "1") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
     env = getenv("TFS_LEVEL_TPB");
     if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
     env = getenv("TFS_PDL");
@@ -1259,9 +1259,10 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 // (k_mx_true, k_mx_cg_update4, k_residual, k_cg_update: y = r D) and whose
 // backward sweep runs with rho in k_sweep0_rho, or 0 when the plain level
 // schedule runs.  Level 0 must be one of the per-level kernels (not part of
-// a tail).  fuse_l0 = 1 fuses the binary32 iteration only: in binary64 the
-// fused body measured slower on the 128^3 Poisson system (5.98 against 6.11
-// solves/s), so it runs there only with fuse_l0 = 2.
+// a tail).  fuse_l0 = 2 (default) fuses both arithmetics, 1 the binary32
+// iteration only (the binary64 fused body first measured slower, 5.98
+// against 6.11 solves/s; since its level-0 rows compute their start values
+// before the dependency wait it is faster, 7.01 against 6.97).
 static int dic_l0_rows(const tfs_handle *h, int method, int prec)
 {
     if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0) return 0;

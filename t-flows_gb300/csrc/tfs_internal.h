@@ -136,7 +136,7 @@ struct tfs_handle {
     int bwd_pre = 1;                   // backward level kernels after a tail: start values before the wait
     int tail_pf = 1;                   // prefetching tail (k_sweep_tail1): one row per thread, loads ahead
     int pf_tail_level = 0, pf_C = 0;   // its first level and cluster size (0: not usable)
-    int fuse_l0 = 1;                   // DIC-CG level 0 swept inside the neighbouring kernels (1: binary32 iteration, 2: binary64 too)
+    int fuse_l0 = 2;                   // DIC-CG level 0 swept inside the neighbouring kernels (1: binary32 iteration only, 2: binary64 too)
     int level_tpb = TFS_TPB;           // threads per block of the level-sweep kernels (TFS_LEVEL_TPB;
                                        // 128/256/512/1024 measured 147.7/146.4/147.4/150.1 us per DIC application)
     int dic_r = 0;                     // rows per thread of the cooperative sweep (0: not chosen yet)
