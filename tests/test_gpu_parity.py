@@ -399,6 +399,37 @@ def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("kind", [POISSON, CONVDIFF])
+def test_per_slice_width_layout(kind, monkeypatch, gpu):
+    """Per-slice SELL widths (TFS_SELL_UNIFORM=0: slice offsets loaded
+    instead of computed, so the direct SpMV kernels and the level-loop tail
+    run instead of the uniform-width ones): SpMV, Prec_Solve bitwise equal
+    to the oracle and CG / BiCG / CGS within the parity gates."""
+    monkeypatch.setenv("TFS_SELL_UNIFORM", "0")
+    s = system(kind, 23, 19, 17)
+    b = np.random.default_rng(8).uniform(-1, 1, s.n)
+    methods = (TFS_CG,) if kind == POISSON else (TFS_BICG, TFS_CGS)
+    with Solver(s.matrix()) as sol:
+        assert np.array_equal(sol.spmv(s.val, b), O.spmv(s.n, s.row, s.col, s.val, b))
+        for prec in (1, 2):
+            assert np.array_equal(sol.prec_solve(s.val, prec, b),
+                                  O.prec_solve(s.n, s.row, s.col, s.dia, s.val, prec, b))
+        for method in methods:
+            for prec in (1, 2):
+                ref = oracle_solve(s, method, prec)
+                x, r = np.zeros(s.n), s.b.copy()
+                res = sol.solve(method, s.val, x, r, prec, 2000, ref["tol"])
+                assert iter_ok(res.niter, ref["niter"])
+                if ref["niter"] <= 2000:
+                    assert res.status == 0 and rel_l2(x, ref["x"]) <= SOL_REL
+    with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+        ref = oracle_solve(s, methods[0], 2)
+        x, r = np.zeros(s.n), s.b.copy()
+        res = sol.solve(methods[0], s.val, x, r, 2, 2000, ref["tol"])
+        if ref["niter"] <= 2000:
+            assert res.status == 0 and res.fin_res < ref["tol"]
+
+
 @pytest.mark.parametrize("knob", ["TFS_BWD_PRE", "TFS_FWD_PRE"])
 @pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17)])
 def test_backward_precompute_bitwise(shape, knob, monkeypatch, gpu):
