@@ -20,8 +20,9 @@ reset x = 0 and r1 = b, form the preconditioner, iterate to the tolerance.
 
 --impl reference times the reference's CPU solver (the oracle restatement;
 no Fortran compiler exists on either machine) on all host cores, one
-independent single-threaded solve per core, each step a bounded sample of
-iterations scaled to a full solve by the measured iteration count.
+independent single-threaded solve per core (run_reference says how a step
+is bounded).  Its processes build the same seeded system with the host-only
+generator libtfs_synth.so and never load the GPU solver library.
 
 Multi-GPU (torchrun): replicas only -- every rank solves its own seeded system
 (seed + rank) with no collective on the data path; the step time is the max
@@ -200,6 +201,18 @@ def pct(v: list[float], q: float) -> float:
     return s[k]
 
 
+def workload_config(args, n: int, nnz: int) -> dict:
+    """The `config` of a single-system workload, identical in both arms."""
+    kind, nside, method, prec, desc = WORKLOADS[args.workload]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return {"workload": args.workload, "description": desc, "cells": n, "nnz": nnz,
+            "solver": ["CG", "BiCG", "CGS"][method], "prec": ["none", "diag", "DIC"][prec],
+            "stop": "||b-Ax|| < 1e-8 ||b||, x0 = 0", "niter_limit": args.niter,
+            "l2": "inputs larger than L2 (matrix + vectors > 129 MB)" if nnz > 4000000
+                  else "inputs smaller than L2 (L2-resident system)",
+            "parallelism": f"replicas x{world}"}
+
+
 # ---------------------------------------------------------------- our arm
 
 def run_ours(args, dist: Dist) -> dict | None:
@@ -216,7 +229,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     s = tflows.SynthSystem(kind, nside, jitter=0.2, seed=BASE_SEED + dist.rank)
     log(f"[bench] system {desc}: n={s.n} nnz={s.nnz} ({time.perf_counter() - t0:.1f}s)")
     t0 = time.perf_counter()
-    sol = tflows.Solver(s.matrix())
+    from tflows.lib import TFS_OPT_LAUNCH
+    sol = tflows.Solver(s.matrix(), options={TFS_OPT_LAUNCH: 1 if args.eager else 0})
     log(f"[bench] registered: {sol.stats()['n_levels']} levels ({time.perf_counter() - t0:.1f}s)")
     # Launch shapes of the single-solve kernels, picked on this system
     # (tfs_autotune) before anything is timed.
@@ -415,11 +429,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         "ms_per_step": round(mixed["ms_per_solve"], 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded jittered-hex mesh, random cell numbering, RHS U[-1,1])",
-        "config": {"workload": args.workload, "description": desc, "cells": n, "nnz": nnz,
-                   "solver": ["CG", "BiCG", "CGS"][method], "prec": ["none", "diag", "DIC"][prec],
-                   "stop": "||b-Ax|| < 1e-8 ||b||, x0 = 0", "niter_limit": args.niter,
-                   "l2": "inputs larger than L2 (matrix + vectors > 129 MB)",
-                   "parallelism": f"replicas x{dist.world}"},
+        "config": workload_config(args, n, nnz),
         "p50_ms": round(mixed["p50_ms"], 4), "p99_ms": round(mixed["p99_ms"], 4),
         "fp64": results.get("fp64"), "mixed": results.get("mixed"),
         "mixed_over_fp64": round(mixed["solves_per_s"] / fp64["solves_per_s"], 4),
@@ -896,20 +906,25 @@ _REF = {}
 
 
 def _ref_init(kind, nside, seed):
+    # The reference arm builds its inputs with the host-only generator
+    # (libtfs_synth.so) and solves them with the oracle: the GPU solver
+    # library is never loaded in these processes.
     sys.path[:0] = [str(REPO), str(REPO / "t-flows_gb300")]
-    import tflows
-    _REF["s"] = tflows.SynthSystem(kind, nside, jitter=0.2, seed=seed)
+    from tflows.synth import SynthSystem
+    _REF["s"] = SynthSystem(kind, nside, jitter=0.2, seed=seed)
 
 
-def _ref_sample(arg):
+def _ref_solve(arg):
+    """One single-threaded binary64 solve of the workload's system by the
+    oracle, stopped after `iters` iterations (or at the tolerance)."""
     import numpy as np
     from oracle import tfs_oracle as O
-    method, prec, iters = arg
+    method, prec, iters, tol = arg
     s = _REF["s"]
     x, r = np.zeros(s.n), s.b.copy()
     t = time.perf_counter()
-    O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, iters, 0.0)
-    return time.perf_counter() - t
+    it, _, _ = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, iters, tol)
+    return time.perf_counter() - t, it
 
 
 def _serve_cpu_one(spec):
@@ -970,48 +985,80 @@ def run_reference_other(args) -> dict:
 
 
 def run_reference(args) -> dict:
+    """The reference's CPU solver (the oracle restatement of Cg/Bicg/Cgs) on
+    all host cores: one independent single-threaded binary64 solve per core,
+    the reference's sequential build being one process per system.
+
+    A step is a bounded sample of that work.  When one full solve takes at
+    most WHOLE_SOLVE_S seconds, every core runs one whole solve per step.
+    Otherwise every core runs the solve from x0 = 0 and stops after k
+    iterations (k sized for about SAMPLE_S seconds); the step then counts
+    (P + k I) / (P + n_it I) solves per core, where n_it is the iteration
+    count of a full solve and P (preconditioner form and initial residual)
+    and I (one iteration) are measured on the same system outside the timed
+    steps.  ms_per_step is the measured wall time of a step, so the timed
+    region is exactly the steps run."""
     import multiprocessing as mp
 
     import numpy as np
     if args.workload not in WORKLOADS:
         return run_reference_other(args)
+    WHOLE_SOLVE_S, SAMPLE_S = 5.0, 3.0
     kind, nside, method, prec, desc = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
-    # Full iteration count of the reference solve (one full solve, untimed).
     _ref_init(kind, nside, BASE_SEED)
     s = _REF["s"]
-    from oracle import tfs_oracle as O
     tol = REL_TOL * float(np.linalg.norm(s.b))
-    x, r = np.zeros(s.n), s.b.copy()
-    t = time.perf_counter()
-    full_it, _, _ = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, args.niter, tol)
-    full_s = time.perf_counter() - t
-    sample_it = max(1, min(full_it, args.ref_sample_iters))
-    log(f"[bench-ref] full solve {full_it} it in {full_s:.1f}s; sampling {sample_it} it x {cores} cores")
+    # Outside the timed steps: the prologue alone (niter = 0), a probe, and
+    # the full solve (iteration count and time) when it is short enough.
+    _ref_solve((method, prec, 0, tol))          # loads the oracle library
+    p_s, _ = _ref_solve((method, prec, 0, tol))
+    probe = 8
+    t_probe, _ = _ref_solve((method, prec, probe, tol))
+    it_s = max(1e-9, (t_probe - p_s) / probe)
+    if p_s + it_s * (args.niter + 1) <= 120.0:
+        full_s, full_it = _ref_solve((method, prec, args.niter, tol))
+        full_known = True
+    else:
+        full_it, full_s, full_known = args.niter + 1, p_s + it_s * (args.niter + 1), False
+    it_s = max(1e-9, (full_s - p_s) / max(1, full_it)) if full_known else it_s
+    if full_s <= WHOLE_SOLVE_S:
+        k, frac = args.niter, 1.0
+    else:
+        k = max(1, min(full_it, int(round((SAMPLE_S - p_s) / it_s))))
+        frac = (p_s + k * it_s) / (p_s + full_it * it_s)
+    log(f"[bench-ref] full solve {full_it} it in {full_s:.2f}s (prologue {p_s:.3f}s); "
+        f"step = {k if frac < 1 else 'all'} iterations x {cores} cores = {cores * frac:.4f} solves")
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores, initializer=_ref_init, initargs=(kind, nside, BASE_SEED)) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_sample, [(method, prec, sample_it)] * cores)
+            pool.map(_ref_solve, [(method, prec, k, tol)] * cores)
         step_s = []
         for _ in range(args.steps):
             t = time.perf_counter()
-            per = pool.map(_ref_sample, [(method, prec, sample_it)] * cores)
-            wall = time.perf_counter() - t
-            # scale the sample to a full solve on every core
-            step_s.append(wall * full_it / sample_it)
-    per_solve = statistics.mean(step_s)
-    value = cores / per_solve
+            pool.map(_ref_solve, [(method, prec, k, tol)] * cores)
+            step_s.append(time.perf_counter() - t)
+    total_s = sum(step_s)
+    value = cores * frac * args.steps / total_s
+    if frac >= 1.0:
+        sample = (f"each step: {cores} whole single-threaded binary64 solves, one per core "
+                  f"({full_it} iterations each)")
+    else:
+        sample = (f"each step: {cores} single-threaded binary64 solves from x0 = 0, one per core, each "
+                  f"stopped after {k} of the {full_it} iterations of a full solve"
+                  f"{'' if full_known else ' (the iteration limit + 1: a full solve was not run)'}, "
+                  f"counted as {frac:.5f} of a solve each (prologue {p_s:.3f} s and {it_s * 1e3:.2f} ms "
+                  f"per iteration, measured outside the steps; a full solve took {full_s:.1f} s)")
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT,
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(per_solve * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(total_s / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded system as our arm)",
-        "config": {"workload": args.workload, "description": desc, "cells": s.n, "nnz": s.nnz,
-                   "stop": "||r|| < 1e-8 ||b||, x0 = 0", "iterations": full_it},
+        "config": workload_config(args, s.n, s.nnz),
         "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent single-threaded binary64 solves (one per "
-                                   f"core), each step {sample_it} of {full_it} iterations scaled "
-                                   f"to a full solve; one full solve took {full_s:.1f} s"},
+                         "sample": sample},
+        "reference_solve": {"iterations": full_it, "seconds_one_core": round(full_s, 3),
+                            "full_solve_run": full_known},
         "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -1035,7 +1082,6 @@ def main(argv=None) -> int:
     ap.add_argument("--batch-systems", type=int, default=256)
     ap.add_argument("--niter", type=int, default=5000)
     ap.add_argument("--spmv-reps", type=int, default=50)
-    ap.add_argument("--ref-sample-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
@@ -1044,6 +1090,9 @@ def main(argv=None) -> int:
                     help="skip the device topology / assembly measurements")
     ap.add_argument("--modes", default="fp64,mixed",
                     help="arithmetic legs to run (profiling runs may pick one)")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch the solve kernels from a host loop instead of a CUDA graph "
+                         "(TFS_OPT_LAUNCH = 1), for kernel-level profiling")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

@@ -88,8 +88,7 @@ typedef struct tfs_stats {
     int64_t  kernel_launches;   /* kernels launched by the last solve            */
     int64_t  device_bytes;      /* device memory held by the handle             */
     int32_t  spmv_kernel;       /* SpMV kernel of the CG iterations: 0 direct,
-                                   1 software-pipelined, 2 bulk-copy,
-                                   3 cp.async-staged                          */
+                                   1 software-pipelined                        */
     int32_t  sell_width;        /* uniform SELL-32 slice width, 0 if per slice  */
 } tfs_stats;
 
@@ -111,6 +110,53 @@ int tfs_release(tfs_handle *h);
 /* Arithmetic of the Krylov iterations for later solves on h: TFS_FP64 or
  * TFS_MIXED.  Replaces nothing in the reference (it has binary64 only). */
 int tfs_set_precision(tfs_handle *h, int mode);
+
+/* Precision (TFS_FP64 or TFS_MIXED) of the handles that the library keeps
+ * for tfs_cg/tfs_bicg/tfs_cgs and tfs_solve(h = NULL): those already built
+ * and those built later.  A Fortran caller selects mixed precision for its
+ * drop-in Cg/Bicg/Cgs calls with this one call.  Replaces nothing in the
+ * reference. */
+int tfs_set_default_precision(int mode);
+
+/* ---- options of a handle ------------------------------------------------
+ * Alternatives the library was measured with, kept selectable for profiling
+ * and for the tests that check them against each other.  The defaults are the
+ * fastest measured on GB300.  Except TFS_OPT_FUSE_L0 (another summation
+ * order of rho in DIC-CG), every alternative gives bitwise the same results.
+ * Setting an option drops the handle's captured graphs; the layout options
+ * (TFS_OPT_LAYOUT, TFS_OPT_SELL_UNIFORM) also drop its device layout, which
+ * the next solve rebuilds.  No option is read from the environment. */
+#define TFS_OPT_LAUNCH        1  /* 0 one CUDA graph per solve (default); 1 eager
+                                    launches from a host loop (kernel tracing)   */
+#define TFS_OPT_LAYOUT        2  /* 0 RCM row order unless DIC (default); 1 DIC
+                                    level order for every preconditioner        */
+#define TFS_OPT_BICG          3  /* 0 BiCG on the CG kernels (default: its iterates
+                                    equal CG's bit for bit); 1 both sequences   */
+#define TFS_OPT_SELL_UNIFORM  4  /* 1 one SELL slice width when it costs <= 5%
+                                    padding (default); 0 per-slice widths       */
+#define TFS_OPT_SPMV          5  /* 1 software-pipelined SpMV where the width
+                                    allows (default); 0 the direct kernel       */
+#define TFS_OPT_SPMV_GRID     6  /* 0 8 blocks per SM, grid-stride (default);
+                                    1 one block per 256-row chunk               */
+#define TFS_OPT_LEVEL_TPB     7  /* threads per block of the DIC level kernels:
+                                    128, 256 (default), 512 or 1024             */
+#define TFS_OPT_TAIL_PF       8  /* 1 prefetching one-block tail (default); 0 the
+                                    level loop                                  */
+#define TFS_OPT_FUSE_L0       9  /* DIC-CG level 0 swept inside its neighbouring
+                                    kernels: 2 both arithmetics (default), 1
+                                    binary32 only, 0 off                        */
+#define TFS_OPT_PDL          10  /* 1 programmatic dependent launch between the
+                                    level kernels (default); 0 plain launches   */
+#define TFS_OPT_PDL_VEC      11  /* 1 PDL-chained CG vector kernels (default); 0 */
+#define TFS_OPT_FWD_PRE      12  /* 1 forward level kernels load b and D before
+                                    their dependency wait (default); 0          */
+#define TFS_OPT_BWD_PRE      13  /* 1 backward level kernels compute their start
+                                    values before the wait (default); 0         */
+
+/* Set / read one option of a handle.  TFS_ERR_ARG for an unknown option or
+ * value.  Replaces nothing in the reference. */
+int tfs_set_option(tfs_handle *h, int option, int value);
+int tfs_get_option(const tfs_handle *h, int option, int *value);
 
 /* ---- solves ------------------------------------------------------------- */
 

@@ -1,6 +1,8 @@
 /*
- * tfs_synth.h -- seeded synthetic finite-volume systems (host code in
- * libtfs_gb300.so) used by the benchmark and the parity tests.
+ * tfs_synth.h -- seeded synthetic finite-volume systems used by the benchmark
+ * and the parity tests.  Host code only, in its own library libtfs_synth.so
+ * (tfs_synth.cpp with the host topology builder it calls), so that a process
+ * that only needs the inputs never loads the GPU solver library.
  *
  * A system is an nx*ny*nz hexahedral mesh of cell size h = 1/nx on
  * [0,1]x[0,ny/nx]x[0,nz/nx], interior nodes jittered by U(-j*h, j*h) per

@@ -29,7 +29,7 @@
  *   - On the first early exit (||b|| < tol, Cg.f90:55-58) the reference
  *     returns an uninitialised local as fin_res.  The oracle returns ||b||,
  *     as the GPU library does; ini_res is left untouched, as in the reference.
- *   - Cgs.f90:338 adds r2*v2 into an uninitialised `alfa` that Cgs.f90:353
+ *   - Cgs.f90:142 adds r2*v2 into an uninitialised `alfa` that Cgs.f90:157
  *     overwrites before use; the statement has no effect and is not restated.
  */
 #include <math.h>

@@ -22,7 +22,6 @@
 #include "tfs_internal.h"
 #include "tfs_kernels.cuh"
 #include "tfs_mixed.cuh"
-#include "tfs_dic.cuh"
 #include "tfs_spmv.cuh"
 
 using namespace tfs;
@@ -163,18 +162,6 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
     return TFS_OK;
 }
 
-static TileTable tile_table(const tfs_handle *h)
-{
-    TileTable t;
-    t.n_tiles = h->n_tiles;
-    t.n_levels = h->n_levels;
-    t.tail_level = h->tail_level;
-    t.tile = h->tiles;
-    t.lvl_begin = h->d_lvl_begin;
-    t.lvl_tiles = h->d_lvl_tiles;
-    return t;
-}
-
 template <typename T>
 static int dalloc(tfs_handle *h, T **p, size_t count)
 {
@@ -185,77 +172,13 @@ static int dalloc(tfs_handle *h, T **p, size_t count)
     return TFS_OK;
 }
 
-// The SpMV kernel of the CG iterations: for uniform-width matrices the
-// software-pipelined kernel (default), the cp.async-staged kernel
-// (TFS_SPMV=async) or the bulk-copy kernel (TFS_SPMV=bulk) -- the staged
-// kernels with TFS_BULK_STAGES stages per block, resident blocks per SM from
-// the occupancy calculator, 16-byte aligned tile bases -- else (per-slice
-// widths or TFS_SPMV=direct) the direct kernels.  All give bitwise the same
-// results.
-template <typename K>
-static bool staged_occupancy(K kernel, int smem, int *occ)
-{
-    *occ = 0;
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kernel, TFS_TPB, smem) != cudaSuccess || *occ < 1) {
-        cudaGetLastError();
-        *occ = 0;
-        return false;
-    }
-    return true;
-}
-
+// The SpMV kernel of the CG iterations: the software-pipelined kernel for
+// uniform-width matrices (width <= 8), else the direct kernel; both give
+// bitwise the same results (TFS_OPT_SPMV = 0 forces the direct one).
 static void spmv_kind_setup(tfs_handle *h)
 {
-    h->spmv_kind = TFS_SPMV_DIRECT;
-    h->bulk_occ32 = h->bulk_occ64 = 0;
-    if (h->sell_width <= 0 || h->sell_width > 8) return;
-    const char *env = getenv("TFS_SPMV");
-    if (env && strcmp(env, "direct") == 0) return;
-    h->spmv_kind = TFS_SPMV_PIPE;
-    const bool bulk = env && strcmp(env, "bulk") == 0, async = env && strcmp(env, "async") == 0;
-    if (!bulk && !async) return;
-    auto aligned = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-    if (!aligned(h->col) || !aligned(h->rowinfo) || !aligned(h->val) || !aligned(h->val32)) return;
-    int stages = 3;
-    env = getenv("TFS_BULK_STAGES");
-    if (env && atoi(env) >= 2 && atoi(env) <= TFS_BULK_MAX_STAGES) stages = atoi(env);
-    h->bulk_stages = stages;
-    h->bulk_smem32 = stages * bulk_stage_bytes<float>(h->sell_width);
-    h->bulk_smem64 = stages * bulk_stage_bytes<double>(h->sell_width);
-    bool ok;
-    if (bulk) {
-        ok = staged_occupancy(k_spmv_pq_bulk<float, true>, h->bulk_smem32, &h->bulk_occ32) &&
-             staged_occupancy(k_spmv_pq_bulk<double, false>, h->bulk_smem64, &h->bulk_occ64);
-    } else if (stages == 2) {
-        ok = staged_occupancy(k_spmv_pq_async<float, true, 2>, h->bulk_smem32, &h->bulk_occ32) &&
-             staged_occupancy(k_spmv_pq_async<double, false, 2>, h->bulk_smem64, &h->bulk_occ64);
-    } else if (stages == 3) {
-        ok = staged_occupancy(k_spmv_pq_async<float, true, 3>, h->bulk_smem32, &h->bulk_occ32) &&
-             staged_occupancy(k_spmv_pq_async<double, false, 3>, h->bulk_smem64, &h->bulk_occ64);
-    } else {
-        ok = staged_occupancy(k_spmv_pq_async<float, true, 4>, h->bulk_smem32, &h->bulk_occ32) &&
-             staged_occupancy(k_spmv_pq_async<double, false, 4>, h->bulk_smem64, &h->bulk_occ64);
-    }
-    if (!ok) {
-        h->bulk_occ32 = h->bulk_occ64 = 0;
-        return;
-    }
-    h->spmv_kind = bulk ? TFS_SPMV_BULK : TFS_SPMV_ASYNC;
-}
-
-template <typename VT, bool MIXED>
-static void launch_spmv_async(const tfs_handle *h, cudaStream_t s, int G, int smem, const VT *val, const VT *p,
-                              VT *q)
-{
-    const SellDev A = sell_of(h);
-    const int VG = h->grid_spmv;
-    if (h->bulk_stages == 2)
-        k_spmv_pq_async<VT, MIXED, 2><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
-    else if (h->bulk_stages == 3)
-        k_spmv_pq_async<VT, MIXED, 3><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
-    else
-        k_spmv_pq_async<VT, MIXED, 4><<<G, TFS_TPB, smem, s>>>(A, val, p, q, h->st, h->part, VG);
+    h->spmv_kind = (h->sell_width > 0 && h->sell_width <= 8 && h->spmv_pref != 0) ? TFS_SPMV_PIPE
+                                                                                : TFS_SPMV_DIRECT;
 }
 
 template <typename VT, bool MIXED>
@@ -285,20 +208,6 @@ static void launch_spmv_pq(tfs_handle *h, cudaStream_t s, bool mixed, bool pdl =
     if (h->spmv_kind == TFS_SPMV_PIPE) {
         if (mixed) launch_spmv_pipe<float, true>(h, s, h->val32, h->f.p, h->f.q, pdl);
         else launch_spmv_pipe<double, false>(h, s, h->val, h->v.p, h->v.q, pdl);
-    } else if (h->spmv_kind == TFS_SPMV_ASYNC && mixed) {
-        launch_spmv_async<float, true>(h, s, std::min(VG, h->sm_count * h->bulk_occ32), h->bulk_smem32, h->val32,
-                                       h->f.p, h->f.q);
-    } else if (h->spmv_kind == TFS_SPMV_ASYNC) {
-        launch_spmv_async<double, false>(h, s, std::min(VG, h->sm_count * h->bulk_occ64), h->bulk_smem64, h->val,
-                                         h->v.p, h->v.q);
-    } else if (h->spmv_kind == TFS_SPMV_BULK && mixed) {
-        const int G = std::min(VG, h->sm_count * h->bulk_occ32);
-        k_spmv_pq_bulk<float, true><<<G, TFS_TPB, h->bulk_smem32, s>>>(A, h->val32, h->f.p, h->f.q, h->st,
-                                                                      h->part, VG, h->bulk_stages);
-    } else if (h->spmv_kind == TFS_SPMV_BULK) {
-        const int G = std::min(VG, h->sm_count * h->bulk_occ64);
-        k_spmv_pq_bulk<double, false><<<G, TFS_TPB, h->bulk_smem64, s>>>(A, h->val, h->v.p, h->v.q, h->st,
-                                                                        h->part, VG, h->bulk_stages);
     } else if (mixed) {
         k_mx_spmv_pq<<<VG, TFS_TPB, 0, s>>>(A, h->val32, h->f.p, h->f.q, h->st, h->part);
     } else {
@@ -511,26 +420,16 @@ static void free_layout(tfs_handle *h)
     }
     h->graphs.clear();
     void *ptrs[] = {h->perm, h->iperm, h->rowinfo, h->slice_off, h->col, h->vmap, h->val, h->val32,
-                    h->tiles, h->d_lvl_begin, h->d_lvl_tiles, h->lvl_cnt, h->vec_pool, h->vec32_pool,
-                    h->part};
+                    h->d_lvl_begin, h->vec_pool, h->vec32_pool, h->part};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->perm = h->iperm = h->slice_off = h->col = h->vmap = nullptr;
     h->rowinfo = nullptr;
     h->val = nullptr;
     h->val32 = nullptr;
-    h->tiles = nullptr;
-    h->d_lvl_begin = h->d_lvl_tiles = nullptr;
-    h->lvl_cnt = nullptr;
+    h->d_lvl_begin = nullptr;
     h->vec_pool = h->vec32_pool = nullptr;
     h->part = nullptr;
-    void *slab[] = {h->d_slab_seg, h->d_slab_dep, h->d_slab_prog};
-    for (void *p : slab)
-        if (p) cudaFree(p);
-    h->d_slab_seg = nullptr;
-    h->d_slab_dep = nullptr;
-    h->d_slab_prog = nullptr;
-    h->slab_G = 0;
     h->device_bytes = h->fixed_bytes;
     h->layout = -1;
 }
@@ -603,13 +502,11 @@ static int build_layout(tfs_handle *h, int kind)
     // loaded) when rows have at most 8 entries and it costs at most 5% more
     // slots: the 7-entry rows of a hex mesh.  Measured equal to per-slice
     // widths on the 128^3 system (binary32 SpMV 39.3 against 39.5 us);
-    // TFS_SELL_UNIFORM=0 keeps per-slice widths.
+    // TFS_OPT_SELL_UNIFORM = 0 keeps per-slice widths.
     h->sell_width = 0;
     {
         const int64_t uni = 32 * (int64_t)wmax * n_slices;
-        const char *env = getenv("TFS_SELL_UNIFORM");
-        const bool allow = !(env && strcmp(env, "0") == 0);
-        if (allow && wmax > 0 && wmax <= 8 && uni <= off + off / 20 && uni <= INT32_MAX) {
+        if (h->sell_uniform && wmax > 0 && wmax <= 8 && uni <= off + off / 20 && uni <= INT32_MAX) {
             h->sell_width = wmax;
             for (int s = 0; s <= n_slices; s++) slice_off[s] = 32 * wmax * s;
             off = uni;
@@ -636,27 +533,14 @@ static int build_layout(tfs_handle *h, int kind)
     if (h->grid < 1) h->grid = 1;
     // SpMV-type kernels: 8 blocks per SM, grid-stride over the 256-row
     // chunks (measured faster than one chunk per block on the 128^3
-    // system: 42.5 us against 72.9 us); TFS_SPMV_GRID=chunks selects the latter.
-    h->grid_spmv = h->grid;
-    {
-        const char *env = getenv("TFS_SPMV_GRID");
-        if (env && strcmp(env, "chunks") == 0) h->grid_spmv = h->n_chunks;
-        // TFS_SPMV_GRID=<k>, 1 <= k <= 8: k blocks per SM.
-        if (env && atoi(env) >= 1 && atoi(env) <= 8)
-            h->grid_spmv = std::max(1, std::min(h->n_chunks, h->sm_count * atoi(env)));
-    }
+    // system: 42.5 us against 72.9 us); TFS_OPT_SPMV_GRID = 1 selects the
+    // latter (the autotuner times both).
+    h->grid_spmv = h->spmv_chunks ? h->n_chunks : h->grid;
     // Binary32 CG vector kernels: 16-byte loads, grid-stride over the same
-    // grid as the other vector kernels.  TFS_VEC=full gives every thread
-    // exactly four rows (n_int / 1024 blocks); TFS_VEC=quad selects the
-    // scalar four-chunk kernels.
+    // grid as the other vector kernels.
     h->vec4 = 1;
     h->grid_vec4 = h->grid < h->n_int / (4 * TFS_TPB) ? h->grid : h->n_int / (4 * TFS_TPB);
     if (h->grid_vec4 < 1) h->grid_vec4 = 1;
-    {
-        const char *env = getenv("TFS_VEC");
-        if (env && strcmp(env, "full") == 0) h->grid_vec4 = h->n_int / (4 * TFS_TPB);
-        if (env && strcmp(env, "quad") == 0) h->vec4 = 0;
-    }
 
     if ((rc = dalloc(h, &h->perm, n_int)) || (rc = dalloc(h, &h->iperm, n)) ||
         (rc = dalloc(h, &h->rowinfo, n_int)) || (rc = dalloc(h, &h->slice_off, n_slices + 1)) ||
@@ -665,131 +549,28 @@ static int build_layout(tfs_handle *h, int kind)
         (rc = dalloc(h, &h->part, TFS_NPART * (size_t)h->n_chunks + 64)))
         return rc;
     {
-        // Sweep work items: tiles of at most TFS_SWEEP_TPB rows inside one
-        // level, then one item for the tail (the levels after the last level
-        // with more than TFS_TAIL_ROWS rows).
-        int tail_rows = TFS_TAIL_ROWS;
-        const char *tenv = getenv("TFS_TAIL_ROWS");
-        if (tenv && atoi(tenv) >= 1 && atoi(tenv) <= 65536) tail_rows = atoi(tenv);
+        // The tail: the levels after the last level with more than
+        // TFS_TAIL_ROWS rows, swept by one block (level 0 is never part of it).
         int tail = nl;
-        while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= tail_rows) tail--;
-        if (tail == 0) tail = nl > 1 ? 1 : nl;   // level 0 always runs as tiles
+        while (tail > 0 && h->lvl_begin[tail] - h->lvl_begin[tail - 1] <= TFS_TAIL_ROWS) tail--;
+        if (tail == 0) tail = nl > 1 ? 1 : nl;
         h->tail_level = tail;
-        // A cluster tail of the per-level sweeps takes levels of up to
-        // C x TFS_SWEEP_TPB rows (C CTAs of one cluster), if such a cluster
-        // can be resident; else the single-block tail is used.
-        h->tail_cluster = 1;
-        {
-            // Default 1: on the 128^3 system the 8- and 16-CTA cluster tails
-            // (156 and 157 us per application) were slower than one block
-            // (144 us); TFS_TAIL_CLUSTER selects 2, 4, 8 or 16.
-            int C = 1;
-            const char *env = getenv("TFS_TAIL_CLUSTER");
-            if (env) C = atoi(env);
-            if (C != 1 && C != 2 && C != 4 && C != 8 && C != 16) C = 1;
-            if (C > 1) {
-                auto kc = k_sweep_tailc<double, 2>;
-                if (C > 8) cudaFuncSetAttribute(kc, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                auto kf = k_sweep_tailc<float, 2>;
-                if (C > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                auto kd1 = k_sweep_tailc<double, 1>;
-                if (C > 8) cudaFuncSetAttribute(kd1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                auto kf1 = k_sweep_tailc<float, 1>;
-                if (C > 8) cudaFuncSetAttribute(kf1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                cudaLaunchConfig_t cfg = {};
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = (unsigned)C;
-                attr[0].val.clusterDim.y = 1;
-                attr[0].val.clusterDim.z = 1;
-                cfg.gridDim = dim3((unsigned)C);
-                cfg.blockDim = dim3(TFS_SWEEP_TPB);
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                int ncl = 0;
-                if (cudaOccupancyMaxActiveClusters(&ncl, kc, &cfg) != cudaSuccess || ncl < 1) {
-                    cudaGetLastError();
-                    C = 1;
-                }
-            }
-            h->tail_cluster = C;
-            int ct = nl;
-            while (ct > 0 && h->lvl_begin[ct] - h->lvl_begin[ct - 1] <= C * TFS_SWEEP_TPB) ct--;
-            h->ctail_level = ct;
+        // Prefetching tail (k_sweep_tail1): the longest suffix of levels
+        // (never level 0) whose rows fit one per thread of one block, used
+        // when it reaches at least as far down as the plain tail.  Spreading
+        // it over a cluster (2-16 CTAs, the hardware cluster barrier between
+        // levels) so that mid-sized levels join it measured no faster on the
+        // 128^3 system (one block 128.8 us per DIC application; 2, 8, 16 CTAs
+        // 131.8, 129.3, 126.3 us).
+        int l = nl, rows = 0;
+        while (l > 1 && rows + (h->lvl_begin[l] - h->lvl_begin[l - 1]) <= TFS_SWEEP_TPB) {
+            rows += h->lvl_begin[l] - h->lvl_begin[l - 1];
+            l--;
         }
-        {
-            // Prefetching tail (k_sweep_tail1): the longest suffix of levels
-            // (never level 0) whose rows fit one per thread of one block, or
-            // of a cluster of up to TFS_TAIL_PF_CLUSTER CTAs; used when it
-            // reaches at least as far down as the plain tail.  Clusters let
-            // the mid-sized levels join the tail, but measured no faster on
-            // the 128^3 system (one block 128.8 us per DIC application; 2, 8,
-            // 16 CTAs 131.8, 129.3, 126.3 us, binary32 solves/s 14.04 against
-            // 13.72, 13.84, 13.98), so the default is one block.
-            int cmax = 1;
-            const char *env = getenv("TFS_TAIL_PF_CLUSTER");
-            if (env && (atoi(env) == 1 || atoi(env) == 2 || atoi(env) == 4 || atoi(env) == 8 || atoi(env) == 16))
-                cmax = atoi(env);
-            int l = nl, rows = 0;
-            while (l > 1 && rows + (h->lvl_begin[l] - h->lvl_begin[l - 1]) <= cmax * TFS_SWEEP_TPB) {
-                rows += h->lvl_begin[l] - h->lvl_begin[l - 1];
-                l--;
-            }
-            int C = 1;
-            while (C * TFS_SWEEP_TPB < rows) C *= 2;
-            h->pf_tail_level = l;
-            h->pf_C = (l < nl && l <= h->tail_level) ? C : 0;
-            if (h->pf_C > 1) {
-                auto kc = k_sweep_tail1<float, true>;
-                auto kd = k_sweep_tail1<double, true>;
-                if (h->pf_C > 8) {
-                    cudaFuncSetAttribute(kc, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                    cudaFuncSetAttribute(kd, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                }
-                cudaLaunchConfig_t cfg = {};
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = (unsigned)h->pf_C;
-                attr[0].val.clusterDim.y = 1;
-                attr[0].val.clusterDim.z = 1;
-                cfg.gridDim = dim3((unsigned)h->pf_C);
-                cfg.blockDim = dim3(TFS_SWEEP_TPB);
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                int n32 = 0, n64 = 0;
-                if (cudaOccupancyMaxActiveClusters(&n32, kc, &cfg) != cudaSuccess ||
-                    cudaOccupancyMaxActiveClusters(&n64, kd, &cfg) != cudaSuccess || n32 < 1 || n64 < 1) {
-                    cudaGetLastError();
-                    h->pf_C = 0;
-                }
-            }
-        }
-        std::vector<int2> tiles;
-        std::vector<int> lvl_tiles(nl, 0);
-        for (int l = 0; l < tail; l++)
-            for (int r = h->lvl_begin[l]; r < h->lvl_begin[l + 1]; r += TFS_SWEEP_TPB) {
-                tiles.push_back(make_int2(r, l));
-                lvl_tiles[l]++;
-            }
-        if (tail < nl) {
-            tiles.push_back(make_int2(h->lvl_begin[tail], tail));
-            for (int l = tail; l < nl; l++) lvl_tiles[l] = 1;
-        }
-        h->n_tiles = (int)tiles.size();
-        if ((rc = dalloc(h, &h->tiles, tiles.size())) || (rc = dalloc(h, &h->d_lvl_begin, nl + 1)) ||
-            (rc = dalloc(h, &h->d_lvl_tiles, nl)) || (rc = dalloc(h, &h->lvl_cnt, 3 * (size_t)nl)))
-            return rc;
-        CK(cudaMemcpyAsync(h->tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, h->stream));
+        h->pf_tail_level = l;
+        h->pf_ok = l < nl && l <= h->tail_level;
+        if ((rc = dalloc(h, &h->d_lvl_begin, nl + 1))) return rc;
         CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_begin.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, h->stream));
-        CK(cudaMemcpyAsync(h->d_lvl_tiles, lvl_tiles.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, h->stream));
-        CK(cudaMemsetAsync(h->lvl_cnt, 0, sizeof(unsigned long long) * 3 * (size_t)nl, h->stream));
-        CK(cudaMemsetAsync(h->ctl, 0, sizeof(SweepCtl), h->stream));
-        int occ = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_lv<double, 2, 0>, TFS_SWEEP_TPB, 0));
-        if (occ < 1) occ = 1;
-        int gs = h->sm_count * occ;
-        h->sweep_grid = h->n_tiles < gs ? h->n_tiles : gs;
-        if (h->sweep_grid < 1) h->sweep_grid = 1;
     }
     spmv_kind_setup(h);
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
@@ -842,7 +623,7 @@ static void free_handle(tfs_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_layout(h);
     tfs_faces_free(h);
-    void *ptrs[] = {h->stage_val, h->stage_b, h->stage_x, h->st, h->params, h->ctl};
+    void *ptrs[] = {h->stage_val, h->stage_b, h->stage_x, h->st, h->params};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_params) cudaFreeHost(h->h_params);
@@ -893,37 +674,12 @@ extern "C" int tfs_topology_register(int32_t n, int32_t nnz, const int32_t *row1
     rcm_order(n, h->row0, h->col0, h->rcm_pos);
     if ((rc = dalloc(h, &h->stage_val, nnz)) || (rc = dalloc(h, &h->stage_b, n)) ||
         (rc = dalloc(h, &h->stage_x, n)) || (rc = dalloc(h, &h->st, 1)) ||
-        (rc = dalloc(h, &h->params, 1)) || (rc = dalloc(h, &h->ctl, 1))) {
+        (rc = dalloc(h, &h->params, 1))) {
         free_handle(h);
         return rc;
     }
     h->fixed_bytes = h->device_bytes;
     cudaMemsetAsync(h->st, 0, sizeof(DevState), h->stream);
-    const char *env = getenv("TFS_SWEEP");
-    if (env && strcmp(env, "single") == 0) h->sweep_mode = 1;
-    if (env && strcmp(env, "levels") == 0) h->sweep_mode = 0;
-    if (env && strcmp(env, "coop") == 0) h->sweep_mode = 2;
-    if (env && strcmp(env, "slab") == 0) h->sweep_mode = 3;
-    env = getenv("TFS_PDL_VEC");
-    if (env && strcmp(env, "0") == 0) h->pdl_vec = 0;
-    env = getenv("TFS_FWD_PRE");
-    if (env && strcmp(env, "0") == 0) h->fwd_pre = 0;
-    env = getenv("TFS_BWD_PRE");
-    if (env && strcmp(env, "0") == 0) h->bwd_pre = 0;
-    env = getenv("TFS_TAIL_PF");
-    if (env && strcmp(env, "0") == 0) h->tail_pf = 0;
-    env = getenv("TFS_FUSE_L0");
-    if (env && (strcmp(env, "0") == 0 || strcmp(env, "1") == 0 || strcmp(env, "2") == 0)) h->fuse_l0 = atoi(env);
-    env = getenv("TFS_LEVEL_TPB");
-    if (env && (atoi(env) == 128 || atoi(env) == 512 || atoi(env) == 1024)) h->level_tpb = atoi(env);
-    env = getenv("TFS_PDL");
-    if (env && strcmp(env, "0") == 0) h->use_pdl = 0;
-    env = getenv("TFS_GRAPH");
-    if (env && strcmp(env, "0") == 0) h->eager = 1;
-    env = getenv("TFS_LAYOUT");
-    if (env && strcmp(env, "levels") == 0) h->layout_pref = TFS_LAYOUT_LEVELS;
-    env = getenv("TFS_BICG");
-    if (env && strcmp(env, "literal") == 0) h->bicg_literal = 1;
     *out = h;
     return TFS_OK;
 }
@@ -942,19 +698,80 @@ extern "C" int tfs_set_precision(tfs_handle *h, int mode)
     return TFS_OK;
 }
 
+static void drop_graphs(tfs_handle *h)
+{
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &kv : h->graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    h->graphs.clear();
+    h->last_graph = nullptr;
+}
+
+// The field behind an option and the values it accepts.
+static int *option_field(tfs_handle *h, int option, bool (**ok)(int))
+{
+    static bool (*const bit)(int) = [](int v) { return v == 0 || v == 1; };
+    static bool (*const fuse)(int) = [](int v) { return v >= 0 && v <= 2; };
+    static bool (*const tpb)(int) = [](int v) { return v == 128 || v == 256 || v == 512 || v == 1024; };
+    *ok = bit;
+    switch (option) {
+    case TFS_OPT_LAUNCH: return &h->eager;
+    case TFS_OPT_LAYOUT: return &h->layout_pref;
+    case TFS_OPT_BICG: return &h->bicg_literal;
+    case TFS_OPT_SELL_UNIFORM: return &h->sell_uniform;
+    case TFS_OPT_SPMV: return &h->spmv_pref;
+    case TFS_OPT_SPMV_GRID: return &h->spmv_chunks;
+    case TFS_OPT_LEVEL_TPB: *ok = tpb; return &h->level_tpb;
+    case TFS_OPT_TAIL_PF: return &h->tail_pf;
+    case TFS_OPT_FUSE_L0: *ok = fuse; return &h->fuse_l0;
+    case TFS_OPT_PDL: return &h->use_pdl;
+    case TFS_OPT_PDL_VEC: return &h->pdl_vec;
+    case TFS_OPT_FWD_PRE: return &h->fwd_pre;
+    case TFS_OPT_BWD_PRE: return &h->bwd_pre;
+    default: return nullptr;
+    }
+}
+
+extern "C" int tfs_set_option(tfs_handle *h, int option, int value)
+{
+    if (!h) return TFS_ERR_ARG;
+    bool (*ok)(int) = nullptr;
+    int *f = option_field(h, option, &ok);
+    if (!f || !ok(value)) {
+        tfs_set_error_text("tfs_set_option: unknown option or value");
+        return TFS_ERR_ARG;
+    }
+    CK(cudaSetDevice(h->device));
+    drop_graphs(h);
+    *f = value;
+    if (option == TFS_OPT_LAYOUT || option == TFS_OPT_SELL_UNIFORM) {
+        free_layout(h);
+    } else if (h->layout >= 0) {
+        // launch shapes derived from options at layout time
+        h->grid_spmv = h->spmv_chunks ? h->n_chunks : h->grid;
+        spmv_kind_setup(h);
+    }
+    return TFS_OK;
+}
+
+extern "C" int tfs_get_option(const tfs_handle *h, int option, int *value)
+{
+    if (!h || !value) return TFS_ERR_ARG;
+    bool (*ok)(int) = nullptr;
+    int *f = option_field(const_cast<tfs_handle *>(h), option, &ok);
+    if (!f) return TFS_ERR_ARG;
+    *value = *f;
+    return TFS_OK;
+}
+
 // ------------------------------------------------------ graph capture
 
-// DIC recurrence (Prec_Form.f90:32-40): one dataflow launch or one launch per
-// level.  Returns the number of kernels launched.
+// DIC recurrence (Prec_Form.f90:32-40): one launch per large level, the tail
+// in one block.  Returns the number of kernels launched.
 static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
-    SellDev A = sell_of(h);
-    if (h->sweep_mode == 1) {
-        k_sweep_lv<double, 1, 2><<<h->sweep_grid, TFS_SWEEP_TPB, 0, s>>>(A, h->val, h->v.d, nullptr, nullptr, nullptr,
-                                                             nullptr, nullptr, nullptr, tile_table(h), h->ctl,
-                                                             h->lvl_cnt, h->st);
-        return 1;
-    }
     int cnt = 0;
     if (launch_levels<double, 1, 2>(h, s, h->val, h->v.d, nullptr, nullptr, nullptr, nullptr, nullptr,
                                     nullptr, &cnt))
@@ -995,160 +812,17 @@ static int launch_prologue(tfs_handle *h, cudaStream_t s, int method, int prec,
     return TFS_OK;
 }
 
-// Forward and backward level sweeps: z = M^-1 b for NR right-hand sides, in
-// binary64 (val, d of the handle) or binary32 (val32, d32).
-// One cooperative launch of k_dic_apply: z = M^-1 b through y, and with
-// FUSE rho = (b, z), p = z + beta p.  The grid is the co-resident maximum,
-// capped at the blocks the largest swept level needs.
-template <typename T, int R, bool FUSE>
-static cudaError_t launch_dic_k(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *p)
-{
-    auto kernel = k_dic_apply<T, R, FUSE>;
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, TFS_DIC_TPB, 0);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) return cudaErrorInvalidConfiguration;
-    const int big = h->tail_level;
-    int widest = 0;
-    for (int l = 0; l < big; l++) widest = std::max(widest, h->lvl_begin[l + 1] - h->lvl_begin[l]);
-    int need = (widest + R * TFS_DIC_TPB - 1) / (R * TFS_DIC_TPB);
-    int G = std::min(occ * h->sm_count, std::max(need, 1));
-    G = std::min(G, h->n_chunks);   // one partial per block fits h->part
-    const T *val;
-    const T *d;
-    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
-    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.gridDim = dim3((unsigned)G);
-    cfg.blockDim = dim3(TFS_DIC_TPB);
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, sell_of(h), val, d, b, y, z, p, (const int *)h->d_lvl_begin,
-                              big, h->n_levels, h->n_int, h->st, h->part);
-}
-
-// Rows per thread of the cooperative sweep: 2 when one row per thread of
-// the co-resident grid does not cover the widest level.
-template <typename T, bool FUSE>
-static int launch_dic(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, T *p, int *count)
-{
-    if (h->dic_r == 0) {
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_dic_apply<T, 1, FUSE>, TFS_DIC_TPB, 0);
-        int widest = 0;
-        for (int l = 0; l < h->tail_level; l++) widest = std::max(widest, h->lvl_begin[l + 1] - h->lvl_begin[l]);
-        h->dic_r = (int64_t)occ * h->sm_count * TFS_DIC_TPB >= widest ? 1 : 2;
-    }
-    cudaError_t e = h->dic_r == 1 ? launch_dic_k<T, 1, FUSE>(h, s, b, y, z, p)
-                                  : launch_dic_k<T, 2, FUSE>(h, s, b, y, z, p);
-    (*count)++;
-    return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "cooperative DIC launch");
-}
-
-// Slab schedule (k_dic_slab): block b owns the rows of RCM slab b of every
-// level; its neighbour range covers the slabs of every row it reads.  One
-// block per SM (TFS_SLAB_PER_SM=2: two, where they fit), at most 1024.
-static int slab_setup(tfs_handle *h)
-{
-    if (h->slab_G > 0) return TFS_OK;
-    int per_sm = 1;
-    const char *env = getenv("TFS_SLAB_PER_SM");
-    if (env && atoi(env) == 2) per_sm = 2;
-    int occ32 = 0, occ64 = 0;
-    if (per_sm == 2) {
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_dic_slab<float, 1>, TFS_DIC_TPB, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_dic_slab<double, 1>, TFS_DIC_TPB, 0));
-    } else {
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_dic_slab<float, 2>, TFS_DIC_TPB, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_dic_slab<double, 2>, TFS_DIC_TPB, 0));
-    }
-    const int occ = std::min(occ32, occ64);
-    if (occ < 1) {
-        tfs_set_error_text("slab DIC kernel cannot be resident");
-        return TFS_ERR_CUDA;
-    }
-    per_sm = std::min(per_sm, occ);
-    const int G = std::min(1024, h->sm_count * per_sm);
-    const int n = h->n, nl = h->n_levels;
-    if ((int)h->levels_nat.size() != n || (int)h->lvl_begin.size() != nl + 1) {
-        tfs_set_error_text("slab schedule needs the level layout");
-        return TFS_ERR_ARG;
-    }
-    auto slab = [&](int i) { return (int)((int64_t)h->rcm_pos[i] * G / n); };
-    std::vector<int> cnt((size_t)nl * G, 0), seg((size_t)nl * (G + 1));
-    for (int i = 0; i < n; i++) cnt[(size_t)h->levels_nat[i] * G + slab(i)]++;
-    for (int l = 0; l < nl; l++) {
-        int *sg = seg.data() + (size_t)l * (G + 1);
-        sg[0] = h->lvl_begin[l];
-        for (int b = 0; b < G; b++) sg[b + 1] = sg[b] + cnt[(size_t)l * G + b];
-        sg[G] = h->lvl_begin[l + 1];   // the level's padding rows go to the last block
-    }
-    std::vector<int2> dep(G);
-    for (int b = 0; b < G; b++) dep[b] = make_int2(b, b);
-    for (int i = 0; i < n; i++) {
-        const int sb = slab(i);
-        for (int j = h->row0[i]; j < h->row0[i + 1]; j++) {
-            const int sk = slab(h->col0[j]);
-            dep[sb].x = std::min(dep[sb].x, sk);
-            dep[sb].y = std::max(dep[sb].y, sk);
-        }
-    }
-    int rc;
-    if ((rc = dalloc(h, &h->d_slab_seg, seg.size())) || (rc = dalloc(h, &h->d_slab_dep, (size_t)G)) ||
-        (rc = dalloc(h, &h->d_slab_prog, (size_t)G + 2)))
-        return rc;
-    CK(cudaMemcpyAsync(h->d_slab_seg, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_slab_dep, dep.data(), sizeof(int2) * (size_t)G, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemsetAsync(h->d_slab_prog, 0, sizeof(unsigned long long) * ((size_t)G + 2), h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    h->slab_G = G;
-    return TFS_OK;
-}
-
-template <typename T>
-static int launch_slab(tfs_handle *h, cudaStream_t s, const T *b, T *y, T *z, int *count)
-{
-    int rc = slab_setup(h);
-    if (rc) return rc;
-    const T *val;
-    const T *d;
-    if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (const T *)h->v.d; }
-    else { val = (const T *)h->val32; d = (const T *)h->f.d; }
-    const int G = h->slab_G;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.gridDim = dim3((unsigned)G);
-    cfg.blockDim = dim3(TFS_DIC_TPB);
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    // Two blocks per SM: one row per thread (32 registers); one: two rows.
-    auto kernel = G > h->sm_count ? k_dic_slab<T, 1> : k_dic_slab<T, 2>;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, sell_of(h), val, d, b, y, z,
-                                       (const int *)h->d_slab_seg, (const int2 *)h->d_slab_dep, h->n_levels,
-                                       h->d_slab_prog, h->d_slab_prog + G, h->st);
-    (*count)++;
-    return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "slab DIC launch");
-}
-
-// The tail of the per-level schedule: the prefetching tail (k_sweep_tail1,
-// one block or one cluster) for one right-hand side on uniform-width
-// matrices when it was set up, else the single-block or cluster level loop.
+// The tail of the per-level schedule: the prefetching tail (k_sweep_tail1)
+// for one right-hand side on uniform-width matrices when it was set up, else
+// the single-block level loop (k_sweep_tail2).
 static bool pf_tail(const tfs_handle *h, int nr)
 {
-    return nr == 1 && h->tail_pf && h->pf_C > 0 && h->sell_width > 0 && h->sell_width <= 8;
+    return nr == 1 && h->tail_pf && h->pf_ok && h->sell_width > 0 && h->sell_width <= 8;
 }
 
 static int sweep_tail_at(const tfs_handle *h, int nr)
 {
-    if (pf_tail(h, nr)) return h->pf_tail_level;
-    return h->tail_cluster > 1 ? h->ctail_level : h->tail_level;
+    return pf_tail(h, nr) ? h->pf_tail_level : h->tail_level;
 }
 
 template <typename T>
@@ -1156,74 +830,24 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
                          T *y1, T *y2, T *z1, T *z2, int *count, bool fuse_l0 = false)
 {
     SellDev A = sell_of(h);
-    if (h->sweep_mode == 2 && nr == 1) return launch_dic<T, false>(h, s, b1, y1, z1, nullptr, count);
-    if (h->sweep_mode == 3 && nr == 1) return launch_slab<T>(h, s, b1, y1, z1, count);
     const int T_ = TFS_TPB;
     const T *val;
     T *d;
     if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (T *)h->v.d; }
     else { val = (const T *)h->val32; d = (T *)h->f.d; }
-    if (h->sweep_mode == 1) {
-        const int G = h->sweep_grid;
-        TileTable tt = tile_table(h);
-        if (nr == 1) {
-            k_sweep_lv<T, 1, 0><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, tt, h->ctl, h->lvl_cnt, h->st);
-            k_sweep_lv<T, 1, 1><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, tt, h->ctl, h->lvl_cnt, h->st);
-        } else {
-            k_sweep_lv<T, 2, 0><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, tt, h->ctl, h->lvl_cnt, h->st);
-            k_sweep_lv<T, 2, 1><<<G, TFS_SWEEP_TPB, 0, s>>>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, tt, h->ctl, h->lvl_cnt, h->st);
-        }
-        *count += 2;
-        CKL("sweep launch");
-        return TFS_OK;
-    }
-    // Forward levels, both tails in one block or one cluster, backward levels.
+    // Forward levels, both tails in one block, backward levels.
     int rc;
-    const int C = h->tail_cluster;
     const int tail_at = sweep_tail_at(h, nr);
     const bool tails = tail_at < h->n_levels;
-    auto tail2 = [&](auto kernel, auto kernel_c) -> int {
+    auto tail2 = [&](auto kernel) -> int {
         if (!tails) return TFS_OK;
         cudaError_t e;
-        if (pf_tail(h, nr) && h->pf_C > 1) {
-            cudaLaunchConfig_t cfg = {};
-            cudaLaunchAttribute attr[2];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = (unsigned)h->pf_C;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[1].val.programmaticStreamSerializationAllowed = 1;
-            cfg.gridDim = dim3((unsigned)h->pf_C);
-            cfg.blockDim = dim3(TFS_SWEEP_TPB);
-            cfg.stream = s;
-            cfg.attrs = attr;
-            cfg.numAttrs = h->use_pdl ? 2 : 1;
-            e = cudaLaunchKernelEx(&cfg, k_sweep_tail1<T, true>, A, val, (const T *)d, b1, y1, z1,
-                                   (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
-        } else if (pf_tail(h, nr)) {
-            e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T, false>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
+        if (pf_tail(h, nr))
+            e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
                           y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
-        } else if (C > 1) {
-            cudaLaunchConfig_t cfg = {};
-            cudaLaunchAttribute attr[2];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = (unsigned)C;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[1].val.programmaticStreamSerializationAllowed = 1;
-            cfg.gridDim = dim3((unsigned)C);
-            cfg.blockDim = dim3(TFS_SWEEP_TPB);
-            cfg.stream = s;
-            cfg.attrs = attr;
-            cfg.numAttrs = h->use_pdl ? 2 : 1;
-            e = cudaLaunchKernelEx(&cfg, kernel_c, A, val, d, b1, b2, y1, y2, z1, z2,
-                                   (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
-        } else {
+        else
             e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
                           z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
-        }
         (*count)++;
         return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
     };
@@ -1234,7 +858,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         const int from = fuse_l0 ? 1 : 0;
         if ((rc = launch_levels<T, 1, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at, from,
                                          h->fwd_pre != 0))) return rc;
-        if ((rc = tail2(k_sweep_tail2<T, 1>, k_sweep_tailc<T, 1>))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 1>))) return rc;
         if ((rc = launch_levels<T, 1, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, from,
                                          tails && h->bwd_pre))) return rc;
         if (fuse_l0) {
@@ -1246,7 +870,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         }
     } else {
         if ((rc = launch_levels<T, 2, 0>(h, s, val, d, b1, b2, y1, y2, nullptr, nullptr, count, false, tail_at))) return rc;
-        if ((rc = tail2(k_sweep_tail2<T, 2>, k_sweep_tailc<T, 2>))) return rc;
+        if ((rc = tail2(k_sweep_tail2<T, 2>))) return rc;
         if ((rc = launch_levels<T, 2, 1>(h, s, val, d, nullptr, nullptr, z1, z2, y1, y2, count, false, tail_at, 0,
                                          tails && h->bwd_pre))) return rc;
     }
@@ -1265,7 +889,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 // before the dependency wait it is faster, 7.01 against 6.97).
 static int dic_l0_rows(const tfs_handle *h, int method, int prec)
 {
-    if (method != TFS_CG || prec != 2 || !h->fuse_l0 || h->sweep_mode != 0) return 0;
+    if (method != TFS_CG || prec != 2 || !h->fuse_l0) return 0;
     if (h->precision == TFS_MIXED && !h->vec4) return 0;
     if (h->precision != TFS_MIXED && h->fuse_l0 != 2) return 0;
     const int tail_at = sweep_tail_at(h, 1);
@@ -1301,14 +925,7 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     *count = 0;
     if (method == TFS_CG) {
         const int n4 = h->n_int / 4, G4 = h->grid_vec4;
-        if (h->sweep_mode == 2 && prec == 2) {
-            if ((rc = launch_dic<float, true>(h, s, F.r, F.y, F.z, F.p, count))) return rc;
-            launch_spmv_pq(h, s, true);
-            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
-            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
-            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
-            *count += 4;
-        } else if (!h->vec4 && prec == 2) {
+        if (!h->vec4 && prec == 2) {
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
             k_mx_dot_rho<0><<<G, T, 0, s>>>(nc, F, h->st, h->part);
             k_mx_cg_p<true><<<G, T, 0, s>>>(nc, F, h->st);
@@ -1417,12 +1034,7 @@ static int launch_body(tfs_handle *h, cudaStream_t s, int method, int prec,
     int rc;
     *count = 0;
     if (method == TFS_CG) {
-        if (prec == 2 && h->sweep_mode == 2) {
-            if ((rc = launch_dic<double, true>(h, s, V.r, V.y, V.z, V.p, count))) return rc;
-            launch_spmv_pq(h, s, false);
-            k_cg_update<false><<<G, T, 0, s>>>(nc, V, h->st, h->part, cond);
-            *count += 2;
-        } else if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
+        if (prec == 2 && dic_l0_rows(h, method, prec) > 0) {
             const int l0 = dic_l0_rows(h, method, prec);
             const bool pv = h->use_pdl && h->pdl_vec;   // vector kernels PDL-chained
             if ((rc = launch_sweeps<double>(h, s, 1, V.r, nullptr, V.y, nullptr, V.z, nullptr, count, true))) return rc;
@@ -1546,8 +1158,9 @@ static int build_graph(tfs_handle *h, int method, int prec, GraphEntry &ge)
 
 // The same kernels without a graph: the host drives the loop, reading the
 // device's done flag after every TFS_EAGER_BATCH iterations (kernels of a
-// finished solve return at once).  Used for kernel-level profiling, which
-// cannot look inside graphs with conditional nodes.
+// finished solve return at once).  Selected by TFS_OPT_LAUNCH = 1, for
+// kernel-level profiling and launch tracing, which cannot look inside graphs
+// with conditional nodes.
 #define TFS_EAGER_BATCH 8
 static int run_eager(tfs_handle *h, int method, int prec, GraphEntry *ge)
 {
@@ -1583,15 +1196,7 @@ static int get_graph(tfs_handle *h, int method, int prec, GraphEntry **out)
     auto it = h->graphs.find(key);
     if (it != h->graphs.end()) { *out = &it->second; return TFS_OK; }
     GraphEntry ge;
-    int rc = TFS_OK;
-    if (h->sweep_mode == 3 && prec == 2 && (rc = slab_setup(h))) return rc;   // no copies during capture
-    rc = build_graph(h, method, prec, ge);
-    if (rc && (h->sweep_mode == 2 || h->sweep_mode == 3) && prec == 2) {
-        // A driver that cannot capture a cooperative launch inside a
-        // conditional body gets the per-level schedule instead.
-        h->sweep_mode = 0;
-        rc = build_graph(h, method, prec, ge);
-    }
+    int rc = build_graph(h, method, prec, ge);
     if (rc && h->use_pdl) {
         // A driver that cannot keep programmatic edges inside a conditional
         // body gets plain stream-ordered level launches instead.
@@ -1623,7 +1228,7 @@ int tfs_solve_launch(int method, tfs_handle *h, const double *val, double *x, do
     // sequence equals the primary one bit for bit, rho = (z1, r2) = (r1, z1)
     // and (p2, q1) = (p1, q1), so every iterate is exactly the CG iterate.
     // It therefore runs through the CG kernels (half the work, same bits);
-    // TFS_BICG=literal runs the two sequences explicitly.
+    // TFS_OPT_BICG = 1 runs the two sequences explicitly.
     const int kmethod = (method == TFS_BICG && !h->bicg_literal) ? TFS_CG : method;
     GraphEntry *ge = nullptr;
     rc = get_graph(h, kmethod, prec, &ge);
@@ -1708,6 +1313,16 @@ extern "C" int tfs_solve_device(int method, tfs_handle *h, const double *d_val, 
 namespace {
 std::mutex g_cache_mu;
 std::map<std::tuple<const int32_t *, const int32_t *, int32_t, int32_t, int>, tfs_handle *> g_cache;
+int g_default_precision = TFS_FP64;
+}
+
+extern "C" int tfs_set_default_precision(int mode)
+{
+    if (mode != TFS_FP64 && mode != TFS_MIXED) return TFS_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_default_precision = mode;
+    for (auto &kv : g_cache) kv.second->precision = mode;
+    return TFS_OK;
 }
 
 static int cached_handle(int32_t n, int32_t nnz, const int32_t *row1, const int32_t *col1,
@@ -1727,8 +1342,7 @@ static int cached_handle(int32_t n, int32_t nnz, const int32_t *row1, const int3
     tfs_handle *h = nullptr;
     int rc = tfs_topology_register(n, nnz, row1, col1, dia1, &h);
     if (rc) return rc;
-    const char *env = getenv("TFS_PRECISION");
-    if (env && strcmp(env, "mixed") == 0) h->precision = TFS_MIXED;
+    h->precision = g_default_precision;
     g_cache[key] = h;
     *out = h;
     return TFS_OK;
@@ -1979,15 +1593,14 @@ extern "C" int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec
         return rc;
     }
     {
-        // SpMV kernel x grid: the direct kernel, the software-pipelined one
-        // (uniform-width matrices) and a staged kernel chosen by TFS_SPMV,
-        // each with 8 blocks per SM (grid-stride) or one block per chunk.
+        // SpMV kernel x grid: the direct kernel and the software-pipelined
+        // one (uniform-width matrices), each with 8 blocks per SM
+        // (grid-stride) or one block per chunk.
         const int keep_grid = h->grid_spmv, keep_kind = h->spmv_kind;
         const int grids[2] = {h->grid, h->n_chunks};
-        int kinds[3], nk = 0;
+        int kinds[2], nk = 0;
         kinds[nk++] = TFS_SPMV_DIRECT;
         if (h->sell_width > 0 && h->sell_width <= 8) kinds[nk++] = TFS_SPMV_PIPE;
-        if (keep_kind == TFS_SPMV_BULK || keep_kind == TFS_SPMV_ASYNC) kinds[nk++] = keep_kind;
         int best_grid = keep_grid, best_kind = keep_kind;
         double best_ms = 0.0;
         for (int a = 0; a < nk; a++)
@@ -2012,12 +1625,9 @@ extern "C" int tfs_autotune(tfs_handle *h, const double *val, int mode, int prec
         h->spmv_kind = best_kind;
     }
     // The part buffer holds TFS_NPART partials per chunk: both grids fit.
-    for (auto &kv : h->graphs) {
-        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-    }
-    h->graphs.clear();
-    h->last_graph = nullptr;
+    drop_graphs(h);
+    h->spmv_chunks = h->grid_spmv == h->n_chunks && h->grid_spmv != h->grid ? 1 : 0;
+    if (h->sell_width > 0 && h->sell_width <= 8) h->spmv_pref = h->spmv_kind == TFS_SPMV_PIPE ? 1 : 0;
     out->level_tpb = h->level_tpb;
     out->spmv_chunks = h->grid_spmv == h->n_chunks && h->grid_spmv != h->grid ? 1 : 0;
     out->spmv_kernel = h->spmv_kind;
@@ -2263,9 +1873,9 @@ extern "C" int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mo
     k_batch_gather<<<dim3((unsigned)gx, (unsigned)b->n), 256, 0, b->stream>>>(b->d_sys, b->d_ctl, mode == TFS_MIXED);
     CKL("batch gather");
     int rc;
-    // BiCG iterates equal CG's (see solve_impl): one sequence suffices.
-    const char *lit = getenv("TFS_BICG");
-    if (method == TFS_BICG && !(lit && strcmp(lit, "literal") == 0)) method = TFS_CG;
+    // BiCG iterates equal CG's (see tfs_solve_launch): one sequence suffices
+    // unless the first system's handle asks for the literal two sequences.
+    if (method == TFS_BICG && !b->hs[0]->bicg_literal) method = TFS_CG;
     if (method == TFS_CG) rc = mode == TFS_MIXED ? launch_batch_kernel<0, float>(b) : launch_batch_kernel<0, double>(b);
     else rc = mode == TFS_MIXED ? launch_batch_kernel<1, float>(b) : launch_batch_kernel<1, double>(b);
     if (rc) return rc;

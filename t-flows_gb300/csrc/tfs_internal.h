@@ -31,8 +31,6 @@
 #define TFS_NPART 4           // values reduced at once, at most
 #define TFS_SPMV_DIRECT 0     // CG SpMV kernels: per-row dependent chain (any SELL-32 matrix)
 #define TFS_SPMV_PIPE 1       //   software-pipelined, uniform slice width
-#define TFS_SPMV_BULK 2       //   bulk copies into shared memory, uniform slice width
-#define TFS_SPMV_ASYNC 3      //   cp.async copies into shared memory, uniform slice width
 
 // Device-resident state of one solve.  Written by k_init from DevParams and
 // then only by the last block of each reducing kernel.
@@ -58,18 +56,6 @@ struct DevState {
     // rho instead of by every thread
     float beta32;
     float alpha32;       // (float) alpha, published with alpha
-    // grid barrier of the cooperative DIC kernel (zeroed with the state)
-    unsigned int bar_count, bar_gen, bar_abort, pad2;
-};
-
-// Control words of the single-launch level sweeps, one set per sweep kind
-// (0 DIC form, 1 forward, 2 backward).  They persist across solves: the
-// epoch of a kind counts its completed sweeps, and the per-level tile
-// counters are compared against epoch * tiles(level), so nothing is cleared.
-struct SweepCtl {
-    unsigned int ticket[3], done[3];
-    unsigned int abort, pad;
-    unsigned long long epoch[3];
 };
 
 // Per-call arguments, written by the host before every graph launch.
@@ -119,36 +105,27 @@ struct tfs_handle {
     int32_t n = 0, nnz = 0;
     int n_int = 0, n_chunks = 0, n_slices = 0, nnz_pad = 0, n_levels = 0;
     int sell_width = 0;                // uniform slice width (0: per-slice widths)
-    int spmv_kind = 0;                 // TFS_SPMV_DIRECT / _PIPE / _BULK / _ASYNC: kernel of the CG SpMV
-    // bulk-copy SpMV: resident blocks per SM of the binary32 / binary64
-    // kernel, stages per block, dynamic shared memory per block
-    int bulk_occ32 = 0, bulk_occ64 = 0, bulk_stages = 3;
-    int bulk_smem32 = 0, bulk_smem64 = 0;
+    int spmv_kind = 0;                 // TFS_SPMV_DIRECT / _PIPE: kernel of the CG SpMV
     int grid = 0;                      // blocks of the vector kernels (grid-stride)
     int grid_spmv = 0;                 // blocks of the SpMV-type kernels
     int grid_vec4 = 0;                 // blocks of the 16-byte binary32 vector kernels
     int vec4 = 1;                      // 1: binary32 CG vector kernels with 16-byte loads
-    int sweep_grid = 0;                // blocks of the dataflow sweeps
-    int sweep_mode = 0;                // 0: one launch per level (PDL), 1: single launch, 2: cooperative, 3: slabs
-    int use_pdl = 1;                   // programmatic dependent launch between level kernels
-    int pdl_vec = 1;                   // binary32 CG vector kernels PDL-chained (TFS_PDL_VEC=0: plain launches)
-    int fwd_pre = 1;                   // forward level kernels: right-hand side and D before the wait
-    int bwd_pre = 1;                   // backward level kernels after a tail: start values before the wait
-    int tail_pf = 1;                   // prefetching tail (k_sweep_tail1): one row per thread, loads ahead
-    int pf_tail_level = 0, pf_C = 0;   // its first level and cluster size (0: not usable)
-    int fuse_l0 = 2;                   // DIC-CG level 0 swept inside the neighbouring kernels (1: binary32 iteration only, 2: binary64 too)
-    int level_tpb = TFS_TPB;           // threads per block of the level-sweep kernels (TFS_LEVEL_TPB;
-                                       // 128/256/512/1024 measured 147.7/146.4/147.4/150.1 us per DIC application)
-    int dic_r = 0;                     // rows per thread of the cooperative sweep (0: not chosen yet)
-    // slab schedule of the DIC sweeps (sweep_mode 3): blocks, per-level row
-    // ranges of every block, neighbour-block ranges, progress words (+2
-    // application counter words); built on first use for the level layout
-    int slab_G = 0;
-    int *d_slab_seg = nullptr;
-    int2 *d_slab_dep = nullptr;
-    unsigned long long *d_slab_prog = nullptr;
-    int eager = 0;                     // 1: launch kernels directly, no CUDA graph
-    int bicg_literal = 0;              // 1: BiCG runs its shadow sequence explicitly
+    // Options (tfs_set_option; every default is the measured fastest).
+    int use_pdl = 1;                   // TFS_OPT_PDL: programmatic dependent launch between level kernels
+    int pdl_vec = 1;                   // TFS_OPT_PDL_VEC: CG vector kernels PDL-chained
+    int fwd_pre = 1;                   // TFS_OPT_FWD_PRE: forward level kernels load b and D before the wait
+    int bwd_pre = 1;                   // TFS_OPT_BWD_PRE: backward level kernels after a tail compute start values before the wait
+    int tail_pf = 1;                   // TFS_OPT_TAIL_PF: prefetching tail (k_sweep_tail1)
+    int fuse_l0 = 2;                   // TFS_OPT_FUSE_L0: DIC-CG level 0 inside the neighbouring kernels (1: binary32 only, 2: both)
+    int level_tpb = TFS_TPB;           // TFS_OPT_LEVEL_TPB: threads per block of the level kernels
+                                       // (128/256/512/1024 measured 147.7/146.4/147.4/150.1 us per DIC application)
+    int sell_uniform = 1;              // TFS_OPT_SELL_UNIFORM: one slice width when it costs <= 5% padding
+    int spmv_pref = 1;                 // TFS_OPT_SPMV: 1 software-pipelined where possible, 0 direct
+    int spmv_chunks = 0;               // TFS_OPT_SPMV_GRID: 1 one block per 256-row chunk
+    int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
+    int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
+    int pf_tail_level = 0;             // first level of the prefetching tail
+    bool pf_ok = false;                // the prefetching tail can run
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row
@@ -156,7 +133,7 @@ struct tfs_handle {
     std::vector<int> row0, col0, dia0;  // the topology, 0-based (host copy)
     std::vector<int> rcm_pos;          // RCM position of every natural row
     int layout = -1;                   // TFS_LAYOUT_* built, -1 none yet
-    int layout_pref = TFS_LAYOUT_RCM;  // TFS_LAYOUT=levels forces level order
+    int layout_pref = TFS_LAYOUT_RCM;  // TFS_OPT_LAYOUT = 1 forces level order
     int64_t fixed_bytes = 0;           // device bytes independent of the layout
     // device arrays
     int *perm = nullptr, *iperm = nullptr, *slice_off = nullptr, *col = nullptr, *vmap = nullptr;
@@ -165,12 +142,8 @@ struct tfs_handle {
     float *val32 = nullptr;
     double *stage_val = nullptr, *stage_b = nullptr, *stage_x = nullptr;
     double *part = nullptr;
-    unsigned long long *lvl_cnt = nullptr;  // finished tiles per level, 3 sets
-    int2 *tiles = nullptr;             // (first row, level) per sweep tile
-    int *d_lvl_begin = nullptr, *d_lvl_tiles = nullptr;
-    int n_tiles = 0, tail_level = 0;
-    int tail_cluster = 1, ctail_level = 0;   // CTAs of the sweep tail's cluster, its first level
-    SweepCtl *ctl = nullptr;
+    int *d_lvl_begin = nullptr;
+    int tail_level = 0;                // first level of the one-block tail
     DevState *st = nullptr;
     DevParams *params = nullptr;
     void *vec_pool = nullptr, *vec32_pool = nullptr;

@@ -478,112 +478,7 @@ k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
 
 // ------------------------------------------------------- level-scheduled DIC
 
-// Forward sweep of one level (Prec_Solve.f90:46-53) for NR right-hand sides:
-// y_i = (b_i - sum_{lower j} a_j y_col(j)) * D_i.  T = double is the
-// reference arithmetic; T = float serves the mixed-precision inner loop.
-template <typename T, int NR>
-__global__ void __launch_bounds__(TFS_TPB)
-k_fwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
-      const T *b1, const T *b2, T *y1, T *y2, int row0, int row1,
-      DevState *st, int first)
-{
-    if (st->done) return;
-    if (first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
-    if (i >= row1) return;
-    RowGeom g = row_geom(A, i);
-    if (g.len == 0) {
-        y1[i] = (T)0;
-        if (NR == 2) y2[i] = (T)0;
-        return;
-    }
-    T di = d[i];
-    if (NR == 1) {
-        T s = row_accum<true, T, T, T>(b1[i], A.col, val, y1, g.off, 0, g.dpos);
-        y1[i] = s * di;
-    } else {
-        T s1 = b1[i], s2 = b2[i];
-        row_accum2<true, T, T, T>(s1, s2, A.col, val, y1, y2, g.off, 0, g.dpos);
-        y1[i] = s1 * di;
-        y2[i] = s2 * di;
-    }
-}
-
-// Scaling and backward sweep of one level (Prec_Solve.f90:55-67):
-// z_i = (y_i / (D_i + TINY) - sum_{upper j} a_j z_col(j)) * D_i.
-template <typename T, int NR>
-__global__ void __launch_bounds__(TFS_TPB)
-k_bwd(SellDev A, const T *__restrict__ val, const T *__restrict__ d,
-      const T *y1, const T *y2, T *z1, T *z2, int row0, int row1,
-      DevState *st)
-{
-    if (st->done) return;
-    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
-    if (i >= row1) return;
-    RowGeom g = row_geom(A, i);
-    if (g.len == 0) {
-        z1[i] = (T)0;
-        if (NR == 2) z2[i] = (T)0;
-        return;
-    }
-    T di = d[i];
-    const T tiny = (T)TINY;
-    if (NR == 1) {
-        T s = y1[i] / (di + tiny);
-        s = row_accum<true, T, T, T>(s, A.col, val, z1, g.off, g.dpos + 1, g.len);
-        z1[i] = s * di;
-    } else {
-        T s1 = y1[i] / (di + tiny), s2 = y2[i] / (di + tiny);
-        row_accum2<true, T, T, T>(s1, s2, A.col, val, z1, z2, g.off, g.dpos + 1, g.len);
-        z1[i] = s1 * di;
-        z2[i] = s2 * di;
-    }
-}
-
-// ---------------------------------------------- single-launch level sweeps
-//
-// One launch runs a whole triangular sweep (or the DIC form) with blocks of
-// TFS_SWEEP_TPB threads.  Rows of the large levels are cut into tiles of at
-// most TFS_SWEEP_TPB rows that never straddle a level; the small trailing
-// levels (each at most TFS_TAIL_ROWS rows, the "tail") form one extra work
-// item that a single block runs level after level with __syncthreads()
-// between levels, so the deep, narrow end of the dependency chain costs no
-// grid-wide signalling.  Blocks take work items from a ticket counter in
-// level order (forward: large tiles then the tail; backward: the tail first,
-// then large tiles in descending order).  Before touching its dependencies a
-// large tile waits until every tile of the neighbouring level (l-1 forward,
-// l+1 backward) has finished in this sweep: each finished tile (and the tail
-// block, once per tail level) adds one to a 64-bit per-level counter, and
-// sweep number e is complete on level l when the counter reaches
-// e * tiles(l).  Rows keep the reference's per-row arithmetic.
-//
-// No deadlock is possible: a work item only waits for items with smaller
-// tickets, and a ticket is taken only by a block that is already running.
-// Every wait is bounded: after TFS_MAX_POLLS polls the kernel raises
-// ctl->abort, the other waiters give up within 64 polls, and the solve ends
-// with TFS_ERR_TIMEOUT.  The last block to finish publishes the sweep's epoch
-// and re-arms the ticket counter.
-
-#define TFS_MAX_POLLS (1 << 20)
-
-struct TileTable {
-    int n_tiles, n_levels, tail_level;   // tail_level == n_levels: no tail
-    const int2 *tile;          // (first internal row, level); the tail item is last
-    const int *lvl_begin;      // internal row offset of every level, n_levels + 1
-    const int *lvl_tiles;      // work items per level (1 for every tail level)
-};
-
-// Thread 0 of the block: wait until *cnt >= target (bounded).
-__device__ __noinline__ void wait_count(const unsigned long long *cnt, unsigned long long target,
-                                        SweepCtl *ctl)
-{
-    for (int it = 0; it < TFS_MAX_POLLS; it++) {
-        if (*(volatile const unsigned long long *)cnt >= target) return;
-        if (it >= 16) __nanosleep(64);
-        if ((it & 63) == 63 && *(volatile unsigned *)&ctl->abort) return;
-    }
-    atomicExch(&ctl->abort, 1u);
-}
+// ------------------------------------------------------ sweep rows
 
 // One row of a sweep.  MODE 0: forward y = (b - L y) * D; MODE 1: backward
 // z = (y/(D+TINY) - U z) * D; MODE 2: DIC form D_i = 1/(a_ii - sum D_k a^2).
@@ -640,92 +535,6 @@ __device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict_
     if (MODE == 2) { d[i] = (T)1 / s1; return; }
     o1[i] = s1 * di;
     if (NR == 2) o2[i] = s2 * di;
-}
-
-template <typename T, int NR, int MODE>
-__global__ void __launch_bounds__(TFS_SWEEP_TPB)
-k_sweep_lv(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2,
-           T *o1, T *o2, const T *y1, const T *y2, TileTable tt, SweepCtl *ctl,
-           unsigned long long *cnt_all, DevState *st)
-{
-    if (st->done) return;
-    constexpr int KIND = MODE == 2 ? 0 : (MODE == 0 ? 1 : 2);
-    unsigned long long *cnt = cnt_all + (size_t)KIND * tt.n_levels;
-    __shared__ int s_tile;
-    const unsigned long long e = *(volatile unsigned long long *)&ctl->epoch[KIND] + 1ull;
-    const bool has_tail = tt.tail_level < tt.n_levels;
-    if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl->ticket[KIND], 1u);
-        __syncthreads();
-        const int t = s_tile;
-        if (t >= tt.n_tiles) break;
-        const int tix = MODE == 1 ? tt.n_tiles - 1 - t : t;
-        if (has_tail && tix == tt.n_tiles - 1) {
-            // The tail: all small levels by this block, level after level.
-            if (MODE != 1 && threadIdx.x == 0 && tt.tail_level > 0) {
-                int dep = tt.tail_level - 1;
-                wait_count(cnt + dep, e * (unsigned long long)__ldg(tt.lvl_tiles + dep), ctl);
-                __threadfence();
-            }
-            __syncthreads();
-            const int nt = tt.n_levels - tt.tail_level;
-            for (int q = 0; q < nt; q++) {
-                const int lev = MODE == 1 ? tt.n_levels - 1 - q : tt.tail_level + q;
-                const int r1 = __ldg(tt.lvl_begin + lev + 1);
-                for (int i = __ldg(tt.lvl_begin + lev) + threadIdx.x; i < r1; i += TFS_SWEEP_TPB) {
-                    RowGeom g = row_geom(A, i);
-                    sweep_row<T, NR, MODE, 0>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, nullptr, nullptr);
-                }
-                __threadfence();
-                __syncthreads();
-                if (threadIdx.x == 0) atomicAdd(cnt + lev, 1ull);
-            }
-            continue;
-        }
-        const int2 tinfo = __ldg(tt.tile + tix);
-        const int lev = tinfo.y;
-        const int i = tinfo.x + threadIdx.x;
-        const bool active = i < __ldg(tt.lvl_begin + lev + 1);
-        RowGeom g{0, 0, 0};
-        if (active) g = row_geom(A, i);
-        const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
-        // Prefetch the first entries of the row before waiting.
-        int kk[4];
-        T aa[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            int j = j0 + q;
-            kk[q] = 0;
-            aa[q] = (T)0;
-            if (j < j1) { int ee = g.off + (j << 5); kk[q] = __ldg(A.col + ee); aa[q] = __ldg(val + ee); }
-        }
-        const int dep = MODE == 1 ? lev + 1 : lev - 1;
-        if (threadIdx.x == 0 && dep >= 0 && dep < tt.n_levels) {
-            wait_count(cnt + dep, e * (unsigned long long)__ldg(tt.lvl_tiles + dep), ctl);
-            __threadfence();
-        }
-        __syncthreads();
-        if (active) sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa);
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(cnt + lev, 1ull);
-    }
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(&ctl->done[KIND], 1u) == gridDim.x - 1) {
-            ctl->ticket[KIND] = 0u;
-            ctl->done[KIND] = 0u;
-            ctl->epoch[KIND] = e;
-            if (ctl->abort) {
-                ctl->abort = 0u;
-                st->status = TFS_ERR_TIMEOUT;
-                st->done = 1;
-                st->niter_out = st->iter + 1;
-            }
-            __threadfence();
-        }
-    }
 }
 
 // ------------------------------------------------ one launch per level
@@ -972,18 +781,12 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
 // completed before the first level kernel of the sweep started), so a level
 // step is only the gathers of the rows written in the steps before, the
 // row's arithmetic and a block barrier.  Per-row arithmetic as sweep_row.
-//
-// CLUSTER: the tail spread over the C CTAs of one thread-block cluster (one
-// row per thread of the cluster), the hardware cluster barrier (release /
-// acquire at cluster scope) between levels, so that levels of a few
-// thousand rows join the tail instead of taking a launch each.
-template <typename T, bool CLUSTER>
+template <typename T>
 __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, T *z,
               const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
 {
-    const int rank = CLUSTER ? (int)cooperative_groups::this_cluster().block_rank() : 0;
-    const int i = __ldg(lvl_begin + l_begin) + rank * TFS_SWEEP_TPB + (int)threadIdx.x;
+    const int i = __ldg(lvl_begin + l_begin) + (int)threadIdx.x;
     const bool mine = i < __ldg(lvl_begin + l_end);
     int lev = -1;
     RowGeom g{0, 0, 0};
@@ -1021,8 +824,7 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
                 if (!skip) y[i] = yi;
             }
         }
-        if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
-        else __syncthreads();
+        __syncthreads();
     }
     // Every row's backward start value, all at once after the forward half
     // (one division per thread instead of one on every backward step).
@@ -1039,43 +841,7 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
                 if (!skip) z[i] = s * di;
             }
         }
-        if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
-        else __syncthreads();
-    }
-}
-
-// Both tails by one thread-block cluster of C CTAs (C x TFS_SWEEP_TPB
-// threads): levels [l_begin, l_end) forward, then backward, one row per
-// thread and pass, the hardware cluster barrier between levels (release /
-// acquire at cluster scope: every CTA sees the rows the others wrote).  With
-// C CTAs the tail can take levels of up to C x 1024 rows, so fewer levels
-// need a launch of their own.
-template <typename T, int NR>
-__global__ void __launch_bounds__(TFS_SWEEP_TPB)
-k_sweep_tailc(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
-              T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
-{
-    cudaGridDependencySynchronize();
-    cudaTriggerProgrammaticLaunchCompletion();   // after the wait, as in k_sweep_tail2
-    if (st->done) return;
-    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
-    const int t = (int)cl.block_rank() * TFS_SWEEP_TPB + (int)threadIdx.x;
-    const int stride = (int)cl.num_blocks() * TFS_SWEEP_TPB;
-    for (int lev = l_begin; lev < l_end; lev++) {
-        const int r1 = __ldg(lvl_begin + lev + 1);
-        for (int i = __ldg(lvl_begin + lev) + t; i < r1; i += stride) {
-            RowGeom g = row_geom(A, i);
-            sweep_row<T, NR, 0, 0>(A, val, d, b1, b2, y1, y2, nullptr, nullptr, i, g, nullptr, nullptr);
-        }
-        cl.sync();
-    }
-    for (int lev = l_end - 1; lev >= l_begin; lev--) {
-        const int r1 = __ldg(lvl_begin + lev + 1);
-        for (int i = __ldg(lvl_begin + lev) + t; i < r1; i += stride) {
-            RowGeom g = row_geom(A, i);
-            sweep_row<T, NR, 1, 0>(A, val, d, nullptr, nullptr, z1, z2, y1, y2, i, g, nullptr, nullptr);
-        }
-        if (lev > l_begin) cl.sync();
+        __syncthreads();
     }
 }
 

@@ -1,6 +1,13 @@
-"""Build recipe of libtfs_gb300.so (sm_103a only) and of the oracle library.
+"""Build recipe of libtfs_gb300.so (sm_103a only), of the host-only
+generator of seeded synthetic systems libtfs_synth.so, and of the oracle
+library.
 
     python -m tflows.build          (from the t-flows_gb300 directory)
+
+libtfs_synth.so holds only the benchmark's input generator (tfs_synth.cpp and
+the host topology builder it calls): processes that need the seeded systems
+but must not touch the GPU solver (the CPU reference arm of the benchmark)
+load it alone.
 
 The CUDA translation unit is compiled with ``--fmad=false`` so that every
 binary64 product and sum is rounded separately, as in the reference Fortran
@@ -24,6 +31,8 @@ INCLUDE = REPO / "include"
 LIB_DIR = PKG_DIR / "lib"
 BUILD_DIR = PROJ_DIR / "_build"
 LIB_PATH = LIB_DIR / "libtfs_gb300.so"
+SYNTH_PATH = LIB_DIR / "libtfs_synth.so"
+SYNTH_SOURCES = ["tfs_synth.cpp", "tfs_topology.cpp"]
 ORACLE_SRC = REPO / "oracle" / "tfs_oracle.c"
 ORACLE_LIB = REPO / "oracle" / "_build" / "libtfs_oracle.so"
 
@@ -57,7 +66,8 @@ def _stale(target: Path, sources: list[Path]) -> bool:
 
 
 def build_library(force: bool = False, verbose: bool = False) -> Path:
-    sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.cpp")) \
+    sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) \
+        + [c for c in sorted(CSRC.glob("*.cpp")) if c.name != "tfs_synth.cpp"] \
         + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
     if not force and not _stale(LIB_PATH, sources):
         return LIB_PATH
@@ -72,6 +82,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
                      "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I", str(INCLUDE), "-c", str(cu), "-o", str(o)])
     for cpp in sorted(CSRC.glob("*.cpp")):
+        if cpp.name == "tfs_synth.cpp":
+            continue
         o = BUILD_DIR / (cpp.stem + ".o")
         objs.append(o)
         cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
@@ -84,6 +96,19 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     _run_parallel([[nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+def build_synth(force: bool = False) -> Path:
+    """Host-only library of the seeded synthetic systems (no CUDA)."""
+    sources = [CSRC / f for f in SYNTH_SOURCES] + sorted(INCLUDE.glob("*.h"))
+    if not force and not _stale(SYNTH_PATH, sources):
+        return SYNTH_PATH
+    LIB_DIR.mkdir(parents=True, exist_ok=True)
+    tmp = SYNTH_PATH.with_suffix(".so.tmp")
+    _run_parallel([["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
+                    "-I", str(INCLUDE), "-o", str(tmp), *[str(CSRC / f) for f in SYNTH_SOURCES]]])
+    os.replace(tmp, SYNTH_PATH)
+    return SYNTH_PATH
 
 
 def build_oracle(force: bool = False) -> Path:
@@ -101,6 +126,7 @@ def build_oracle(force: bool = False) -> Path:
 def main(argv: list[str]) -> int:
     force = "--force" in argv
     print(build_library(force=force, verbose="-v" in argv))
+    print(build_synth(force=force))
     print(build_oracle(force=force))
     return 0
 

@@ -1,6 +1,7 @@
-"""ctypes binding of libtfs_gb300.so (declarations in include/tfs_solver.h and
-include/tfs_synth.h).  The library is built in-tree by ``tflows.build``; a
-missing library raises instead of falling back to anything else."""
+"""ctypes binding of libtfs_gb300.so (declarations in include/tfs_solver.h)
+and of the host-only generator libtfs_synth.so (include/tfs_synth.h).  Both
+are built in-tree by ``tflows.build``; a missing library raises instead of
+falling back to anything else."""
 from __future__ import annotations
 
 import ctypes as C
@@ -14,10 +15,15 @@ TFS_CG, TFS_BICG, TFS_CGS = 0, 1, 2
 TFS_PREC_NONE, TFS_PREC_DIAG, TFS_PREC_DIC = 0, 1, 2
 TFS_FP64, TFS_MIXED = 0, 1
 TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF = 0, 1
+# options of a handle (tfs_set_option)
+(TFS_OPT_LAUNCH, TFS_OPT_LAYOUT, TFS_OPT_BICG, TFS_OPT_SELL_UNIFORM, TFS_OPT_SPMV, TFS_OPT_SPMV_GRID,
+ TFS_OPT_LEVEL_TPB, TFS_OPT_TAIL_PF, TFS_OPT_FUSE_L0, TFS_OPT_PDL, TFS_OPT_PDL_VEC, TFS_OPT_FWD_PRE,
+ TFS_OPT_BWD_PRE) = range(1, 14)
 
 _PKG = Path(__file__).resolve().parent
 # TFS_LIBRARY selects another build of the library (same ABI).
 lib_path = Path(os.environ["TFS_LIBRARY"]) if os.environ.get("TFS_LIBRARY") else _PKG / "lib" / "libtfs_gb300.so"
+synth_path = _PKG / "lib" / "libtfs_synth.so"
 
 i32, i64, u64, dbl = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 P_i32, P_dbl, P_void = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p
@@ -57,6 +63,9 @@ SIGNATURES = {
     "tfs_topology_register": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, C.POINTER(P_void)]),
     "tfs_release": (C.c_int, [P_void]),
     "tfs_set_precision": (C.c_int, [P_void, C.c_int]),
+    "tfs_set_default_precision": (C.c_int, [C.c_int]),
+    "tfs_set_option": (C.c_int, [P_void, C.c_int, C.c_int]),
+    "tfs_get_option": (C.c_int, [P_void, C.c_int, C.POINTER(C.c_int)]),
     "tfs_solve": (C.c_int, [C.c_int, P_void, i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl,
                             i32, P_i32, dbl, P_dbl, P_dbl]),
     "tfs_cg": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl, i32, P_i32, dbl, P_dbl, P_dbl]),
@@ -110,6 +119,10 @@ SIGNATURES = {
     "tfs_timer_stop": (C.c_int, [P_void, P_dbl]),
     "tfs_topology_count": (i32, [i32, i32, P_i32]),
     "tfs_topology_build": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_i32, P_i32, P_i32]),
+}
+
+# Symbols of libtfs_synth.so (include/tfs_synth.h).
+SYNTH_SIGNATURES = {
     "tfs_synth_create": (C.c_int, [C.c_int, i32, i32, i32, dbl, u64, C.c_int, C.POINTER(P_void)]),
     "tfs_synth_dims": (C.c_int, [P_void, P_i32, P_i32, P_i32]),
     "tfs_synth_export": (C.c_int, [P_void, P_i32, P_i32, P_i32, P_i32, P_dbl, P_dbl]),
@@ -119,6 +132,24 @@ SIGNATURES = {
 }
 
 _lib = None
+_synth = None
+
+
+def load_synth_library() -> C.CDLL:
+    """Load libtfs_synth.so (the seeded synthetic systems; host code only)."""
+    global _synth
+    if _synth is not None:
+        return _synth
+    if not synth_path.exists():
+        raise FileNotFoundError(f"{synth_path} is missing: build it with `python -m tflows.build` "
+                                "(or __graft_entry__.build())")
+    lib = C.CDLL(str(synth_path))
+    for name, (res, args) in SYNTH_SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _synth = lib
+    return lib
 
 
 def load_library(path: str | os.PathLike | None = None) -> C.CDLL:

@@ -42,7 +42,9 @@ class Solver:
     """A registered topology (one tfs_handle): device layout, DIC level
     schedule and work vectors stay resident between solves."""
 
-    def __init__(self, A: Matrix_Type, precision: int = TFS_FP64):
+    def __init__(self, A: Matrix_Type, precision: int = TFS_FP64, options: dict | None = None):
+        """options: {TFS_OPT_*: value} (include/tfs_solver.h), set before the
+        first solve."""
         self.lib = load_library()
         self.n, self.nnz = A.n_cells, A.nnz
         self._row, self._col, self._dia = A.row, A.col, A.dia
@@ -51,10 +53,20 @@ class Solver:
                                              ptr(A.dia, _i32), C.byref(h)), "tfs_topology_register")
         self.h = h
         self.set_precision(precision)
+        for opt, value in (options or {}).items():
+            self.set_option(opt, value)
 
     def set_precision(self, mode: int) -> None:
         check(self.lib.tfs_set_precision(self.h, mode), "tfs_set_precision")
         self.precision = mode
+
+    def set_option(self, option: int, value: int) -> None:
+        check(self.lib.tfs_set_option(self.h, option, value), "tfs_set_option")
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int(0)
+        check(self.lib.tfs_get_option(self.h, option, C.byref(v)), "tfs_get_option")
+        return v.value
 
     def close(self) -> None:
         if self.h:

@@ -1,15 +1,25 @@
-"""Seeded synthetic systems (include/tfs_synth.h) for tests and benchmarks."""
+"""Seeded synthetic systems (include/tfs_synth.h) for tests and benchmarks.
+
+The generator lives in libtfs_synth.so, a host-only library: building a
+system never loads the GPU solver library."""
 from __future__ import annotations
 
 import ctypes as C
 
 import numpy as np
 
-from .lib import TFS_SYNTH_CONVDIFF, TFS_SYNTH_POISSON, check, load_library
+from .lib import TFS_SYNTH_CONVDIFF, TFS_SYNTH_POISSON, load_synth_library
 from .matrix_mod import Matrix_Type, ptr
 
 POISSON, CONVDIFF = TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF
 BASE_SEED = 20261203
+
+
+def _check(status: int, where: str) -> None:
+    # The generator reports argument errors only (no error text); the
+    # message is built here so that no other library is loaded.
+    if status != 0:
+        raise ValueError(f"{where}: invalid arguments (status {status})")
 
 
 class SynthSystem:
@@ -18,12 +28,12 @@ class SynthSystem:
 
     def __init__(self, kind: int, nx: int, ny: int | None = None, nz: int | None = None,
                  jitter: float = 0.2, seed: int = BASE_SEED, permute: bool = True):
-        lib = load_library()
+        lib = load_synth_library()
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         h = C.c_void_p()
-        check(lib.tfs_synth_create(kind, nx, ny, nz, float(jitter), seed & (2**64 - 1),
-                                   1 if permute else 0, C.byref(h)), "tfs_synth_create")
+        _check(lib.tfs_synth_create(kind, nx, ny, nz, float(jitter), seed & (2**64 - 1),
+                                    1 if permute else 0, C.byref(h)), "tfs_synth_create")
         try:
             n, nnz, nf = C.c_int32(), C.c_int32(), C.c_int32()
             lib.tfs_synth_dims(h, C.byref(n), C.byref(nnz), C.byref(nf))
@@ -36,10 +46,10 @@ class SynthSystem:
             self.val = np.zeros(self.nnz)
             self.b = np.zeros(self.n)
             i32 = C.c_int32
-            check(lib.tfs_synth_export(h, ptr(self.faces_c, i32), ptr(self.row, i32),
-                                       ptr(self.col, i32), ptr(self.dia, i32),
-                                       ptr(self.val, C.c_double), ptr(self.b, C.c_double)),
-                  "tfs_synth_export")
+            _check(lib.tfs_synth_export(h, ptr(self.faces_c, i32), ptr(self.row, i32),
+                                        ptr(self.col, i32), ptr(self.dia, i32),
+                                        ptr(self.val, C.c_double), ptr(self.b, C.c_double)),
+                   "tfs_synth_export")
         finally:
             lib.tfs_synth_free(h)
 
@@ -48,8 +58,8 @@ class SynthSystem:
 
 
 def loguniform(lo: int, hi: int, seed: int, index: int) -> int:
-    return int(load_library().tfs_synth_loguniform(lo, hi, seed & (2**64 - 1), index))
+    return int(load_synth_library().tfs_synth_loguniform(lo, hi, seed & (2**64 - 1), index))
 
 
 def uniform(seed: int, stream: int, index: int) -> float:
-    return float(load_library().tfs_synth_uniform(seed & (2**64 - 1), stream, index))
+    return float(load_synth_library().tfs_synth_uniform(seed & (2**64 - 1), stream, index))

@@ -24,6 +24,7 @@ def pytest_configure(config):
 def _built():
     from tflows import build
     build.build_library()
+    build.build_synth()
     build.build_oracle()
     yield
 

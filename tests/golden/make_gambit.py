@@ -1,7 +1,9 @@
 """Regenerate the mesh fixtures of tests/golden/ from the reference's own test
 meshes (run from the repo root where the reference tree is present):
 
-    python tests/golden/make_gambit.py [reference root, default /root/reference]
+    python tests/golden/make_gambit.py <root of the T-FlowS source tree>
+
+(or with the root in TFS_REFERENCE_ROOT)
 
 The reference's test cases ship their meshes as Gambit neutral files (the
 input of its Neu2TFlowS converter).  The two smallest are turned into
@@ -26,6 +28,7 @@ tests/gambit_fixture.py.
 from __future__ import annotations
 
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -69,7 +72,10 @@ def write_reference_format(root: Path, name: str, out_dir: Path) -> None:
 
 
 def main() -> None:
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TFS_REFERENCE_ROOT")
+    if not arg:
+        sys.exit("usage: make_gambit.py <root of the T-FlowS source tree>")
+    root = Path(arg)
     golden = REPO / "tests" / "golden"
     for name in MESHES:
         d = build(root, name)

@@ -4,6 +4,7 @@ present, and the committed mesh fixtures against the oracle's topology,
 face loop and solver."""
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -14,13 +15,16 @@ from gambit_fixture import NAMES, load
 from oracle import tfs_oracle as O
 from tflows import gambit as G
 
-REF = Path("/root/reference")
+# Root of a T-FlowS source tree (its Tests/ directory holds the meshes); the
+# reader tests run only where one is named.
+REF = Path(os.environ.get("TFS_REFERENCE_ROOT", "") or "/nonexistent")
 MESHES = ["Tests/Rans/Channel_Re_Tau_590/chan.neu.gz",
           "Tests/Rans/Channel_Re_Tau_590_Rsm/chan_full.neu.gz",
           "Tests/Rans/Flow_over_plain/plain_50.neu.gz",
           "Tests/Rans/Impinging_Jet_2d_Distant_Re_23000/jet.neu.gz",
           "Tests/Les/Pipe_Re_Tau_180/pipe.neu.gz"]
-needs_ref = pytest.mark.skipif(not (REF / "Tests").is_dir(), reason="reference tree not present")
+needs_ref = pytest.mark.skipif(not (REF / "Tests").is_dir(),
+                               reason="no T-FlowS tree named by TFS_REFERENCE_ROOT")
 
 
 @needs_ref

@@ -15,7 +15,9 @@ import pytest
 from helpers import SOL_REL, iter_ok, oracle_solve, rel_l2, system
 from oracle import tfs_oracle as O
 from tflows import (TFS_BICG, TFS_CG, TFS_CGS, TFS_FP64, TFS_MIXED, Matrix_Type, Solver)
-from tflows.lib import TFS_ERR_NONFINITE
+from tflows.lib import (TFS_ERR_NONFINITE, TFS_OPT_BICG, TFS_OPT_BWD_PRE, TFS_OPT_FUSE_L0, TFS_OPT_FWD_PRE,
+                        TFS_OPT_LEVEL_TPB, TFS_OPT_SELL_UNIFORM, TFS_OPT_SPMV, TFS_OPT_SPMV_GRID,
+                        TFS_OPT_TAIL_PF)
 from tflows.synth import CONVDIFF, POISSON
 
 pytestmark = pytest.mark.gpu
@@ -298,24 +300,16 @@ def test_matrix_mod_example_nonsymmetric_pattern(gpu):
             assert iter_ok(res.niter, it) and rel_l2(x, xo) <= 1e-12
 
 
-@pytest.mark.parametrize("mode", ["levels", "levels-c1", "levels-c16", "coop", "single", "slab", "slab-p2"])
-def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
-    """The DIC schedules -- one launch per level with the small levels in one
-    8-CTA cluster (default), in one block (c1) or in a 16-CTA cluster (c16),
-    one cooperative launch with grid barriers, the single-launch dataflow
-    sweep, and RCM slabs per block with neighbour-only waits (one or two
-    blocks per SM) -- do the same per-row arithmetic: Prec_Form and Prec_Solve bitwise
-    equal to the oracle, and solves within the parity gates.  The 40^3 system
-    has levels of more than 8192 rows, so the grid-wide part of each schedule
-    runs, not only the tail."""
-    monkeypatch.setenv("TFS_SWEEP", mode.split("-")[0])
-    if "-c" in mode:
-        monkeypatch.setenv("TFS_TAIL_CLUSTER", mode.split("-c")[1])
-    if mode == "slab-p2":
-        monkeypatch.setenv("TFS_SLAB_PER_SM", "2")
+@pytest.mark.parametrize("tpb", [128, 256, 512, 1024])
+def test_level_kernel_block_sizes_agree(tpb, gpu):
+    """The level kernels at every block size the autotuner may pick do the
+    same per-row arithmetic: Prec_Form and Prec_Solve bitwise equal to the
+    oracle, and solves within the parity gates.  The 40^3 system has levels
+    of more than a block, so several blocks run per level, not only the
+    tail."""
     for s, method in ((system(CONVDIFF, 10, 9, 8), TFS_BICG), (system(POISSON, 40, 40, 40), TFS_CG)):
         b = np.random.default_rng(9).uniform(-1, 1, s.n)
-        with Solver(s.matrix()) as sol:
+        with Solver(s.matrix(), options={TFS_OPT_LEVEL_TPB: tpb}) as sol:
             assert np.array_equal(sol.prec_form(s.val, 2), O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
             assert np.array_equal(sol.prec_solve(s.val, 2, b),
                                   O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
@@ -325,36 +319,29 @@ def test_sweep_modes_agree_bitwise(mode, monkeypatch, gpu):
             assert res.status == 0
             assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
         if s.n > 60000:
-            with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+            with Solver(s.matrix(), precision=TFS_MIXED, options={TFS_OPT_LEVEL_TPB: tpb}) as sol:
                 x, r = np.zeros(s.n), s.b.copy()
                 res = sol.solve(method, s.val, x, r, 2, 2000, ref["tol"])
                 assert res.status == 0 and res.fin_res < ref["tol"]
                 assert iter_ok(res.niter, ref["niter"]) and rel_l2(x, ref["x"]) < 1e-6
 
 
-@pytest.mark.parametrize("grid", ["sm8", "chunks"])
-@pytest.mark.parametrize("kind", ["pipe", "bulk-2", "bulk-4", "async-2", "async-3", "async-4"])
-def test_spmv_kernels_bitwise(grid, kind, monkeypatch, gpu):
-    """The CG SpMV kernels for uniform-width matrices -- software-pipelined
-    (the next row's column indices loaded while the current row's gathers
-    are in flight), bulk-copy (matrix tiles streamed into shared memory by
-    cp.async.bulk, 2 or 4 stages) and cp.async-staged (2 to 4 stages) -- take the direct kernel's rows,
-    dot-product order and reductions over the same (virtual) grid: q = A p
-    and whole CG solves (binary64 and mixed, diagonal and DIC) are bitwise
-    those of the direct kernel (TFS_SPMV=direct)."""
-    if grid == "chunks":
-        monkeypatch.setenv("TFS_SPMV_GRID", "chunks")
-    if "-" in kind:
-        monkeypatch.setenv("TFS_BULK_STAGES", kind.split("-")[1])
+@pytest.mark.parametrize("grid", [0, 1])
+def test_spmv_kernels_bitwise(grid, gpu):
+    """The software-pipelined CG SpMV for uniform-width matrices (the next
+    row's column indices loaded while the current row's gathers are in
+    flight) takes the direct kernel's rows, dot-product order and reductions
+    over the same grid (8 blocks per SM, or one block per chunk): q = A p and
+    whole CG solves (binary64 and mixed, diagonal and DIC) are bitwise those
+    of the direct kernel (TFS_OPT_SPMV = 0)."""
     s = system(POISSON, 40, 40, 40)
     ref = oracle_solve(s, TFS_CG, 2)
     pv = np.random.default_rng(5).uniform(-1, 1, s.n)
     out = {}
-    for k in (kind.split("-")[0], "direct"):
-        monkeypatch.setenv("TFS_SPMV", k)
+    for k in (1, 0):
         res = []
         for mode in (TFS_FP64, TFS_MIXED):
-            with Solver(s.matrix(), precision=mode) as sol:
+            with Solver(s.matrix(), precision=mode, options={TFS_OPT_SPMV: k, TFS_OPT_SPMV_GRID: grid}) as sol:
                 if mode == TFS_FP64:
                     res.append(sol.spmv(s.val, pv))
                 for prec in (1, 2):
@@ -362,31 +349,27 @@ def test_spmv_kernels_bitwise(grid, kind, monkeypatch, gpu):
                     st = sol.solve(TFS_CG, s.val, x, r, prec, 2000, ref["tol"])
                     assert st.status == 0 and st.fin_res < ref["tol"]
                     res += [x, r, st.niter, st.fin_res]
+                assert sol.stats()["spmv_kernel"] == k
         out[k] = res
-    assert np.array_equal(out["direct"][0], O.spmv(s.n, s.row, s.col, s.val, pv))
-    for a, b in zip(out[kind.split("-")[0]], out["direct"]):
+    assert np.array_equal(out[0][0], O.spmv(s.n, s.row, s.col, s.val, pv))
+    for a, b in zip(out[1], out[0]):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("cluster", ["1", "8", "16"])
 @pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17), (9, 8, 8)])
-def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
+def test_tail_prefetch_bitwise(shape, gpu):
     """The one-row-per-thread tail (every row's entries, right-hand side and
-    diagonal loaded before the dependency wait), in one block or spread over
-    a cluster of up to 8 or 16 CTAs (so that mid-sized levels join it), gives
-    the DIC application and whole DIC-CG solves bitwise equal to the
-    level-by-level tail loop (TFS_TAIL_PF=0), and Prec_Solve equal to the
-    oracle."""
-    monkeypatch.setenv("TFS_TAIL_PF_CLUSTER", cluster)
+    diagonal loaded before the dependency wait) gives the DIC application
+    and whole DIC-CG solves bitwise equal to the level-by-level tail loop
+    (TFS_OPT_TAIL_PF = 0), and Prec_Solve equal to the oracle."""
     s = system(POISSON, *shape)
     ref = oracle_solve(s, TFS_CG, 2)
     b = np.random.default_rng(4).uniform(-1, 1, s.n)
     out = {}
-    for pf in ("1", "0"):
-        monkeypatch.setenv("TFS_TAIL_PF", pf)
+    for pf in (1, 0):
         res = []
         for mode in (TFS_FP64, TFS_MIXED):
-            with Solver(s.matrix(), precision=mode) as sol:
+            with Solver(s.matrix(), precision=mode, options={TFS_OPT_TAIL_PF: pf}) as sol:
                 if mode == TFS_FP64:
                     res.append(sol.prec_solve(s.val, 2, b))
                 x, r = np.zeros(s.n), s.b.copy()
@@ -394,23 +377,24 @@ def test_tail_prefetch_bitwise(shape, cluster, monkeypatch, gpu):
                 assert st.status == 0 and st.fin_res < ref["tol"]
                 res += [x, r, st.niter]
         out[pf] = res
-    assert np.array_equal(out["1"][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
-    for a, c in zip(out["1"], out["0"]):
+    assert np.array_equal(out[1][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+    for a, c in zip(out[1], out[0]):
         assert np.array_equal(a, c)
 
 
 @pytest.mark.parametrize("kind", [POISSON, CONVDIFF])
-def test_per_slice_width_layout(kind, monkeypatch, gpu):
-    """Per-slice SELL widths (TFS_SELL_UNIFORM=0: slice offsets loaded
+def test_per_slice_width_layout(kind, gpu):
+    """Per-slice SELL widths (TFS_OPT_SELL_UNIFORM = 0: slice offsets loaded
     instead of computed, so the direct SpMV kernels and the level-loop tail
     run instead of the uniform-width ones): SpMV, Prec_Solve bitwise equal
     to the oracle and CG / BiCG / CGS within the parity gates."""
-    monkeypatch.setenv("TFS_SELL_UNIFORM", "0")
+    opts = {TFS_OPT_SELL_UNIFORM: 0}
     s = system(kind, 23, 19, 17)
     b = np.random.default_rng(8).uniform(-1, 1, s.n)
     methods = (TFS_CG,) if kind == POISSON else (TFS_BICG, TFS_CGS)
-    with Solver(s.matrix()) as sol:
+    with Solver(s.matrix(), options=opts) as sol:
         assert np.array_equal(sol.spmv(s.val, b), O.spmv(s.n, s.row, s.col, s.val, b))
+        assert sol.stats()["sell_width"] == 0
         for prec in (1, 2):
             assert np.array_equal(sol.prec_solve(s.val, prec, b),
                                   O.prec_solve(s.n, s.row, s.col, s.dia, s.val, prec, b))
@@ -422,7 +406,7 @@ def test_per_slice_width_layout(kind, monkeypatch, gpu):
                 assert iter_ok(res.niter, ref["niter"])
                 if ref["niter"] <= 2000:
                     assert res.status == 0 and rel_l2(x, ref["x"]) <= SOL_REL
-    with Solver(s.matrix(), precision=TFS_MIXED) as sol:
+    with Solver(s.matrix(), precision=TFS_MIXED, options=opts) as sol:
         ref = oracle_solve(s, methods[0], 2)
         x, r = np.zeros(s.n), s.b.copy()
         res = sol.solve(methods[0], s.val, x, r, 2, 2000, ref["tol"])
@@ -430,52 +414,50 @@ def test_per_slice_width_layout(kind, monkeypatch, gpu):
             assert res.status == 0 and res.fin_res < ref["tol"]
 
 
-@pytest.mark.parametrize("knob", ["TFS_BWD_PRE", "TFS_FWD_PRE"])
+@pytest.mark.parametrize("knob", ["bwd", "fwd"])
 @pytest.mark.parametrize("shape", [(40, 40, 40), (23, 19, 17)])
-def test_backward_precompute_bitwise(shape, knob, monkeypatch, gpu):
+def test_backward_precompute_bitwise(shape, knob, gpu):
     """Level kernels that load or compute their rows' start values before
     the dependency wait -- backward: y_i / (D_i + TINY) (the tail releases
     them only past its own wait); forward: b_i and D_i (written before the
     level chain starts) -- give the DIC application, DIC-CG solves in both
     precisions and the literal two-sequence BiCG bitwise equal to loading
-    them after the wait (TFS_BWD_PRE=0, TFS_FWD_PRE=0)."""
+    them after the wait (TFS_OPT_BWD_PRE = 0, TFS_OPT_FWD_PRE = 0)."""
+    opt = TFS_OPT_BWD_PRE if knob == "bwd" else TFS_OPT_FWD_PRE
     s = system(POISSON, *shape)
     ref = oracle_solve(s, TFS_CG, 2)
     b = np.random.default_rng(6).uniform(-1, 1, s.n)
     out = {}
-    for pre in ("1", "0"):
-        monkeypatch.setenv(knob, pre)
+    for pre in (1, 0):
         res = []
         for mode in (TFS_FP64, TFS_MIXED):
-            with Solver(s.matrix(), precision=mode) as sol:
+            with Solver(s.matrix(), precision=mode, options={opt: pre}) as sol:
                 if mode == TFS_FP64:
                     res.append(sol.prec_solve(s.val, 2, b))
                 x, r = np.zeros(s.n), s.b.copy()
                 st = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
                 assert st.status == 0 and st.fin_res < ref["tol"]
                 res += [x, r, st.niter]
-        monkeypatch.setenv("TFS_BICG", "literal")
-        with Solver(s.matrix()) as sol:
+        with Solver(s.matrix(), options={opt: pre, TFS_OPT_BICG: 1}) as sol:
             x, r = np.zeros(s.n), s.b.copy()
             st = sol.solve(TFS_BICG, s.val, x, r, 2, 2000, ref["tol"])
             res += [x, r, st.niter]
-        monkeypatch.delenv("TFS_BICG")
         out[pre] = res
-    assert np.array_equal(out["1"][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
-    for a, c in zip(out["1"], out["0"]):
+    assert np.array_equal(out[1][0], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+    for a, c in zip(out[1], out[0]):
         assert np.array_equal(a, c)
 
 
-@pytest.mark.parametrize("fuse", ["0", "1", "2"])
-def test_level0_fusion_parity(fuse, monkeypatch, gpu):
+@pytest.mark.parametrize("fuse", [0, 1, 2])
+def test_level0_fusion_parity(fuse, gpu):
     """DIC-CG with level 0 swept inside the residual, update and rho kernels
-    (TFS_FUSE_L0: 0 off, 1 binary32 iteration, 2 binary64 too) stays within
-    the parity gates of the oracle in both precisions on the 40^3 system."""
-    monkeypatch.setenv("TFS_FUSE_L0", fuse)
+    (TFS_OPT_FUSE_L0: 0 off, 1 binary32 iteration, 2 binary64 too) stays
+    within the parity gates of the oracle in both precisions on the 40^3
+    system."""
     s = system(POISSON, 40, 40, 40)
     ref = oracle_solve(s, TFS_CG, 2)
     for mode, sol_tol in ((TFS_FP64, SOL_REL), (TFS_MIXED, 1e-6)):
-        with Solver(s.matrix(), precision=mode) as sol:
+        with Solver(s.matrix(), precision=mode, options={TFS_OPT_FUSE_L0: fuse}) as sol:
             x, r = np.zeros(s.n), s.b.copy()
             res = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
             assert res.status == 0 and res.fin_res < ref["tol"]
@@ -484,7 +466,7 @@ def test_level0_fusion_parity(fuse, monkeypatch, gpu):
 
 @pytest.mark.parametrize("mode", [TFS_FP64, TFS_MIXED])
 @pytest.mark.parametrize("prec", [1, 2])
-def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
+def test_bicg_equals_cg_bitwise(mode, prec, gpu):
     """The reference's BiCG (shadow residual r2 = r1, driven by A) produces the
     CG iterates bit for bit; the library runs it through the CG kernels.  In
     binary64 the literal two-sequence BiCG (TFS_BICG=literal) and CG agree
@@ -499,12 +481,10 @@ def test_bicg_equals_cg_bitwise(mode, prec, monkeypatch, gpu):
     tol = 1e-8 * np.linalg.norm(s.b)
     # Both runs reduce rho with the same kernel: the CG body's fusion of rho
     # into the level-0 backward sweep sums the partials in another order.
-    monkeypatch.setenv("TFS_FUSE_L0", "0")
     out = {}
     for tag in ("cg", "literal"):
-        if tag == "literal":
-            monkeypatch.setenv("TFS_BICG", "literal")
-        with Solver(s.matrix(), precision=mode) as sol:
+        opts = {TFS_OPT_FUSE_L0: 0, TFS_OPT_BICG: 1 if tag == "literal" else 0}
+        with Solver(s.matrix(), precision=mode, options=opts) as sol:
             x, r = np.zeros(s.n), s.b.copy()
             method = TFS_CG if tag == "cg" else TFS_BICG
             out[tag] = (x, r, sol.solve(method, s.val, x, r, prec, 2000, tol))

@@ -12,7 +12,8 @@ import pytest
 
 from oracle import tfs_oracle as O
 from tflows import Matrix_Mod_Topology, SynthSystem
-from tflows.lib import (SIGNATURES, TFS_ERR_ARG, TFS_ERR_MATRIX, lib_path, load_library)
+from tflows.lib import (SIGNATURES, SYNTH_SIGNATURES, TFS_ERR_ARG, TFS_ERR_MATRIX, lib_path,
+                        load_library, load_synth_library)
 from tflows.matrix_mod import ptr
 from tflows.synth import CONVDIFF, POISSON, loguniform
 
@@ -20,9 +21,9 @@ REPO = Path(__file__).resolve().parents[1]
 GOLD = REPO / "tests" / "golden"
 
 
-def header_functions() -> set[str]:
+def header_functions(pattern: str = "*.h") -> set[str]:
     names = set()
-    for h in (REPO / "include").glob("*.h"):
+    for h in (REPO / "include").glob(pattern):
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
         names |= set(re.findall(r"\b(tfs_[a-z0-9_]+)\s*\(", text))
     return names
@@ -30,12 +31,26 @@ def header_functions() -> set[str]:
 
 def test_library_exports_every_declared_symbol():
     lib = load_library()
-    declared = header_functions()
+    declared = header_functions("tfs_solver.h")
     assert len(declared) >= 25
     missing = [n for n in sorted(declared) if not hasattr(lib, n)]
     assert not missing, missing
     # the ctypes table covers the same set
     assert declared <= set(SIGNATURES), sorted(declared - set(SIGNATURES))
+
+
+def test_synth_library_exports_its_header_and_nothing_of_the_solver():
+    """The seeded systems come from a host-only library, so a process that
+    only builds inputs (the CPU reference arm of the benchmark) never loads
+    the GPU solver library."""
+    syn = load_synth_library()
+    declared = header_functions("tfs_synth.h")
+    assert declared and declared <= set(SYNTH_SIGNATURES)
+    assert all(hasattr(syn, n) for n in declared)
+    for n in ("tfs_solve", "tfs_cg", "tfs_topology_register", "tfs_batch_create"):
+        assert not hasattr(syn, n), n
+    lib = load_library()
+    assert not hasattr(lib, "tfs_synth_create")
 
 
 def test_library_is_in_tree_and_built_for_sm103a():
