@@ -682,16 +682,8 @@ def run_serving(args, dist: Dist) -> dict | None:
 # ---------------------------------------------------------------- batched arm
 
 def batch_specs(n_sys: int, seed: int) -> list[tuple[int, int, int, float, int]]:
-    """(nx, ny, nz, jitter, seed) of every system of the batched workload."""
-    from tflows.synth import loguniform, uniform
-    out = []
-    for k in range(n_sys):
-        n = loguniform(5000, 500000, seed, k)
-        kk = max(2, int(round(n ** (1.0 / 3.0))))
-        m = max(1, int(round(n / (kk * kk))))
-        jit = 0.25 * uniform(seed, 21, k)
-        out.append((kk, kk, m, jit, seed * 1000 + k))
-    return out
+    from tflows.synth import batched_poisson_specs
+    return batched_poisson_specs(n_sys, seed)
 
 
 def run_batched(args, dist: Dist) -> dict | None:

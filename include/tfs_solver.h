@@ -350,11 +350,16 @@ typedef struct tfs_result {
     int32_t niter, status;          /* as the solve entry points return them  */
     double  ini_res, fin_res;
     double  queued_ms, run_ms, latency_ms;  /* submit->start, start->done, submit->done */
+    /* The GPU's global nanosecond timer when the solve's first kernel began
+     * and when its iterations had ended (the store of x and r1 began): two
+     * requests whose intervals intersect ran on the device at once. */
+    int64_t device_begin_ns, device_end_ns;
 } tfs_result;
 
 typedef struct tfs_server_stats {
     int64_t submitted, completed, refused, evictions, registrations;
     int64_t resident_bytes, resident_systems, running, queued;
+    int64_t peak_running;           /* most solves launched and unfinished at once */
 } tfs_server_stats;
 
 int tfs_server_create(int device, int64_t hbm_budget_bytes, int max_inflight,
@@ -390,11 +395,14 @@ int tfs_server_get_stats(tfs_server *s, tfs_server_stats *out);
  * holding one partial sum per 256 rows, sized for TFS_NOALLOC_MAX_ROWS rows;
  * every GPU that loads the library keeps it (about 128 KB) until the process
  * exits.  Larger n is rejected with TFS_ERR_ARG.  The call is asynchronous on
- * `stream` (a cudaStream_t; NULL = the default stream).  The first call on a
- * device looks up the scratch array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  Calls share the scratch
- * array, so calls that overlap on the GPU (different streams or threads)
- * race: serialise them. */
+ * `stream` (a cudaStream_t; NULL = the default stream).  The first call in a
+ * CUDA context looks up the scratch array's device address
+ * (cudaGetSymbolAddress) and caches it for that context; a call under another
+ * context of the same device (after cudaDeviceReset, after the primary
+ * context was released and retained again, or in a context the caller
+ * created) looks it up again.  Make a context's first call before any stream
+ * capture.  Calls share the scratch array, so calls that overlap on the GPU
+ * (different streams or threads) race: serialise them. */
 #define TFS_NOALLOC_MAX_ROWS 4194304
 int tfs_residual_norm_noalloc(int32_t n, const int32_t *d_row1,
                               const int32_t *d_col1, const double *d_val,

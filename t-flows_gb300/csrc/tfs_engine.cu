@@ -1096,7 +1096,7 @@ static int launch_epilogue(tfs_handle *h, int *count)
 {
     int g = (h->n_int + 255) / 256;
     if (g > h->sm_count * 8) g = h->sm_count * 8;
-    k_store<<<g, 256, 0, h->stream>>>(h->n_int, h->perm, h->v.x, h->v.r, h->params);
+    k_store<<<g, 256, 0, h->stream>>>(h->n_int, h->perm, h->v.x, h->v.r, h->params, h->st);
     *count = 1;
     CKL("epilogue launch");
     return TFS_OK;

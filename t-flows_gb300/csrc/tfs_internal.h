@@ -56,6 +56,9 @@ struct DevState {
     // rho instead of by every thread
     float beta32;
     float alpha32;       // (float) alpha, published with alpha
+    // global timer (ns) at the start of the solve's first kernel and at the
+    // start of its epilogue
+    unsigned long long t_begin, t_end;
 };
 
 // Per-call arguments, written by the host before every graph launch.

@@ -350,6 +350,7 @@ __global__ void k_init(DevState *st, const DevParams *prm, int prec)
     s.iter = 1;
     s.loop_limit = (prm->niter_max > 0 ? prm->niter_max : 0) + 8;
     s.delta = 0.1;
+    s.t_begin = gtimer();
     *st = s;
 }
 
@@ -1150,8 +1151,9 @@ k_cgs_spmv_r(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, d
 
 // x and r1 back to natural order.
 __global__ void k_store(int n_int, const int *__restrict__ perm, const double *__restrict__ x,
-                        const double *__restrict__ r, const DevParams *prm)
+                        const double *__restrict__ r, const DevParams *prm, DevState *st)
 {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_end = gtimer();
     double *xo = prm->x, *ro = prm->r_out;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_int; i += gridDim.x * blockDim.x) {
         int o = __ldg(perm + i);

@@ -10,11 +10,22 @@
 // the device, and it allocates nothing.  Its only scratch is the file-scope
 // array below (one partial sum per 256-row block plus an arrival counter),
 // which every GPU that loads the library keeps until the process exits.
+//
+// Host code cannot hand the array's name to a kernel (on the host it is a
+// stand-in, not a device address), so the address is looked up with
+// cudaGetSymbolAddress and cached per CUDA context (tfs_ctx_cache.h): a
+// call under another context than the cached one -- after cudaDeviceReset,
+// after the primary context was released and retained again, or in a
+// context the caller created -- looks it up again in that context.  The
+// lookup of a context's first call is the only set-up; it should come
+// before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <mutex>
 
+#include "tfs_ctx_cache.h"
 #include "tfs_internal.h"
 
 namespace {
@@ -29,10 +40,38 @@ struct NoallocScratch {
 
 static __device__ __align__(256) NoallocScratch g_scratch;
 
-// Device address of g_scratch per device, looked up once per device (the
-// host-side symbol is not a device address).
-std::mutex g_mu;
-NoallocScratch *g_addr[64] = {};
+// Device address of g_scratch per device ordinal and context.
+tfs::CtxAddrCache<NoallocScratch> g_cache;
+
+// Unique id + 1 of the calling thread's current CUDA context, 0 when there
+// is none or the driver cannot say.  The driver entry points come through
+// the runtime, so the library does not link the driver library.
+uint64_t current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_cur = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = (GetCurrent)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)p;
+        cudaGetLastError();
+    });
+    if (!get_cur || !get_id) return 0;
+    CUcontext c = nullptr;
+    if (get_cur(&c) != CUDA_SUCCESS || !c) return 0;
+    unsigned long long id = 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return (uint64_t)id + 1;
+}
 
 // r1 <- r1 - A x for 1-based CSR, one row per thread, and the norm.
 __global__ void __launch_bounds__(kRows)
@@ -84,7 +123,14 @@ extern "C" int tfs_residual_norm_noalloc(int32_t n, const int32_t *d_row1, const
                                          const double *d_val, const double *d_x, double *d_r1,
                                          double *d_norm, void *stream)
 {
-    if (n <= 0 || !d_row1 || !d_col1 || !d_val || !d_x || !d_r1 || !d_norm) return TFS_ERR_ARG;
+    if (n <= 0) {
+        tfs_set_error_text("tfs_residual_norm_noalloc: n must be positive");
+        return TFS_ERR_ARG;
+    }
+    if (!d_row1 || !d_col1 || !d_val || !d_x || !d_r1 || !d_norm) {
+        tfs_set_error_text("tfs_residual_norm_noalloc: a device array is NULL");
+        return TFS_ERR_ARG;
+    }
     if (n > TFS_NOALLOC_MAX_ROWS) {
         tfs_set_error_text("tfs_residual_norm_noalloc: n exceeds TFS_NOALLOC_MAX_ROWS (4,194,304 rows)");
         return TFS_ERR_ARG;
@@ -92,18 +138,22 @@ extern "C" int tfs_residual_norm_noalloc(int32_t n, const int32_t *d_row1, const
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return tfs_engine_error(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 64) return TFS_ERR_ARG;
-    NoallocScratch *scr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_scratch);
-            if (e != cudaSuccess) return tfs_engine_error(e, "cudaGetSymbolAddress");
-            g_addr[dev] = (NoallocScratch *)p;
-        }
-        scr = g_addr[dev];
+    NoallocScratch *scr = nullptr;
+    cudaError_t le = cudaSuccess;
+    const int rc = g_cache.get(
+        dev, current_context_id(),
+        [&](NoallocScratch **p) {
+            void *a = nullptr;
+            le = cudaGetSymbolAddress(&a, g_scratch);
+            *p = (NoallocScratch *)a;
+            return le == cudaSuccess ? 0 : 1;
+        },
+        [] { return current_context_id(); }, &scr);
+    if (rc == -1) {
+        tfs_set_error_text("tfs_residual_norm_noalloc: device ordinal beyond 63");
+        return TFS_ERR_ARG;
     }
+    if (rc) return tfs_engine_error(le, "cudaGetSymbolAddress");
     cudaStream_t s = (cudaStream_t)stream;
     // The counter starts at zero for every call (a failed earlier call may
     // have left it elsewhere); the partials are all rewritten before use.

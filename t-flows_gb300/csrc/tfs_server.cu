@@ -166,6 +166,7 @@ static bool try_start(tfs_server *S, Request *r)
     sy.last_used = r->t_start;
     r->state = 1;
     S->running.push_back(r);
+    if ((int64_t)S->running.size() > S->stats.peak_running) S->stats.peak_running = (int64_t)S->running.size();
     return true;
 }
 
@@ -177,6 +178,8 @@ static void finish(tfs_server *S, Request *r, System &sy)
     r->res.niter = it;
     r->res.ini_res = ini;
     r->res.fin_res = fin;
+    r->res.device_begin_ns = (int64_t)sy.h->h_state->t_begin;
+    r->res.device_end_ns = (int64_t)sy.h->h_state->t_end;
     r->t_done = clk::now();
     r->state = 2;
     sy.busy = false;

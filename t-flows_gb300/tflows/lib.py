@@ -44,12 +44,14 @@ class tfs_stats(C.Structure):
 
 class tfs_result(C.Structure):
     _fields_ = [("ticket", i64), ("niter", i32), ("status", i32), ("ini_res", dbl), ("fin_res", dbl),
-                ("queued_ms", dbl), ("run_ms", dbl), ("latency_ms", dbl)]
+                ("queued_ms", dbl), ("run_ms", dbl), ("latency_ms", dbl),
+                ("device_begin_ns", i64), ("device_end_ns", i64)]
 
 
 class tfs_server_stats(C.Structure):
     _fields_ = [(k, i64) for k in ("submitted", "completed", "refused", "evictions", "registrations",
-                                   "resident_bytes", "resident_systems", "running", "queued")]
+                                   "resident_bytes", "resident_systems", "running", "queued",
+                                   "peak_running")]
 
 
 class TfsError(RuntimeError):

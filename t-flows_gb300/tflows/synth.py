@@ -63,3 +63,31 @@ def loguniform(lo: int, hi: int, seed: int, index: int) -> int:
 
 def uniform(seed: int, stream: int, index: int) -> float:
     return float(load_synth_library().tfs_synth_uniform(seed & (2**64 - 1), stream, index))
+
+
+def batched_poisson_specs(n_sys: int, seed: int) -> list[tuple[int, int, int, float, int]]:
+    """(nx, ny, nz, jitter, seed) of every system of the batched workload:
+    cells log-uniform in [5k, 500k] realised as k x k x m meshes (k =
+    round(cbrt(n)), m = round(n / k^2)), jitter U(0, 25%), own seed each."""
+    out = []
+    for k in range(n_sys):
+        n = loguniform(5000, 500000, seed, k)
+        kk = max(2, int(round(n ** (1.0 / 3.0))))
+        m = max(1, int(round(n / (kk * kk))))
+        jit = 0.25 * uniform(seed, 21, k)
+        out.append((kk, kk, m, jit, seed * 1000 + k))
+    return out
+
+
+def serving_pool_specs(n_pool: int, seed: int) -> list[tuple[int, int, int, int, int]]:
+    """(kind, nx, ny, nz, seed) of the resident systems of the serving trace:
+    70% pressure-Poisson, 30% convection-diffusion, cells log-uniform in
+    [10k, 2M]."""
+    out = []
+    for k in range(n_pool):
+        kind = POISSON if uniform(seed, 31, k) < 0.7 else CONVDIFF
+        n = loguniform(10000, 2000000, seed, 1000 + k)
+        kk = max(2, int(round(n ** (1.0 / 3.0))))
+        m = max(1, int(round(n / (kk * kk))))
+        out.append((kind, kk, kk, m, seed * 100 + k))
+    return out

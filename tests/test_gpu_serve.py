@@ -168,3 +168,56 @@ def test_separate_b_and_zero_start(pool):
         assert np.array_equal(a.get("b"), s.b)
     finally:
         a.free()
+
+
+def test_continuous_batching_requests_overlap_on_the_device(gpu):
+    """Requests that arrive while others are on the GPU are admitted at once
+    and their solves overlap on the device: request k + 1 is submitted only
+    after request k has been launched (the server reports it running), the
+    server reports at least two solves running at once, and the device
+    intervals of consecutive requests (the GPU's global timer at each
+    solve's first kernel and at its epilogue) intersect.  Every result is
+    bitwise the result of the same request run alone."""
+    import time
+    specs = [(POISSON, 40, 40, 40, 11), (POISSON, 36, 36, 36, 12), (POISSON, 44, 40, 38, 13),
+             (POISSON, 38, 38, 38, 14)]
+    pool = [system(k, nx, ny, nz, seed=sd) for k, nx, ny, nz, sd in specs]
+    reqs = [(k, TFS_CG, 2, TFS_FP64 if k % 2 == 0 else TFS_MIXED) for k in range(len(pool))]
+    alone = []
+    for r in reqs:
+        out, _ = _run(pool, [r], max_inflight=1)
+        alone.append(out[0])
+    arrs = [DevArrays(s) for s in pool]
+    try:
+        with Server(1 << 34, max_inflight=8) as srv:
+            ids = [srv.add_system(s.n, s.row, s.col, s.dia) for s in pool]
+            # resident systems and captured graphs first, so that admission is
+            # a launch and not a layout build
+            for k, (_, method, prec, mode) in enumerate(reqs):
+                srv.wait(srv.submit(ids[k], method, prec, arrs[k].p["val"], arrs[k].p["x"], arrs[k].p["r"],
+                                    2000, 1e-8 * np.linalg.norm(pool[k].b), mode))
+                arrs[k].reset()
+            tickets = []
+            for k, (_, method, prec, mode) in enumerate(reqs):
+                tickets.append(srv.submit(ids[k], method, prec, arrs[k].p["val"], arrs[k].p["x"],
+                                          arrs[k].p["r"], 2000, 1e-8 * np.linalg.norm(pool[k].b), mode))
+                if k + 1 < len(reqs):
+                    t0 = time.perf_counter()
+                    # the next request arrives once this one is on the GPU
+                    while srv.stats()["running"] < 1 and time.perf_counter() - t0 < 5.0:
+                        time.sleep(1e-5)
+            results = [srv.wait(t) for t in tickets]
+            stats = srv.stats()
+        assert stats["peak_running"] >= 2, stats
+        spans = [(r["device_begin_ns"], r["device_end_ns"]) for r in results]
+        assert all(0 < b < e for b, e in spans), spans
+        overlaps = sum(1 for (b0, e0), (b1, e1) in zip(spans, spans[1:]) if b1 < e0 and b0 < e1)
+        assert overlaps >= 1, spans
+        for k, res in enumerate(results):
+            ra, xa, rra = alone[k]
+            assert res["status"] == ra["status"] == 0
+            assert res["niter"] == ra["niter"] and res["fin_res"] == ra["fin_res"]
+            assert np.array_equal(arrs[k].get("x"), xa) and np.array_equal(arrs[k].get("r"), rra)
+    finally:
+        for a in arrs:
+            a.free()

@@ -206,3 +206,34 @@ def test_abi_struct_layouts_match_ctypes(tmp_path):
         assert got[(name, "size")] == C.sizeof(py), name
         for fname, _ in py._fields_:
             assert got[(name, fname)] == getattr(py, fname).offset, (name, fname)
+
+
+def test_noalloc_scratch_address_is_cached_per_context(tmp_path):
+    """The no-allocation entry point caches its scratch array's device
+    address per CUDA context, not per device ordinal: a call under another
+    context (after a device reset, a re-retained primary context or a
+    caller's own context) looks the address up again.  The cache logic is
+    compiled on the host and driven with simulated context ids."""
+    import subprocess
+    exe = tmp_path / "ctx_cache_check"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", str(REPO / "t-flows_gb300" / "csrc"),
+                    str(REPO / "tests" / "native" / "ctx_cache_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
+
+
+@pytest.mark.parametrize("case", ["n0", "null"])
+def test_noalloc_rejections_set_error_text(case):
+    """Every refusal of the no-allocation entry point says why (no GPU call
+    happens before the checks)."""
+    lib = load_library()
+    dummy = C.c_void_p(1)     # never dereferenced: the checks come first
+    if case == "n0":
+        st = lib.tfs_residual_norm_noalloc(0, dummy, dummy, dummy, dummy, dummy, dummy, None)
+        want = "n must be positive"
+    else:
+        st = lib.tfs_residual_norm_noalloc(10, dummy, None, dummy, dummy, dummy, dummy, None)
+        want = "NULL"
+    assert st == TFS_ERR_ARG
+    from tflows.lib import last_error
+    assert want in last_error()

@@ -29,6 +29,9 @@ def _cudart():
             rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
             rt.cudaMemcpy.restype = C.c_int
             rt.cudaDeviceSynchronize.restype = C.c_int
+            rt.cudaStreamCreate.argtypes = [C.POINTER(C.c_void_p)]
+            rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+            rt.cudaStreamDestroy.argtypes = [C.c_void_p]
             return rt
         except OSError:
             continue
@@ -44,7 +47,11 @@ def test_noalloc_rejects_more_rows_than_its_scratch_holds():
 
 
 @pytest.mark.gpu
-def test_noalloc_residual_norm_matches_tfs_residual(gpu):
+@pytest.mark.parametrize("stream", ["default", "created"])
+def test_noalloc_residual_norm_matches_tfs_residual(stream, gpu):
+    """Two calls in a row on the default stream, or on a stream the caller
+    created (the calls serialised by synchronising that stream), each equal
+    to the allocating entry point."""
     s = system(0, 24, 20, 18, seed=7)
     x = np.random.default_rng(11).uniform(-1, 1, s.n)
     with Solver(s.matrix()) as sol:            # the existing, allocating entry point
@@ -54,6 +61,9 @@ def test_noalloc_residual_norm_matches_tfs_residual(gpu):
 
     lib, rt = load_library(), _cudart()
     bufs = {}
+    strm = C.c_void_p()
+    if stream == "created":
+        assert rt.cudaStreamCreate(C.byref(strm)) == 0
     host = {"row": s.row, "col": s.col, "val": s.val, "x": x}
     try:
         # The test allocates the caller's device arrays; the entry point does not.
@@ -66,8 +76,10 @@ def test_noalloc_residual_norm_matches_tfs_residual(gpu):
         for call in range(2):
             assert rt.cudaMemcpy(bufs["r1"], s.b.ctypes.data, s.b.nbytes, H2D) == 0
             st = lib.tfs_residual_norm_noalloc(s.n, bufs["row"], bufs["col"], bufs["val"],
-                                               bufs["x"], bufs["r1"], bufs["norm"], None)
+                                               bufs["x"], bufs["r1"], bufs["norm"], strm if strm.value else None)
             assert st == TFS_OK, last_error()
+            if strm.value:
+                assert rt.cudaStreamSynchronize(strm) == 0
             assert rt.cudaDeviceSynchronize() == 0
             r = np.empty(s.n)
             nrm = np.zeros(1)
@@ -78,3 +90,5 @@ def test_noalloc_residual_norm_matches_tfs_residual(gpu):
     finally:
         for p in bufs.values():
             lib.tfs_device_free(p)
+        if strm.value:
+            rt.cudaStreamDestroy(strm)
