@@ -543,30 +543,70 @@ def measure_reference_meshes() -> dict:
     return out
 
 
-# ---------------------------------------------------------------- serving arm
+# ---------------------------------------------------------------- shared by the legs
 
-def run_serving(args, dist: Dist) -> dict | None:
-    """Replay a seeded Poisson-arrival trace through tfs_server, mixed then
-    binary64; latency = submit -> completion."""
+def cg_iteration_bytes(n: int, nnz: int, mixed: bool) -> int:
+    """Algorithmic bytes of one diagonal-CG iteration: the matrix once (values
+    and column indices), the row geometry, and every distinct vector read or
+    written once (p, q, r, x, the diagonal: 12 nnz + 76 n + 4 in binary64).
+    Mixed: 4-byte values and vectors in the iteration, the binary32
+    correction e in place of x (8 nnz + 40 n + 4); its binary64 true
+    residuals are not counted, so the mixed figure is a lower bound."""
+    return 8 * nnz + 40 * n + 4 if mixed else 12 * nnz + 76 * n + 4
+
+
+def _pinned(lib, nbytes, dtype, count):
+    import numpy as np
+    from tflows.lib import check
+    p = C.c_void_p()
+    check(lib.tfs_host_alloc(max(1, nbytes), C.byref(p)), "tfs_host_alloc")
+    buf = (C.c_char * max(1, nbytes)).from_address(p.value)
+    return p.value, np.frombuffer(buf, dtype=dtype, count=count)
+
+
+def _oracle_one(arg):
+    """One oracle solve of a seeded system (spawned worker)."""
+    sys.path[:0] = [str(REPO), str(REPO / "t-flows_gb300")]
+    import numpy as np
+    from oracle import tfs_oracle as O
+    from tflows.synth import SynthSystem
+    kind, nx, ny, nz, jit, sd, method, prec, niter, tol_rel = arg
+    s = SynthSystem(kind, nx, ny, nz, jitter=jit, seed=sd)
+    x, r = np.zeros(s.n), s.b.copy()
+    t = time.perf_counter()
+    it, _, _ = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, niter,
+                       tol_rel * float(np.linalg.norm(s.b)))
+    return x, it, time.perf_counter() - t
+
+
+def oracle_pool(jobs):
+    """Oracle solves on the host cores (spawned processes: a forked pool would
+    inherit the CUDA context)."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        return pool.map(_oracle_one, jobs)
+
+
+# ---------------------------------------------------------------- serving leg
+
+def serving_leg(args, dist: Dist, n_pool: int, n_requests: int) -> dict:
+    """Replay a seeded Poisson-arrival trace through the request server, each
+    arithmetic twice: operands resident on the device (tfs_server_submit) and
+    end to end from page-locked host arrays (tfs_server_submit_host: val, b
+    and x copied in and x, r1 copied out by every request).  Latency =
+    submit -> completion."""
     import concurrent.futures as cf
 
     import numpy as np
 
     import tflows
     from tflows.lib import TFS_BICG, TFS_CG, TFS_FP64, TFS_MIXED, check, load_library
-    from tflows.synth import loguniform, uniform
+    from tflows.synth import serving_pool_specs, uniform
 
     lib = load_library()
     check(lib.tfs_use_device(dist.local_rank), "tfs_use_device")
     seed = BASE_SEED + 7 + dist.rank
-    n_pool = args.serve_pool
-    specs = []
-    for k in range(n_pool):
-        kind = 0 if uniform(seed, 31, k) < 0.7 else 1
-        n = loguniform(10000, 2000000, seed, 1000 + k)
-        kk = max(2, int(round(n ** (1.0 / 3.0))))
-        m = max(1, int(round(n / (kk * kk))))
-        specs.append((kind, kk, kk, m, seed * 100 + k))
+    specs = serving_pool_specs(n_pool, seed)
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
         systems = list(ex.map(lambda sp: tflows.SynthSystem(sp[0], sp[1], sp[2], sp[3], jitter=0.2,
@@ -579,40 +619,55 @@ def run_serving(args, dist: Dist) -> dict | None:
         check(lib.tfs_device_alloc(nbytes, C.byref(p)), "tfs_device_alloc")
         return p.value
 
-    import ctypes.util
-    rt = C.CDLL("libcudart.so.13") if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else C.CDLL("libcudart.so")
-    rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
     slots = args.serve_slots
-    dev = []
+    dev, host, pinned = [], [], []
     for s in systems:
         d = {"val": dalloc(8 * s.nnz), "b": dalloc(8 * s.n),
              "x": [dalloc(8 * s.n) for _ in range(slots)], "r": [dalloc(8 * s.n) for _ in range(slots)]}
-        rt.cudaMemcpy(C.c_void_p(d["val"]), s.val.ctypes.data, 8 * s.nnz, 1)
-        rt.cudaMemcpy(C.c_void_p(d["b"]), s.b.ctypes.data, 8 * s.n, 1)
+        check(lib.tfs_memcpy(C.c_void_p(d["val"]), s.val.ctypes.data_as(C.c_void_p), 8 * s.nnz), "copy")
+        check(lib.tfs_memcpy(C.c_void_p(d["b"]), s.b.ctypes.data_as(C.c_void_p), 8 * s.n), "copy")
         dev.append(d)
+        pv, hv = _pinned(lib, 8 * s.nnz, np.float64, s.nnz)
+        hv[:] = s.val
+        hx = [_pinned(lib, 8 * s.n, np.float64, s.n) for _ in range(slots)]
+        hr = [_pinned(lib, 8 * s.n, np.float64, s.n) for _ in range(slots)]
+        pinned += [pv] + [q[0] for q in hx + hr]
+        host.append({"val": hv, "x": [q[1] for q in hx], "r": [q[1] for q in hr]})
     # The trace: exponential inter-arrival times, request kind from the pool.
-    rng_t = [uniform(seed, 41, j) for j in range(args.serve_requests)]
-    gaps = [-math.log(1.0 - u) / args.serve_rate for u in rng_t]
+    gaps = [-math.log(1.0 - uniform(seed, 41, j)) / args.serve_rate for j in range(n_requests)]
     arrivals = list(itertools.accumulate(gaps))
     reqs = []
-    for j in range(args.serve_requests):
+    for j in range(n_requests):
         k = min(n_pool - 1, int(uniform(seed, 42, j) * n_pool))
         tol_rel = 1e-6 if uniform(seed, 43, j) < 0.5 else 1e-8
         reqs.append((arrivals[j], k, tol_rel))
-    tols = [float(np.linalg.norm(s.b)) for s in systems]
+    bnorm = [float(np.linalg.norm(s.b)) for s in systems]
 
-    def replay(mode):
+    def method_of(k):
+        # pressure: diagonal CG (limit 2000); transport: diagonal BiCG with the
+        # call sites' limit of 10 iterations (Compute_Scalar.f90:615-618)
+        return (TFS_CG, 2000) if specs[k][0] == 0 else (TFS_BICG, 10)
+
+    def replay(mode, on_host):
         budget = int(args.serve_budget_gb * 1e9)
         lat, qd, runm, its, status = [], [], [], [], []
+        bytes_alg = 0
         with tflows.Server(budget, max_inflight=args.serve_inflight, device=dist.local_rank) as srv:
             ids = [srv.add_system(s.n, s.row, s.col, s.dia) for s in systems]
+
+            def submit(k, slot, niter, tol):
+                method = method_of(k)[0]
+                if on_host:
+                    h = host[k]
+                    h["r"][slot][:] = systems[k].b
+                    return srv.submit_host(ids[k], method, 1, h["val"], h["x"][slot], h["r"][slot],
+                                           niter, tol, mode=mode, x0_zero=True)
+                d = dev[k]
+                return srv.submit(ids[k], method, 1, d["val"], d["x"][slot], d["r"][slot], niter, tol,
+                                  mode=mode, d_b=d["b"], x0_zero=True)
+
             # Warm every system once (layout, graphs), outside the trace.
-            warm = []
-            for k, s in enumerate(systems):
-                method = TFS_CG if specs[k][0] == 0 else TFS_BICG
-                warm.append(srv.submit(ids[k], method, 1, dev[k]["val"], dev[k]["x"][0], dev[k]["r"][0],
-                                       10, 0.0, mode=mode, d_b=dev[k]["b"], x0_zero=True))
-            for t in warm:
+            for t in [submit(k, 0, 10, 0.0) for k in range(len(systems))]:
                 srv.wait(t)
             pending = {}            # (system, slot) -> ticket still using it
             next_slot = [0] * len(systems)
@@ -625,70 +680,135 @@ def run_serving(args, dist: Dist) -> dict | None:
                 slot = next_slot[k] % slots
                 next_slot[k] += 1
                 if (k, slot) in pending:       # slot still in use: wait for it
-                    res = srv.wait(pending.pop((k, slot)))
-                    tickets.append(res)
-                method = TFS_CG if specs[k][0] == 0 else TFS_BICG
-                niter = 2000 if method == TFS_CG else 10
-                t = srv.submit(ids[k], method, 1, dev[k]["val"], dev[k]["x"][slot], dev[k]["r"][slot],
-                               niter, tol_rel * tols[k], mode=mode, d_b=dev[k]["b"], x0_zero=True)
-                pending[(k, slot)] = t
-            for t in pending.values():
-                tickets.append(srv.wait(t))
+                    tickets.append((pending[(k, slot)][1], srv.wait(pending.pop((k, slot))[0])))
+                t = submit(k, slot, method_of(k)[1], tol_rel * bnorm[k])
+                pending[(k, slot)] = (t, k)
+            for t, k in pending.values():
+                tickets.append((k, srv.wait(t)))
             span = time.perf_counter() - start
             stats = srv.stats()
-        for res in tickets:
+        for k, res in tickets:
             lat.append(res["latency_ms"]); qd.append(res["queued_ms"]); runm.append(res["run_ms"])
             its.append(res["niter"]); status.append(res["status"])
-        return {"solves_per_s": len(tickets) / span, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
-                "mean_ms": statistics.mean(lat), "queue_p99_ms": pct(qd, 99), "run_p50_ms": pct(runm, 50),
-                "requests": len(tickets), "span_s": span, "failed": sum(1 for x in status if x != 0),
-                "evictions": stats["evictions"], "resident_gb": stats["resident_bytes"] / 1e9}
+            it_done = min(res["niter"], method_of(k)[1])
+            bytes_alg += it_done * cg_iteration_bytes(systems[k].n, systems[k].nnz, mode == TFS_MIXED)
+        out = {"solves_per_s": len(tickets) / span, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+               "mean_ms": statistics.mean(lat), "queue_p99_ms": pct(qd, 99), "run_p50_ms": pct(runm, 50),
+               "requests": len(tickets), "span_s": span, "failed": sum(1 for x in status if x != 0),
+               "evictions": stats["evictions"], "peak_running": stats["peak_running"],
+               "resident_gb": stats["resident_bytes"] / 1e9, "_bytes": bytes_alg}
+        return out
 
-    results = {}
-    clock_info = None
+    results, clock_info = {}, None
     for mode, name in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
         dist.barrier()
         sampler = ClockSampler(dist.local_rank) if mode == TFS_MIXED else None
         if sampler:
             sampler.__enter__()
-        results[name] = replay(mode)
+        results[name] = replay(mode, False)
         if sampler:
             sampler.__exit__(None, None, None)
             clock_info = sampler.summary()
+        results[name + "_e2e"] = replay(mode, True)
         log(f"[bench] serving {name}: {results[name]['solves_per_s']:.1f} solves/s, "
-            f"p50 {results[name]['p50_ms']:.2f} ms, p99 {results[name]['p99_ms']:.2f} ms")
+            f"p50 {results[name]['p50_ms']:.2f} ms, p99 {results[name]['p99_ms']:.2f} ms; end to end "
+            f"{results[name + '_e2e']['solves_per_s']:.1f} solves/s, p99 {results[name + '_e2e']['p99_ms']:.2f} ms")
+    # Error against the oracle: one request of each of the 4 smallest systems,
+    # both arithmetics, tolerance 1e-8 (transport: the 10-iteration limit).
+    sample = sorted(range(n_pool), key=lambda k: systems[k].n)[:4]
+    jobs = [(specs[k][0], specs[k][1], specs[k][2], specs[k][3], 0.2, specs[k][4], method_of(k)[0], 1,
+             method_of(k)[1], 1e-8) for k in sample]
+    refs = oracle_pool(jobs) if dist.rank == 0 and not args.no_cpu_baseline else None
+    errs = {"fp64": [], "mixed": []}
+    if refs is not None:
+        with tflows.Server(int(args.serve_budget_gb * 1e9), device=dist.local_rank) as srv:
+            for k, (xo, it, _) in zip(sample, refs):
+                sid = srv.add_system(systems[k].n, systems[k].row, systems[k].col, systems[k].dia)
+                for mode, name in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
+                    h = host[k]
+                    h["r"][0][:] = systems[k].b
+                    srv.wait(srv.submit_host(sid, method_of(k)[0], 1, h["val"], h["x"][0], h["r"][0],
+                                             method_of(k)[1], 1e-8 * bnorm[k], mode=mode, x0_zero=True))
+                    errs[name].append(float(np.linalg.norm(h["x"][0] - xo) / np.linalg.norm(xo)))
     for d in dev:
-        for p in [d["val"], d["b"]] + d["x"] + d["r"]:
-            lib.tfs_device_free(C.c_void_p(p))
-    mixed = results["mixed"]
+        for q in [d["val"], d["b"]] + d["x"] + d["r"]:
+            lib.tfs_device_free(C.c_void_p(q))
+    for q in pinned:
+        lib.tfs_host_free(C.c_void_p(q))
+    peak, peak_src = measured_peak_gbs()
+    for name in ("fp64", "mixed"):
+        r = results[name]
+        ach = r.pop("_bytes") / r["span_s"] / 1e9
+        r["roofline"] = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                         "note": "algorithmic bytes of every request's iterations over the trace's wall "
+                                 "span (a lower bound: idle gaps between arrivals included)"}
+        results[name + "_e2e"].pop("_bytes")
+        r["rel_err_vs_oracle_max"] = max(errs[name]) if errs[name] else None
+    mixed, fp64 = results["mixed"], results["fp64"]
+    return {
+        "workload": SERVE_WORKLOAD, "description": SERVE_DESC, "pool": len(systems),
+        "cells": sum(s.n for s in systems), "requests": len(reqs), "rate_per_s": args.serve_rate,
+        "max_inflight": args.serve_inflight, "budget_gb": args.serve_budget_gb,
+        "mixed": mixed, "fp64": fp64,
+        "e2e": {"value": round(results["mixed_e2e"]["solves_per_s"], 3), "unit": UNIT,
+                "p50_ms": round(results["mixed_e2e"]["p50_ms"], 3),
+                "p99_ms": round(results["mixed_e2e"]["p99_ms"], 3),
+                "fp64_value": round(results["fp64_e2e"]["solves_per_s"], 3),
+                "fp64_p99_ms": round(results["fp64_e2e"]["p99_ms"], 3),
+                "h2d_bytes_per_request": "8 nnz + 16 n of the request's system",
+                "d2h_bytes_per_request": "16 n",
+                "timing": "host wall clock over the trace; every request copies val, b, x in and x, r1 "
+                          "out from page-locked host arrays on its system's stream"},
+        "mixed_over_fp64": round(mixed["solves_per_s"] / fp64["solves_per_s"], 3),
+        "mixed_over_fp64_e2e": round(results["mixed_e2e"]["solves_per_s"] /
+                                     results["fp64_e2e"]["solves_per_s"], 3),
+        "error_sample": f"one request of each of the {len(sample)} smallest pool systems per arithmetic "
+                        f"(tol 1e-8 relative; transport solves stop at their 10-iteration limit) against "
+                        f"the oracle",
+        "clocks": clock_info,
+    }
+
+
+def run_serving(args, dist: Dist) -> dict | None:
+    leg = serving_leg(args, dist, args.serve_pool, args.serve_requests)
+    mixed = leg["mixed"]
     line = {
         "metric": METRIC, "value": round(dist.sum(mixed["solves_per_s"]), 3), "unit": UNIT,
-        "n_gpus": dist.world, "steps": len(reqs), "warmup": len(systems),
+        "n_gpus": dist.world, "steps": leg["requests"], "warmup": leg["pool"],
         "ms_per_step": round(mixed["mean_ms"], 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded jittered-hex meshes, random cell numbering, RHS U[-1,1], seeded trace)",
-        "config": {"workload": SERVE_WORKLOAD, "description": SERVE_DESC, "pool": len(systems),
-                   "requests": len(reqs), "rate_per_s": args.serve_rate,
-                   "max_inflight": args.serve_inflight, "budget_gb": args.serve_budget_gb,
-                   "parallelism": f"replicas x{dist.world}"},
+        "config": serving_config(args),
         "p50_ms": round(mixed["p50_ms"], 3), "p99_ms": round(mixed["p99_ms"], 3),
-        "mixed": mixed, "fp64": results["fp64"],
-        "mixed_over_fp64": round(mixed["solves_per_s"] / results["fp64"]["solves_per_s"], 3),
-        "gpu_launches": None, "clocks": clock_info, "e2e": None,
+        "roofline": mixed["roofline"], "gpu_launches": None, "clocks": leg.pop("clocks"), "e2e": leg["e2e"],
+        "serving": leg,
     }
     return line if dist.rank == 0 else None
 
 
-# ---------------------------------------------------------------- batched arm
+def serving_config(args) -> dict:
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return {"workload": SERVE_WORKLOAD, "description": SERVE_DESC, "pool": args.serve_pool,
+            "requests": args.serve_requests, "rate_per_s": args.serve_rate,
+            "max_inflight": args.serve_inflight, "budget_gb": args.serve_budget_gb,
+            "parallelism": f"replicas x{world}"}
+
+
+# ---------------------------------------------------------------- batched leg
 
 def batch_specs(n_sys: int, seed: int) -> list[tuple[int, int, int, float, int]]:
     from tflows.synth import batched_poisson_specs
     return batched_poisson_specs(n_sys, seed)
 
 
-def run_batched(args, dist: Dist) -> dict | None:
-    """256 uneven systems: mixed-precision batched cluster solve vs the plain
-    binary64 single-system path (one tfs_solve_device per system)."""
+def batched_leg(args, dist: Dist, n_sys: int, steps: int, warmup: int) -> dict:
+    """n_sys uneven systems (the first n_sys of the seeded 256-system
+    specification): the batched cluster solve in binary64 and mixed
+    precision against the plain binary64 single-system path (one graph-
+    captured tfs_solve_device per system), with operands resident on the
+    device, and end to end through tfs_batch_solve with page-locked host
+    arrays."""
     import concurrent.futures as cf
 
     import numpy as np
@@ -698,7 +818,7 @@ def run_batched(args, dist: Dist) -> dict | None:
 
     lib = load_library()
     check(lib.tfs_use_device(dist.local_rank), "tfs_use_device")
-    specs = batch_specs(args.batch_systems, BASE_SEED + dist.rank)
+    specs = batch_specs(256, BASE_SEED + dist.rank)[:n_sys]
     t0 = time.perf_counter()
 
     def make(spec):
@@ -748,6 +868,7 @@ def run_batched(args, dist: Dist) -> dict | None:
         for tpb in (256, 512):
             try:
                 batch.configure(cl, tpb)
+                batch_step(TFS_MIXED)
                 t = time.perf_counter()
                 batch_step(TFS_MIXED)
                 tune[(cl, tpb)] = time.perf_counter() - t
@@ -758,11 +879,19 @@ def run_batched(args, dist: Dist) -> dict | None:
     log(f"[bench] autotuned cluster {best[0]} x {best[1]} threads: "
         + ", ".join(f"{k[0]}x{k[1]}={v * 1e3:.1f}ms" for k, v in sorted(tune.items())))
 
-    results = {}
-    launches = 0
-    clock_info = None
+    def read_xs():
+        out = []
+        for k, (s, sv) in enumerate(zip(systems, solvers)):
+            x = np.empty(s.n)
+            check(lib.tfs_copy(sv.h, x.ctypes.data_as(C.c_void_p), C.c_void_p(d_x[k]), 8 * s.n), "copy")
+            check(lib.tfs_sync(sv.h), "sync")
+            out.append(x)
+        return out
+
+    results, xs_by, clock_info = {}, {}, None
+    peak, peak_src = measured_peak_gbs()
     for mode, name in ((TFS_FP64, "batched_fp64"), (TFS_MIXED, "batched_mixed")):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             res = batch_step(mode)
         dist.barrier()
         sampler = ClockSampler(dist.local_rank) if mode == TFS_MIXED else None
@@ -770,7 +899,7 @@ def run_batched(args, dist: Dist) -> dict | None:
             sampler.__enter__()
         t = time.perf_counter()
         lat = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             res = batch_step(mode)
             lat.append(res.ms)
         wall = time.perf_counter() - t
@@ -779,19 +908,31 @@ def run_batched(args, dist: Dist) -> dict | None:
             clock_info = sampler.summary()
         dist.barrier()
         wall = dist.max(wall)
-        results[name] = {"solves_per_s": dist.sum(nsys * args.steps) / wall,
-                         "ms_per_batch": wall / args.steps * 1e3,
-                         "device_ms_per_batch": statistics.mean(lat),
-                         "iterations_total": int(res.niter.sum()),
-                         "iterations_max": int(res.niter.max()),
-                         "failed": int((res.status != 0).sum())}
-        if mode == TFS_MIXED:
-            launches = 2 * args.steps
-        log(f"[bench] {name}: {results[name]['solves_per_s']:.1f} solves/s")
+        its = [int(v) for v in res.niter]
+        alg = sum(min(it, args.niter) * cg_iteration_bytes(s.n, s.nnz, mode == TFS_MIXED)
+                  for it, s in zip(its, systems))
+        dev_ms = statistics.mean(lat)
+        ach = alg / (dev_ms * 1e-3) / 1e9
+        results[name] = {"solves_per_s": dist.sum(nsys * steps) / wall,
+                         "ms_per_batch": wall / steps * 1e3,
+                         "device_ms_per_batch": dev_ms,
+                         "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
+                         "failed": int((res.status != 0).sum()),
+                         "roofline": {"kernel": f"k_batch<CG,{'float' if mode == TFS_MIXED else 'double'}> "
+                                                f"(+ k_batch_gather): whole solves, one {best[0]}-CTA "
+                                                f"cluster per system",
+                                      "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                                      "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                                      "algorithmic_bytes_per_launch": alg,
+                                      "timing": "CUDA events around the gather and the persistent launch"}}
+        xs_by[name] = read_xs()
+        log(f"[bench] {name}: {results[name]['solves_per_s']:.1f} solves/s "
+            f"({dev_ms:.2f} ms device, {ach:.0f} GB/s algorithmic)")
 
     # Plain binary64 path: one graph-captured single-system solve per system.
     for sv in solvers:
         sv.set_precision(TFS_FP64)
+
     def plain_pass():
         its = 0
         for k, sv in enumerate(solvers):
@@ -802,7 +943,7 @@ def run_batched(args, dist: Dist) -> dict | None:
         return its
     plain_pass()
     t = time.perf_counter()
-    plain_steps = max(1, args.steps // 5)
+    plain_steps = max(1, steps // 5)
     for _ in range(plain_steps):
         its = plain_pass()
     wall = dist.max(time.perf_counter() - t)
@@ -810,51 +951,85 @@ def run_batched(args, dist: Dist) -> dict | None:
                              "ms_per_pass": wall / plain_steps * 1e3, "iterations_total": its}
     log(f"[bench] plain fp64: {results['plain_fp64']['solves_per_s']:.1f} solves/s")
 
-    # Error of the mixed batched solutions against the binary64 single path.
-    res = batch_step(TFS_MIXED)
-    errs = []
-    x_m, x_p = np.empty(1), np.empty(1)
-    for k, (s, sv) in enumerate(zip(systems, solvers)):
-        x_m = np.empty(s.n)
-        check(lib.tfs_copy(sv.h, x_m.ctypes.data_as(C.c_void_p), C.c_void_p(d_x[k]), 8 * s.n), "copy")
-        check(lib.tfs_sync(sv.h), "sync")
-        errs.append(x_m)
-    plain_pass()
-    max_err = 0.0
-    for k, (s, sv) in enumerate(zip(systems, solvers)):
-        x_p = np.empty(s.n)
-        check(lib.tfs_copy(sv.h, x_p.ctypes.data_as(C.c_void_p), C.c_void_p(d_x[k]), 8 * s.n), "copy")
-        check(lib.tfs_sync(sv.h), "sync")
-        max_err = max(max_err, float(np.linalg.norm(errs[k] - x_p) / np.linalg.norm(x_p)))
+    # End to end: tfs_batch_solve with page-locked host arrays (copies of
+    # every system's val, b, x in and x, r1 out inside each step).
+    h_val, h_x, h_r, pinned = [], [], [], []
+    for s in systems:
+        pv, v = _pinned(lib, 8 * s.nnz, np.float64, s.nnz)
+        v[:] = s.val
+        px, x = _pinned(lib, 8 * s.n, np.float64, s.n)
+        pr, r = _pinned(lib, 8 * s.n, np.float64, s.n)
+        h_val.append(v); h_x.append(x); h_r.append(r); pinned += [pv, px, pr]
+    e2e_ms = []
+    for i in range(warmup + steps):
+        for k, s in enumerate(systems):
+            h_x[k][:] = 0.0
+            h_r[k][:] = s.b
+        t = time.perf_counter()
+        batch.solve(TFS_CG, 1, h_val, h_x, h_r, args.niter, tols, mode=TFS_MIXED)
+        if i >= warmup:
+            e2e_ms.append((time.perf_counter() - t) * 1e3)
+    for q in pinned:
+        lib.tfs_host_free(C.c_void_p(q))
+    e2e_total = dist.max(sum(e2e_ms))
+    e2e = {"value": round(dist.sum(nsys * steps) / (e2e_total / 1e3), 3), "unit": UNIT,
+           "h2d_bytes_per_step": int(sum(8 * s.nnz + 16 * s.n for s in systems)),
+           "d2h_bytes_per_step": int(sum(16 * s.n for s in systems)),
+           "p50_ms_per_batch": round(pct(e2e_ms, 50), 3),
+           "timing": "host wall clock around each tfs_batch_solve (copies included), mixed precision"}
 
-    cpu = None
+    # Error against the oracle on a sample: every eighth system.
+    sample = list(range(0, nsys, 8))
+    errs = {}
     if dist.rank == 0 and not args.no_cpu_baseline:
-        cpu = batched_cpu_baseline(specs, args)
-
+        t = time.perf_counter()
+        refs = oracle_pool([(0, *specs[k][:3], specs[k][3], specs[k][4], 0, 1, args.niter, REL_TOL)
+                            for k in sample])
+        log(f"[bench] batch oracle sample: {len(sample)} systems ({time.perf_counter() - t:.1f}s)")
+        for name in ("batched_fp64", "batched_mixed"):
+            e = [float(np.linalg.norm(xs_by[name][k] - xo) / np.linalg.norm(xo))
+                 for k, (xo, it, _) in zip(sample, refs)]
+            results[name]["rel_err_vs_oracle_max"] = max(e)
+        errs = {"systems": len(sample), "oracle_iterations": [int(it) for _, it, _ in refs]}
+    batch.close()
+    for sv in solvers:
+        sv.close()
+    for q in d_val + d_b + d_x + d_r + d_zero:
+        lib.tfs_device_free(C.c_void_p(q))
     mixed = results["batched_mixed"]
+    return {
+        "workload": BATCH_WORKLOAD, "description": BATCH_DESC, "systems": nsys, "cells": n_rows,
+        "nnz": nnz_all, "solver": "CG", "prec": "diag", "stop": "||b-Ax|| < 1e-8 ||b|| per system, x0 = 0",
+        "cluster": best[0], "threads_per_cta": best[1], "steps": steps,
+        "batched_mixed": mixed, "batched_fp64": results["batched_fp64"], "plain_fp64": results["plain_fp64"],
+        "mixed_batched_over_plain_fp64": round(mixed["solves_per_s"] / results["plain_fp64"]["solves_per_s"], 3),
+        "e2e": e2e, "error_sample": errs,
+        "autotune_ms": {f"{k[0]}x{k[1]}": round(v * 1e3, 2) for k, v in tune.items()},
+        "gpu_launches": 2 * steps, "clocks": clock_info,
+    }
+
+
+def batched_config(args) -> dict:
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return {"workload": BATCH_WORKLOAD, "description": BATCH_DESC, "systems": args.batch_systems,
+            "solver": "CG", "prec": "diag", "stop": "||b-Ax|| < 1e-8 ||b|| per system, x0 = 0",
+            "niter_limit": args.niter, "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
+
+
+def run_batched(args, dist: Dist) -> dict | None:
+    leg = batched_leg(args, dist, args.batch_systems, args.steps, args.warmup)
+    mixed = leg["batched_mixed"]
     line = {
         "metric": METRIC, "value": round(mixed["solves_per_s"], 3), "unit": UNIT,
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(mixed["ms_per_batch"], 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded jittered-hex meshes, random cell numbering, RHS U[-1,1])",
-        "config": {"workload": BATCH_WORKLOAD, "description": BATCH_DESC, "systems": nsys,
-                   "cells": n_rows, "nnz": nnz_all, "solver": "CG", "prec": "diag",
-                   "stop": "||b-Ax|| < 1e-8 ||b|| per system, x0 = 0",
-                   "cluster": best[0], "threads_per_cta": best[1],
-                   "l2": "inputs larger than L2", "parallelism": f"replicas x{dist.world}"},
-        "batched_mixed": mixed, "batched_fp64": results["batched_fp64"],
-        "plain_fp64": results["plain_fp64"],
-        "mixed_batched_over_plain_fp64": round(mixed["solves_per_s"] / results["plain_fp64"]["solves_per_s"], 3),
-        "max_rel_err_vs_fp64": max_err, "autotune_ms": {f"{k[0]}x{k[1]}": round(v * 1e3, 2) for k, v in tune.items()},
-        "gpu_launches": launches, "clocks": clock_info,
-        "e2e": None,
+        "config": batched_config(args), "roofline": mixed["roofline"], "e2e": leg["e2e"],
+        "gpu_launches": leg.pop("gpu_launches"), "clocks": leg.pop("clocks"), "batched": leg,
     }
-    if cpu:
-        line["cpu_baseline"] = cpu
-    batch.close()
-    for p in d_val + d_b + d_x + d_r + d_zero:
-        lib.tfs_device_free(C.c_void_p(p))
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = batched_cpu_baseline(batch_specs(args.batch_systems, BASE_SEED), args)
     return line if dist.rank == 0 else None
 
 
@@ -919,59 +1094,48 @@ def _ref_solve(arg):
     return time.perf_counter() - t, it
 
 
-def _serve_cpu_one(spec):
-    sys.path[:0] = [str(REPO), str(REPO / "t-flows_gb300")]
-    import numpy as np
-    import tflows
-    from oracle import tfs_oracle as O
-    kind, nx, ny, nz, sd, tol_rel = spec
-    s = tflows.SynthSystem(kind, nx, ny, nz, jitter=0.2, seed=sd)
-    x, r = np.zeros(s.n), s.b.copy()
-    method, niter = (0, 2000) if kind == 0 else (1, 10)
-    t = time.perf_counter()
-    O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 1, niter, tol_rel * float(np.linalg.norm(s.b)))
-    return time.perf_counter() - t
-
-
 def run_reference_other(args) -> dict:
     """Reference arm of the batched and serving workloads: the oracle on all
-    host cores, one single-threaded solve per core, on a sample."""
+    host cores, one single-threaded binary64 solve per core, every step a
+    sample of `cores` systems (batch) or requests (trace) of the workload."""
     import multiprocessing as mp
-    from tflows.synth import loguniform, uniform
+    from tflows.synth import serving_pool_specs, uniform
     cores = os.cpu_count() or 1
     if args.workload == BATCH_WORKLOAD:
         specs = batch_specs(args.batch_systems, BASE_SEED)
-        cpu = batched_cpu_baseline(specs, args)
-        desc, extra = BATCH_DESC, {"systems": len(specs)}
+        jobs_all = [(0, *sp[:3], sp[3], sp[4], 0, 1, args.niter, REL_TOL) for sp in specs]
+        config = batched_config(args)
+        what = "systems of the batch"
     else:
         seed = BASE_SEED + 7
-        pool = []
-        for k in range(args.serve_pool):
-            kind = 0 if uniform(seed, 31, k) < 0.7 else 1
-            n = loguniform(10000, 2000000, seed, 1000 + k)
-            kk = max(2, int(round(n ** (1.0 / 3.0))))
-            m = max(1, int(round(n / (kk * kk))))
-            pool.append((kind, kk, kk, m, seed * 100 + k))
-        sample = []
-        for j in range(cores):
+        pool = serving_pool_specs(args.serve_pool, seed)
+        jobs_all = []
+        for j in range(args.serve_requests):
             k = min(args.serve_pool - 1, int(uniform(seed, 42, j) * args.serve_pool))
             tol_rel = 1e-6 if uniform(seed, 43, j) < 0.5 else 1e-8
-            sample.append(pool[k] + (tol_rel,))
-        t = time.perf_counter()
-        with mp.get_context("spawn").Pool(cores) as p:
-            times = p.map(_serve_cpu_one, sample)
-        wall = time.perf_counter() - t
-        cpu = {"value": round(cores / statistics.mean(times), 4), "unit": UNIT, "cores": cores,
-               "kind": "port",
-               "sample": f"the first {cores} requests of the trace, one single-threaded binary64 solve "
-                         f"per core ({wall:.1f} s wall); throughput = cores / mean solve time"}
-        desc, extra = SERVE_DESC, {"requests_sampled": cores}
+            kind, nx, ny, nz, sd = pool[k]
+            method, niter = (0, 2000) if kind == 0 else (1, 10)
+            jobs_all.append((kind, nx, ny, nz, 0.2, sd, method, 1, niter, tol_rel))
+        config = serving_config(args)
+        what = "requests of the trace"
+    step_s, done = [], 0
+    with mp.get_context("spawn").Pool(cores) as p:
+        for i in range(args.warmup + args.steps):
+            jobs = [jobs_all[(i * cores + c) % len(jobs_all)] for c in range(cores)]
+            t = time.perf_counter()
+            p.map(_oracle_one, jobs)
+            if i >= args.warmup:
+                step_s.append(time.perf_counter() - t)
+                done += cores
+    value = done / sum(step_s)
+    cpu = {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"each step: {cores} {what}, one whole single-threaded binary64 solve per core "
+                     f"(consecutive {what} step after step)"}
     return {
         "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 0,
-        "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded systems as our arm)",
-        "config": dict({"workload": args.workload, "description": desc}, **extra),
-        "cpu_baseline": cpu,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(step_s) * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (same seeded systems as our arm)", "config": config, "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -1057,6 +1221,35 @@ def run_reference(args) -> dict:
 
 # ---------------------------------------------------------------- main
 
+DEFAULT_WORKLOAD = "poisson128_dic_cg"
+
+
+def legs(args, dist: Dist, line: dict | None) -> None:
+    """The batched and served paths of the metric, bounded so the default run
+    stays within a few minutes: the first --leg-batch-systems systems of the
+    256-system specification and a --leg-serve-requests request prefix of the
+    trace over a --leg-serve-pool system pool.  Added to the line as extra
+    keys; the headline value stays the single-system solve."""
+    b = batched_leg(args, dist, args.leg_batch_systems, min(args.steps, 10), 3)
+    sv = serving_leg(args, dist, args.leg_serve_pool, args.leg_serve_requests)
+    if line is None:
+        return
+    b["bounded"] = (f"the first {args.leg_batch_systems} of the 256 systems of {BATCH_WORKLOAD} "
+                    f"(--workload {BATCH_WORKLOAD} runs all)")
+    sv["bounded"] = (f"{args.leg_serve_requests} requests over a {args.leg_serve_pool}-system pool "
+                     f"(--workload {SERVE_WORKLOAD} runs {args.serve_requests} over {args.serve_pool})")
+    line["batched"] = b
+    line["serving"] = sv
+    line["north_star"] = {
+        "target": "mixed, batched, served path >= 1.7x the plain binary64 GPU path's solves/s",
+        "batched_mixed_over_plain_fp64": b["mixed_batched_over_plain_fp64"],
+        "served_mixed_over_fp64": sv["mixed_over_fp64"],
+        "served_mixed_over_fp64_e2e": sv["mixed_over_fp64_e2e"],
+        "single_mixed_over_fp64": line.get("mixed_over_fp64"),
+    }
+
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1064,7 +1257,7 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD],
-                    default="poisson128_dic_cg")
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument("--serve-pool", type=int, default=32)
     ap.add_argument("--serve-requests", type=int, default=1200)
     ap.add_argument("--serve-rate", type=float, default=400.0)
@@ -1072,6 +1265,14 @@ def main(argv=None) -> int:
     ap.add_argument("--serve-inflight", type=int, default=16)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--batch-systems", type=int, default=256)
+    ap.add_argument("--leg-batch-systems", type=int, default=64,
+                    help="systems of the batched leg of the default run")
+    ap.add_argument("--leg-serve-pool", type=int, default=16,
+                    help="resident systems of the serving leg of the default run")
+    ap.add_argument("--leg-serve-requests", type=int, default=400,
+                    help="requests of the serving leg of the default run")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="default run without the batched and serving legs")
     ap.add_argument("--niter", type=int, default=5000)
     ap.add_argument("--spmv-reps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1104,6 +1305,8 @@ def main(argv=None) -> int:
             line = run_serving(args, dist)
         else:
             line = run_ours(args, dist)
+            if args.workload == DEFAULT_WORKLOAD and not args.no_legs:
+                legs(args, dist, line)
     finally:
         dist.close()
     if line is not None:

@@ -152,6 +152,10 @@ int tfs_set_default_precision(int mode);
                                     their dependency wait (default); 0          */
 #define TFS_OPT_BWD_PRE      13  /* 1 backward level kernels compute their start
                                     values before the wait (default); 0         */
+#define TFS_OPT_DIC_BLOCK    14  /* 1 the whole DIC application (and Prec_Form)
+                                    in one thread block with the vector in
+                                    shared memory, where it fits (default); 0
+                                    the level kernels                           */
 
 /* Set / read one option of a handle.  TFS_ERR_ARG for an unknown option or
  * value.  Replaces nothing in the reference. */
@@ -376,6 +380,16 @@ int tfs_server_add_system(tfs_server *s, int32_t n, int32_t nnz, const int32_t *
 int tfs_server_submit(tfs_server *s, int64_t sys_id, int method, int prec, int mode,
                       const double *d_val, const double *d_b, double *d_x, double *d_r1,
                       int x0_zero, int32_t niter, double tol, int64_t *ticket);
+/* As tfs_server_submit with the Fortran call's host arrays: val (nnz), x
+ * (n, the start value unless x0_zero) and r1 (n: b on entry, the final
+ * residual on return), all in host memory (page-locked for overlap).  The
+ * copies in and out run on the system's stream as part of the request, as
+ * the drop-in tfs_cg/tfs_bicg/tfs_cgs do per call; the arrays must stay
+ * valid until the ticket is waited for.  Replaces: Cg.f90:2-4 called from
+ * several threads at once, served concurrently. */
+int tfs_server_submit_host(tfs_server *s, int64_t sys_id, int method, int prec, int mode,
+                           const double *val, double *x, double *r1, int x0_zero, int32_t niter,
+                           double tol, int64_t *ticket);
 /* Wait up to timeout_s for a ticket; TFS_ERR_TIMEOUT if still running.  A
  * ticket is returned once. */
 int tfs_server_wait(tfs_server *s, int64_t ticket, double timeout_s, tfs_result *out);

@@ -23,6 +23,7 @@
 #include "tfs_kernels.cuh"
 #include "tfs_mixed.cuh"
 #include "tfs_spmv.cuh"
+#include "tfs_dic_block.cuh"
 
 using namespace tfs;
 
@@ -569,6 +570,22 @@ static int build_layout(tfs_handle *h, int kind)
         }
         h->pf_tail_level = l;
         h->pf_ok = l < nl && l <= h->tail_level;
+        // One-block DIC: the swept vector (every row of the levels) in the
+        // block's shared memory.
+        h->dicb_bytes64 = h->dicb_bytes32 = 0;
+        if (kind == TFS_LAYOUT_LEVELS) {
+            int optin = 0;
+            CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+            const int64_t rows = h->lvl_begin[nl];
+            if (rows * 8 <= optin) h->dicb_bytes64 = (int)((rows * 8 + 15) & ~15ll);
+            if (rows * 4 <= optin) h->dicb_bytes32 = (int)((rows * 4 + 15) & ~15ll);
+            static std::once_flag attr_once;
+            std::call_once(attr_once, [optin] {
+                cudaFuncSetAttribute(k_dic_block<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            });
+        }
         if ((rc = dalloc(h, &h->d_lvl_begin, nl + 1))) return rc;
         CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_begin.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, h->stream));
     }
@@ -730,6 +747,7 @@ static int *option_field(tfs_handle *h, int option, bool (**ok)(int))
     case TFS_OPT_PDL_VEC: return &h->pdl_vec;
     case TFS_OPT_FWD_PRE: return &h->fwd_pre;
     case TFS_OPT_BWD_PRE: return &h->bwd_pre;
+    case TFS_OPT_DIC_BLOCK: return &h->dic_block;
     default: return nullptr;
     }
 }
@@ -770,8 +788,22 @@ extern "C" int tfs_get_option(const tfs_handle *h, int option, int *value)
 
 // DIC recurrence (Prec_Form.f90:32-40): one launch per large level, the tail
 // in one block.  Returns the number of kernels launched.
+// Bytes of shared memory of the one-block DIC for arithmetic T, 0 when it
+// does not run (the vector does not fit, or TFS_OPT_DIC_BLOCK = 0).
+template <typename T>
+static int dic_block_bytes(const tfs_handle *h)
+{
+    if (!h->dic_block || h->layout != TFS_LAYOUT_LEVELS) return 0;
+    return sizeof(T) == 8 ? h->dicb_bytes64 : h->dicb_bytes32;
+}
+
 static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
+    if (const int bytes = dic_block_bytes<double>(h)) {
+        k_dic_block<double, 2><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), h->val, h->v.d, nullptr, nullptr,
+                                                              h->d_lvl_begin, h->n_levels, h->st);
+        return 1;
+    }
     int cnt = 0;
     if (launch_levels<double, 1, 2>(h, s, h->val, h->v.d, nullptr, nullptr, nullptr, nullptr, nullptr,
                                     nullptr, &cnt))
@@ -835,6 +867,14 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     T *d;
     if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (T *)h->v.d; }
     else { val = (const T *)h->val32; d = (T *)h->f.d; }
+    if (nr == 1 && !fuse_l0) {
+        if (const int bytes = dic_block_bytes<T>(h)) {
+            k_dic_block<T, 0><<<1, TFS_DICB_TPB, bytes, s>>>(A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, h->st);
+            (*count)++;
+            CKL("one-block DIC launch");
+            return TFS_OK;
+        }
+    }
     // Forward levels, both tails in one block, backward levels.
     int rc;
     const int tail_at = sweep_tail_at(h, nr);
@@ -890,6 +930,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 static int dic_l0_rows(const tfs_handle *h, int method, int prec)
 {
     if (method != TFS_CG || prec != 2 || !h->fuse_l0) return 0;
+    if (h->precision == TFS_MIXED ? dic_block_bytes<float>(h) : dic_block_bytes<double>(h)) return 0;
     if (h->precision == TFS_MIXED && !h->vec4) return 0;
     if (h->precision != TFS_MIXED && h->fuse_l0 != 2) return 0;
     const int tail_at = sweep_tail_at(h, 1);

@@ -127,8 +127,10 @@ struct tfs_handle {
     int spmv_chunks = 0;               // TFS_OPT_SPMV_GRID: 1 one block per 256-row chunk
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
+    int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC (vector in shared memory) where it fits
     int pf_tail_level = 0;             // first level of the prefetching tail
     bool pf_ok = false;                // the prefetching tail can run
+    int dicb_bytes64 = 0, dicb_bytes32 = 0;   // shared memory of the one-block DIC, 0: does not fit
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row

@@ -38,6 +38,7 @@ struct Request {
     const double *val = nullptr, *b = nullptr;
     double *x = nullptr, *r1 = nullptr;
     int x0_zero = 0;
+    bool host = false;   // val, x, r1 in host memory (copied on the system's stream)
     int32_t niter = 0;
     double tol = 0.0;
     clk::time_point t_submit, t_start, t_done;
@@ -151,8 +152,8 @@ static bool try_start(tfs_server *S, Request *r)
     }
     tfs_set_precision(sy.h, r->mode);
     r->t_start = clk::now();
-    int rc = tfs_solve_launch(r->method, sy.h, r->val, r->x, r->r1, r->prec, r->niter, r->tol, true,
-                              r->b, r->x0_zero);
+    int rc = tfs_solve_launch(r->method, sy.h, r->val, r->x, r->r1, r->prec, r->niter, r->tol, !r->host,
+                              r->host ? nullptr : r->b, r->x0_zero);
     if (rc) {
         r->res.status = rc;
         r->state = 2;
@@ -289,9 +290,9 @@ extern "C" int tfs_server_add_system(tfs_server *S, int32_t n, int32_t nnz, cons
     return TFS_OK;
 }
 
-extern "C" int tfs_server_submit(tfs_server *S, int64_t sys_id, int method, int prec, int mode,
-                                 const double *d_val, const double *d_b, double *d_x, double *d_r1,
-                                 int x0_zero, int32_t niter, double tol, int64_t *ticket)
+static int submit(tfs_server *S, int64_t sys_id, int method, int prec, int mode, const double *d_val,
+                  const double *d_b, double *d_x, double *d_r1, int x0_zero, int32_t niter, double tol,
+                  bool host, int64_t *ticket)
 {
     if (!S || !ticket || !d_val || !d_x || !d_r1) return TFS_ERR_ARG;
     if (method < TFS_CG || method > TFS_CGS || prec < 0 || prec > 2 ||
@@ -309,6 +310,7 @@ extern "C" int tfs_server_submit(tfs_server *S, int64_t sys_id, int method, int 
     r->r1 = d_r1;
     r->niter = niter;
     r->tol = tol;
+    r->host = host;
     r->t_submit = clk::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -321,6 +323,20 @@ extern "C" int tfs_server_submit(tfs_server *S, int64_t sys_id, int method, int 
     S->cv_work.notify_one();
     *ticket = r->ticket;
     return TFS_OK;
+}
+
+extern "C" int tfs_server_submit(tfs_server *S, int64_t sys_id, int method, int prec, int mode,
+                                 const double *d_val, const double *d_b, double *d_x, double *d_r1,
+                                 int x0_zero, int32_t niter, double tol, int64_t *ticket)
+{
+    return submit(S, sys_id, method, prec, mode, d_val, d_b, d_x, d_r1, x0_zero, niter, tol, false, ticket);
+}
+
+extern "C" int tfs_server_submit_host(tfs_server *S, int64_t sys_id, int method, int prec, int mode,
+                                      const double *val, double *x, double *r1, int x0_zero, int32_t niter,
+                                      double tol, int64_t *ticket)
+{
+    return submit(S, sys_id, method, prec, mode, val, nullptr, x, r1, x0_zero, niter, tol, true, ticket);
 }
 
 extern "C" int tfs_server_wait(tfs_server *S, int64_t ticket, double timeout_s, tfs_result *out)

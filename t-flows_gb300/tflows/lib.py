@@ -18,7 +18,7 @@ TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF = 0, 1
 # options of a handle (tfs_set_option)
 (TFS_OPT_LAUNCH, TFS_OPT_LAYOUT, TFS_OPT_BICG, TFS_OPT_SELL_UNIFORM, TFS_OPT_SPMV, TFS_OPT_SPMV_GRID,
  TFS_OPT_LEVEL_TPB, TFS_OPT_TAIL_PF, TFS_OPT_FUSE_L0, TFS_OPT_PDL, TFS_OPT_PDL_VEC, TFS_OPT_FWD_PRE,
- TFS_OPT_BWD_PRE) = range(1, 14)
+ TFS_OPT_BWD_PRE, TFS_OPT_DIC_BLOCK) = range(1, 15)
 
 _PKG = Path(__file__).resolve().parent
 # TFS_LIBRARY selects another build of the library (same ABI).
@@ -104,6 +104,8 @@ SIGNATURES = {
     "tfs_server_add_system": (C.c_int, [P_void, i32, i32, P_i32, P_i32, P_i32, C.POINTER(i64)]),
     "tfs_server_submit": (C.c_int, [P_void, i64, C.c_int, C.c_int, C.c_int, P_void, P_void, P_void,
                                     P_void, C.c_int, i32, dbl, C.POINTER(i64)]),
+    "tfs_server_submit_host": (C.c_int, [P_void, i64, C.c_int, C.c_int, C.c_int, P_void, P_void, P_void,
+                                         C.c_int, i32, dbl, C.POINTER(i64)]),
     "tfs_server_wait": (C.c_int, [P_void, i64, dbl, C.POINTER(tfs_result)]),
     "tfs_server_get_stats": (C.c_int, [P_void, C.POINTER(tfs_server_stats)]),
     "tfs_residual_norm_noalloc": (C.c_int, [i32, P_void, P_void, P_void, P_void, P_void, P_void, P_void]),

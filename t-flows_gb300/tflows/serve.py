@@ -50,6 +50,20 @@ class Server:
               "tfs_server_submit")
         return t.value
 
+    def submit_host(self, sys_id: int, method: int, prec: int, val: np.ndarray, x: np.ndarray,
+                    r1: np.ndarray, niter: int, tol: float, mode: int = TFS_FP64,
+                    x0_zero: bool = False) -> int:
+        """Queue a solve on host arrays (the drop-in call's arguments): val and
+        r1 = b copied in, x and r1 copied out by the request itself.  The
+        arrays must stay alive until the ticket is waited for."""
+        t = C.c_int64()
+        check(self.lib.tfs_server_submit_host(self.s, sys_id, method, prec, mode,
+                                              val.ctypes.data_as(C.c_void_p), x.ctypes.data_as(C.c_void_p),
+                                              r1.ctypes.data_as(C.c_void_p), 1 if x0_zero else 0, niter,
+                                              tol, C.byref(t)),
+              "tfs_server_submit_host")
+        return t.value
+
     def wait(self, ticket: int, timeout_s: float = 600.0) -> dict:
         r = tfs_result()
         st = self.lib.tfs_server_wait(self.s, ticket, timeout_s, C.byref(r))

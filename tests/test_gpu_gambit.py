@@ -111,3 +111,37 @@ def test_solve_from_reference_format_files(gpu):
             x, r = np.zeros(s.n), s.b.copy()
             res = sol.solve(TFS_CG, s.val, x, r, prec, 5000, ref["tol"])
             assert res.status == 0 and res.fin_res < ref["tol"] and rel_l2(x, ref["x"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_one_block_dic_on_reference_mesh(name, gpu):
+    """The reference's meshes in their own numbering have deep level
+    schedules (plain_50: 148 levels of about 100 rows), which is what the
+    one-block DIC (the swept vector in shared memory) is for: Prec_Form and
+    Prec_Solve bitwise equal to the oracle, and DIC-CG solves in both
+    arithmetics bitwise equal to the level kernels' (TFS_OPT_DIC_BLOCK = 0,
+    with level 0 not fused, so that rho is reduced by the same kernel)."""
+    from tflows.lib import TFS_OPT_DIC_BLOCK, TFS_OPT_FUSE_L0
+    s = load(name)
+    b = np.random.default_rng(3).uniform(-1, 1, s.n)
+    ref = oracle(s, TFS_CG, 2)
+    out = {}
+    for blk in (1, 0):
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode, options={TFS_OPT_DIC_BLOCK: blk, TFS_OPT_FUSE_L0: 0}) as sol:
+                if mode == TFS_FP64:
+                    d = sol.prec_form(s.val, 2)
+                    z = sol.prec_solve(s.val, 2, b)
+                    assert np.array_equal(d, O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
+                    assert np.array_equal(z, O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+                    res += [d, z]
+                x, r = np.zeros(s.n), s.b.copy()
+                st = sol.solve(TFS_CG, s.val, x, r, 2, 5000, ref["tol"])
+                assert st.status == 0 and st.fin_res < ref["tol"]
+                if mode == TFS_FP64:
+                    assert iter_ok(st.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
+                res += [x, r, st.niter, st.fin_res]
+        out[blk] = res
+    for a, c in zip(out[1], out[0]):
+        assert np.array_equal(a, c)

@@ -551,3 +551,38 @@ def test_autotune_keeps_parity(mode, gpu):
         res = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
         assert res.status == 0 and res.fin_res < ref["tol"] and iter_ok(res.niter, ref["niter"])
         assert rel_l2(x, ref["x"]) <= (SOL_REL if mode == TFS_FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("kind,shape", [(POISSON, (16, 16, 16)), (POISSON, (23, 19, 17)),
+                                        (CONVDIFF, (12, 11, 10))])
+def test_one_block_dic_bitwise(kind, shape, gpu):
+    """The one-block DIC (forward sweep, scaling and backward sweep, and the
+    Prec_Form recurrence, in one thread block with the vector in shared
+    memory) gives the level kernels' results bit for bit: Prec_Form and
+    Prec_Solve equal to the oracle, whole DIC solves (CG in both arithmetics,
+    CGS in binary64) equal to TFS_OPT_DIC_BLOCK = 0 with level 0 not fused."""
+    from tflows.lib import TFS_OPT_DIC_BLOCK
+    s = system(kind, *shape)
+    b = np.random.default_rng(12).uniform(-1, 1, s.n)
+    methods = [TFS_CG] if kind == POISSON else [TFS_CGS]
+    out = {}
+    for blk in (1, 0):
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode, options={TFS_OPT_DIC_BLOCK: blk, TFS_OPT_FUSE_L0: 0}) as sol:
+                if mode == TFS_FP64:
+                    res += [sol.prec_form(s.val, 2), sol.prec_solve(s.val, 2, b)]
+                for method in methods:
+                    if mode == TFS_MIXED and method == TFS_CGS:
+                        continue
+                    ref = oracle_solve(s, method, 2)
+                    x, r = np.zeros(s.n), s.b.copy()
+                    st = sol.solve(method, s.val, x, r, 2, 2000, ref["tol"])
+                    if ref["niter"] <= 2000:
+                        assert st.status == 0 and st.fin_res < ref["tol"]
+                    res += [x, r, st.niter]
+        out[blk] = res
+    assert np.array_equal(out[1][0], O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
+    assert np.array_equal(out[1][1], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+    for a, c in zip(out[1], out[0]):
+        assert np.array_equal(a, c)
