@@ -316,11 +316,35 @@ def run_ours(args, dist: Dist) -> dict | None:
     # SpMV alone (CUDA events, back-to-back launches on the resident matrix).
     spmv64_ms = sol.time_spmv(s.val, TFS_FP64, args.spmv_reps)
     spmv32_ms = sol.time_spmv(s.val, TFS_MIXED, args.spmv_reps)
+    # The same SpMV on the same matrix in RCM row order (the layout of the
+    # solves without DIC): the gathers of a warp's 32 rows then share
+    # sectors, where the DIC level order scatters them.
+    spmv_rcm = None
+    if prec == 2:
+        with tflows.Solver(s.matrix()) as sol_rcm:
+            r32 = sol_rcm.time_spmv(s.val, TFS_MIXED, args.spmv_reps)
+            r64 = sol_rcm.time_spmv(s.val, TFS_FP64, args.spmv_reps)
+        spmv_rcm = {"fp32_us": round(r32 * 1e3, 2), "fp64_us": round(r64 * 1e3, 2),
+                    "fp32_gbs": round((8 * nnz + 12 * n + 4) / (r32 * 1e-3) / 1e9, 1),
+                    "fp64_gbs": round((12 * nnz + 20 * n + 4) / (r64 * 1e-3) / 1e9, 1)}
     bytes64 = 12 * nnz + 20 * n + 4
     bytes32 = 8 * nnz + 12 * n + 4
     # DIC application alone (both sweeps), when the workload uses DIC.
     prec32_ms = sol.time_prec(s.val, TFS_MIXED, args.spmv_reps) if prec == 2 else None
     prec_bytes32 = 8 * nnz + 24 * n
+    # Device stamps of one binary32 DIC application's level launches: how a
+    # level step splits into the hand-off between launches (the wait for the
+    # previous level's completion) and the launch's own work.
+    level_split = None
+    if prec == 2 and sol.stats()["dic_kernel"] == 0:
+        prof = sol.profile_prec(s.val, TFS_MIXED)
+        work = [p["end_us"] - p["start_us"] for p in prof]
+        gaps = [b["start_us"] - a["end_us"] for a, b in zip(prof, prof[1:])]
+        level_split = {"launches": len(prof), "span_us": round(prof[-1]["end_us"] - prof[0]["start_us"], 2),
+                       "work_us": round(sum(work), 2), "handoff_us": round(sum(gaps), 2),
+                       "per_launch": [[p["launch"], round(p["start_us"], 2), round(p["end_us"], 2)] for p in prof],
+                       "how": "tfs_profile_prec: global timer when each launch's blocks passed their dependency "
+                              "wait (earliest) and finished (latest); hand-off = next start - this end"}
 
     # End to end through tfs_solve with page-locked host arrays (headline arithmetic).
     e2e = None
@@ -353,6 +377,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     if dist.rank == 0 and not args.no_next_rows:
         next_rows = measure_next_rows(lib, sol, s, dalloc)
         next_rows["reference_meshes"] = measure_reference_meshes()
+        next_rows["process_pattern"] = measure_process_pattern(lib)
     for p in (d_val, d_b, d_x, d_r, d_zero):
         lib.tfs_device_free(C.c_void_p(p))
 
@@ -418,7 +443,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
                 "algorithmic_bytes_per_launch": prec_bytes32,
-                "us_per_application": round(prec32_ms * 1e3, 2),
+                "us_per_application": round(prec32_ms * 1e3, 2), "level_split": level_split,
                 "traffic": ncu_traffic(args.workload, "dic_application"),
                 "timing": "CUDA events, back-to-back applications on the handle's stream"}
     mixed = results.get("mixed") or results["fp64"]
@@ -435,7 +460,10 @@ def run_ours(args, dist: Dist) -> dict | None:
         "mixed_over_fp64": round(mixed["solves_per_s"] / fp64["solves_per_s"], 4),
         "spmv": {"fp64_us": round(spmv64_ms * 1e3, 2), "fp32_us": round(spmv32_ms * 1e3, 2),
                  "fp64_gbs": round(bytes64 / (spmv64_ms * 1e-3) / 1e9, 1),
-                 "fp32_gbs": round(achieved, 1), "timing": "CUDA events, back-to-back launches"},
+                 "fp32_gbs": round(achieved, 1), "timing": "CUDA events, back-to-back launches",
+                 "rcm_order": dict(spmv_rcm, fp32_frac=round(spmv_rcm["fp32_gbs"] / peak, 4),
+                                   layout="the same matrix in RCM row order (no DIC levels)")
+                              if spmv_rcm else None},
         "roofline": roof, "roofline_spmv": roof_spmv, "autotune": tune, "next_rows": next_rows,
         "e2e": e2e, "gpu_launches": int(timed_launches),
         "clocks": clock_info,
@@ -540,6 +568,78 @@ def measure_reference_meshes() -> dict:
         out[name] = row
     out["timing"] = ("device time of one tfs_solve (CUDA events inside the library, median of 3 "
                      "after a warm-up); oracle: one binary64 solve on one host core")
+    return out
+
+
+def measure_process_pattern(lib, calls: int = 20) -> dict:
+    """The solver calls T-FlowS's Process makes, replayed on the reference's
+    own meshes through the Fortran-shaped entry points with host arrays:
+    per outer iteration a pressure-correction solve Bicg(A, pp, b, PREC, 40,
+    PP%STol) (Compute_Pressure_Simple.f90:190-193) and a momentum solve
+    Cg(A, u, b, PREC, 10, U%STol) (NewUVW.f90:592-599), with the settings of
+    the Flow_over_plain deck (T-FlowS.cmn: ic preconditioning, absolute
+    tolerances 1e-6).  Each call uploads the matrix values, b and x and
+    reads x and r1 back, as the drop-in does; the right-hand side changes
+    from call to call (seeded U[-1,1]) and x starts from zero.  The mesh's
+    pressure matrix stands in for both systems (the momentum matrix needs
+    the flow field).  Timed against the oracle making the same calls on one
+    host core; every binary64 GPU call is checked against the oracle's."""
+    import numpy as np
+    from oracle import tfs_oracle as O
+    from tflows import TFS_FP64, TFS_MIXED
+    from tflows import gambit as G
+    out = {}
+    kinds = (("pressure_bicg", 1, 40), ("momentum_cg", 0, 10))
+    for name in ("chan", "plain50"):
+        s = G.system_from_fixture(REPO / "tests" / "golden" / f"gambit_{name}.npz")
+        rng = np.random.default_rng(BASE_SEED)
+        rhs = [rng.uniform(-1.0, 1.0, s.n) for _ in range(calls)]
+        P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+        row = {"cells": s.n, "nnz": s.nnz, "calls": 2 * calls,
+               "settings": "prec 2 (ic), tol 1e-6 absolute, pressure BiCG limit 40, momentum CG limit 10"}
+        # the oracle, one host core
+        ref, t_cpu = {}, []
+        for j in range(calls):
+            for kname, method, lim in kinds:
+                x, r = np.zeros(s.n), rhs[j].copy()
+                t = time.perf_counter()
+                it, _, _ = O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, 2, lim, 1e-6)
+                t_cpu.append(time.perf_counter() - t)
+                ref[(kname, j)] = (x, it)
+        row["oracle_ms_per_call"] = round(statistics.mean(t_cpu) * 1e3, 4)
+        for mode, tag in ((TFS_FP64, "fp64"), (TFS_MIXED, "mixed")):
+            lib.tfs_set_default_precision(mode)
+            t_gpu, errs, its, its_ref = [], [], [], []
+            for rep in range(2):             # the first pass builds the handle and its graphs
+                t_gpu, errs, its, its_ref = [], [], [], []
+                for j in range(calls):
+                    for kname, method, lim in kinds:
+                        x, r = np.zeros(s.n), rhs[j].copy()
+                        niter = C.c_int32(lim)
+                        ini, fin = C.c_double(0.0), C.c_double(0.0)
+                        fn = lib.tfs_bicg if method == 1 else lib.tfs_cg
+                        t = time.perf_counter()
+                        st = fn(s.n, s.nnz, P(s.row, C.c_int32), P(s.col, C.c_int32), P(s.dia, C.c_int32),
+                                P(s.val, C.c_double), P(x, C.c_double), P(r, C.c_double), 2, C.byref(niter),
+                                1e-6, C.byref(ini), C.byref(fin))
+                        t_gpu.append(time.perf_counter() - t)
+                        if st not in (0, 4):
+                            raise RuntimeError(f"{fn.__name__}: status {st}")
+                        xo, it = ref[(kname, j)]
+                        its.append(niter.value)
+                        its_ref.append(it)
+                        errs.append(float(np.linalg.norm(x - xo) / max(np.linalg.norm(xo), 1e-300)))
+            row[tag] = {"ms_per_call": round(statistics.mean(t_gpu) * 1e3, 4),
+                        "p99_ms": round(pct([t * 1e3 for t in t_gpu], 99), 4),
+                        "speedup_vs_oracle_1core": round(statistics.mean(t_cpu) / statistics.mean(t_gpu), 3),
+                        "iterations_equal_to_oracle": sum(1 for a, b in zip(its, its_ref) if a == b),
+                        "max_abs_iteration_difference": max(abs(a - b) for a, b in zip(its, its_ref)),
+                        "max_rel_err_vs_oracle": max(errs)}
+        lib.tfs_set_default_precision(TFS_FP64)
+        out[name] = row
+    out["timing"] = ("host wall clock around each tfs_bicg / tfs_cg call (value, b, x uploads and x, r1 "
+                     "read-back included; handle and graphs built in an untimed first pass) and around each "
+                     "oracle call on one host core")
     return out
 
 

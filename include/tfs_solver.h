@@ -90,6 +90,9 @@ typedef struct tfs_stats {
     int32_t  spmv_kernel;       /* SpMV kernel of the CG iterations: 0 direct,
                                    1 software-pipelined                        */
     int32_t  sell_width;        /* uniform SELL-32 slice width, 0 if per slice  */
+    int32_t  dic_kernel;        /* DIC application last launched: 0 level
+                                   kernels, 1 one-block (TFS_OPT_DIC_BLOCK)    */
+    int32_t  pad;
 } tfs_stats;
 
 /* ---- topology ----------------------------------------------------------- */
@@ -153,9 +156,23 @@ int tfs_set_default_precision(int mode);
 #define TFS_OPT_BWD_PRE      13  /* 1 backward level kernels compute their start
                                     values before the wait (default); 0         */
 #define TFS_OPT_DIC_BLOCK    14  /* 1 the whole DIC application (and Prec_Form)
-                                    in one thread block with the vector in
-                                    shared memory, where it fits (default); 0
-                                    the level kernels                           */
+                                    in one thread block, the vector in shared
+                                    memory and each level's rows staged there
+                                    ahead, where the vector and at least three
+                                    level slots fit (deep schedules of narrow
+                                    levels; default); 0 the level kernels       */
+
+/* One DIC application (the tfs_time_prec workload: factor from val, r = 1)
+ * with its level launches stamped on the device: for slot k (launch order)
+ * start_us[k] = when the launch's blocks passed their dependency wait
+ * (earliest) and end_us[k] = when they had finished (latest), in
+ * microseconds after the first stamp; kind[k] = the level of a forward
+ * launch, -1 - level of a backward one, 1 << 20 for the one-block tail.
+ * Level-kernel schedule only (TFS_ERR_ARG when the one-block DIC runs).
+ * Allocates the stamp buffer itself (a profiling call).  Replaces nothing
+ * in the reference. */
+int tfs_profile_prec(tfs_handle *h, const double *val, int mode, int max_slots, double *start_us,
+                     double *end_us, int32_t *kind, int32_t *n_slots);
 
 /* Set / read one option of a handle.  TFS_ERR_ARG for an unknown option or
  * value.  Replaces nothing in the reference. */

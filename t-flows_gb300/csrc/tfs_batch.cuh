@@ -12,8 +12,14 @@
 // alone and in any mix.
 //
 // Methods: CG and BiCG (A, not A^T, on the shadow system) with no or diagonal
-// preconditioning, in binary64 (the reference's per-row arithmetic) or mixed
-// precision (binary32 iteration, binary64 reliable updates, as tfs_mixed.cuh).
+// preconditioning, and CG (hence the reference's BiCG, whose iterates are
+// CG's) with DIC preconditioning: the factor (Prec_Form.f90:32-40) and both
+// triangular sweeps (Prec_Solve.f90:46-67) run level by level over the
+// system's DIC level schedule, the cluster's threads sharing each level's
+// rows and the cluster barrier between levels; every row keeps the
+// reference's arithmetic.  Binary64 (the reference's per-row arithmetic) or
+// mixed precision (binary32 iteration, binary64 reliable updates, as
+// tfs_mixed.cuh; the factor formed in binary64 and rounded once).
 #pragma once
 #include <cooperative_groups.h>
 
@@ -40,6 +46,8 @@ struct BatchSys {
     double tol;
     int niter_max;
     int prec;
+    const int *lvl_begin;     // DIC level schedule (prec 2): first row of every level, n_levels + 1
+    int n_levels;
     // outputs
     int niter_out, status, early, true_res;
     double ini_res, fin_res;
@@ -135,6 +143,74 @@ __device__ __forceinline__ AccT acc_fma(VT a, VT b, AccT c)
     else return fma((double)a, (double)b, c);
 }
 
+// DIC factor of one system (binary64, Prec_Form.f90:32-40): levels
+// ascending, the cluster's threads sharing each level's rows, the cluster
+// barrier between levels (its release/acquire makes every CTA's stores
+// visible; gathers read past L1).
+__device__ void batch_dic_form(const SellDev &A, const double *val, double *d, const int *lvl_begin, int nl,
+                               int gtid, int stride, cg::cluster_group &cl)
+{
+    for (int l = 0; l < nl; l++) {
+        const int r1 = __ldg(lvl_begin + l + 1);
+        for (int i = __ldg(lvl_begin + l) + gtid; i < r1; i += stride) {
+            const RowGeom g = row_geom(A, i);
+            if (g.len == 0) { d[i] = 1.0; continue; }
+            double s = __ldg(val + g.off + (g.dpos << 5));
+            for (int j = 0; j < g.dpos; j++) {
+                const int ee = g.off + (j << 5);
+                const double a = __ldg(val + ee);
+                s = s - __ldcg(d + __ldg(A.col + ee)) * a * a;
+            }
+            d[i] = 1.0 / s;
+        }
+        cl.sync();
+    }
+}
+
+// z = M^-1 r with the DIC factor d (Prec_Solve.f90:46-67): forward sweep
+// into y, levels ascending, then y / (D + TINY) and the backward sweep into
+// z, levels descending; returns the thread's partial of (r, z).  r must be
+// complete (a cluster barrier after its stores).
+template <typename VT, typename AccT>
+__device__ AccT batch_dic_apply(const SellDev &A, const VT *val, const VT *d, const VT *r, VT *y, VT *z,
+                                const int *lvl_begin, int nl, int gtid, int stride, cg::cluster_group &cl)
+{
+    for (int l = 0; l < nl; l++) {
+        const int r1 = __ldg(lvl_begin + l + 1);
+        for (int i = __ldg(lvl_begin + l) + gtid; i < r1; i += stride) {
+            const RowGeom g = row_geom(A, i);
+            if (g.len == 0) { y[i] = (VT)0; continue; }
+            VT s = __ldcg(r + i);
+            for (int j = 0; j < g.dpos; j++) {
+                const int ee = g.off + (j << 5);
+                s = s - __ldg(val + ee) * __ldcg(y + __ldg(A.col + ee));
+            }
+            y[i] = s * __ldcg(d + i);
+        }
+        cl.sync();
+    }
+    AccT rz = (AccT)0;
+    for (int l = nl - 1; l >= 0; l--) {
+        const int r1 = __ldg(lvl_begin + l + 1);
+        for (int i = __ldg(lvl_begin + l) + gtid; i < r1; i += stride) {
+            const RowGeom g = row_geom(A, i);
+            if (g.len == 0) { z[i] = (VT)0; continue; }
+            const VT di = __ldcg(d + i);
+            VT s = __ldcg(y + i) / (di + (VT)TINY);
+            for (int j = g.dpos + 1; j < g.len; j++) {
+                const int ee = g.off + (j << 5);
+                s = s - __ldg(val + ee) * __ldcg(z + __ldg(A.col + ee));
+            }
+            const VT zi = s * di;
+            z[i] = zi;
+            if constexpr (sizeof(AccT) == 4) rz = fmaf((float)__ldcg(r + i), (float)zi, rz);
+            else rz = fma((double)__ldcg(r + i), (double)zi, rz);
+        }
+        cl.sync();
+    }
+    return rz;
+}
+
 template <int METHOD, typename VT>
 __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_part)[4], int &parity)
 {
@@ -153,6 +229,11 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
     const double tol = S.tol;
     const int niter_max = S.niter_max;
     const bool diag = S.prec == 1;
+    // METHOD 2: the CG sequence with DIC preconditioning (its own instance,
+    // so that the DIC sweeps add no registers to the other kernels)
+    constexpr bool dic = METHOD == 2;
+    VT *yT;
+    if constexpr (MIXED) yT = F.y; else yT = V.y;
 
     // b, x0 in internal order, d, ||b|| (Cg.f90:48-58).  The values were
     // gathered into SELL order by k_batch_gather before this launch.
@@ -171,6 +252,12 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         double di = (diag && g.len > 0) ? S.val[g.off + (g.dpos << 5)] : 1.0;
         V.d[i] = di;
         if (MIXED) { F.d[i] = (float)di; F.e[i] = 0.f; }
+    }
+    if (dic) {
+        cl.sync();
+        batch_dic_form(A, S.val, V.d, S.lvl_begin, S.n_levels, gtid, stride, cl);
+        if (MIXED)
+            for (int i = gtid; i < n_int; i += stride) F.d[i] = (float)__ldcg(V.d + i);
     }
     {
         const double a1[1] = {acc[0]};
@@ -194,8 +281,10 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
             double r = row_accum<true, double, double, double, false, 4>(V.u1[i], A.col, S.val, V.x, g.off, 0, g.len);
             V.r[i] = r;
             e2 = fma(r, r, e2);
-            VT rT = (VT)r, dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
+            VT rT = (VT)r;
             if (MIXED) W.r[i] = rT;
+            if (dic) continue;   // z and (r, z) from the sweeps below
+            VT dT = MIXED ? (VT)F.d[i] : (VT)V.d[i];
             VT z = rT / dT;
             W.z[i] = z;
             if (METHOD == 1) {
@@ -210,6 +299,11 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
     };
     double e2, rz;
     true_residual(true, e2, rz);
+    if (dic) {
+        cl.sync();
+        rz = (double)batch_dic_apply<VT, double>(A, valT, MIXED ? (const VT *)F.d : (const VT *)V.d, W.r, yT, W.z,
+                                                 S.lvl_begin, S.n_levels, gtid, stride, cl);
+    }
     const double a2[2] = {e2, rz};
     double v2[2];
     cluster_sum<2>(a2, v2, s_part, parity, cl);
@@ -229,7 +323,9 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
         for (int i0 = gtid; i0 < n_int; i0 += 2 * stride) {
             const int i1 = i0 + stride;
             const bool ok1 = i1 < n_int;
-            VT z0 = W.z[i0], p0 = W.p[i0], z1 = ok1 ? W.z[i1] : (VT)0, p1 = ok1 ? W.p[i1] : (VT)0;
+            // z past L1: with DIC other threads of the cluster wrote it
+            VT z0 = __ldcg(W.z + i0), p0 = W.p[i0], z1 = ok1 ? __ldcg(W.z + i1) : (VT)0,
+               p1 = ok1 ? W.p[i1] : (VT)0;
             VT a0 = (VT)0, b0 = (VT)0, a1 = (VT)0, b1 = (VT)0;
             if (METHOD == 1) {
                 a0 = W.z2[i0]; b0 = W.p2[i0];
@@ -320,12 +416,18 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
                     else V.x[i] = xv[q] + alfa * (double)pv[q];
                     VT r1 = rv[q] - alfaT * qv[q];
                     W.r[i] = r1;
+                    e2a = acc_fma(r1, r1, e2a);
+                    if (dic) continue;
                     VT z1 = r1 / dv[q];
                     W.z[i] = z1;
-                    e2a = acc_fma(r1, r1, e2a);
                     rza = acc_fma(r1, z1, rza);
                 }
             }
+        }
+        if (dic) {
+            cl.sync();
+            rza = batch_dic_apply<VT, AccT>(A, valT, MIXED ? (const VT *)F.d : (const VT *)V.d, W.r, yT, W.z,
+                                            S.lvl_begin, S.n_levels, gtid, stride, cl);
         }
         const AccT a3[2] = {e2a, rza};
         double v3[2];
@@ -340,6 +442,11 @@ __device__ void batch_solve_one(BatchSys &S, cg::cluster_group &cl, double (*s_p
             }
             cl.sync();
             true_residual(false, e2, rz);
+            if (dic) {
+                cl.sync();
+                rz = (double)batch_dic_apply<VT, double>(A, valT, MIXED ? (const VT *)F.d : (const VT *)V.d, W.r,
+                                                         yT, W.z, S.lvl_begin, S.n_levels, gtid, stride, cl);
+            }
             const double a4[2] = {e2, rz};
             double v4[2];
             cluster_sum<2>(a4, v4, s_part, parity, cl);

@@ -1,135 +1,209 @@
 // tfs_dic_block.cuh -- a whole DIC preconditioner application (or the DIC
-// recurrence of Prec_Form) in one thread block, for systems whose vector fits
-// in shared memory.
+// recurrence of Prec_Form) in one thread block, for systems with deep level
+// schedules of narrow levels whose vector fits in shared memory.
 //
 // The meshes T-FlowS ships are small and, in their own cell numbering, have
-// deep level schedules (the 14,490-cell plain_50 mesh: 148 levels of about
-// 100 rows).  Launched level by level, or level-looped through global memory
+// deep level schedules (the 14,490-cell plain_50 mesh: 148 levels of at most
+// 149 rows).  Launched level by level, or level-looped through global memory
 // in one block, each of the ~300 dependent level steps of an application
 // costs three L2 round trips (row geometry, entries, gathers of rows written
-// one step earlier by other threads) -- about 1.8 us.  Here the swept vector
-// lives in shared memory (one binary64 or binary32 value per row, in place:
-// y, then y / (D + TINY), then z), so the gathers of a step are shared-memory
-// loads; the rows' geometry, entries, diagonal and right-hand side are pulled
-// into L1 by prefetches issued DICB_AHEAD levels before the level runs (each
-// level's rows are contiguous SELL slices, so a level is three contiguous
-// ranges), and a step costs its L1 hits, its shared-memory gathers, the
-// row's arithmetic and one __syncthreads.
+// one step earlier by other threads): about 1.7 us.  Here:
+//   - the swept vector lives in shared memory (one value per row, in place:
+//     y, then y / (D + TINY), then z), so a step's gathers are shared-memory
+//     loads;
+//   - each level's rows -- their SELL slices of column indices and values,
+//     geometry, diagonal and (forward) right-hand side, contiguous in global
+//     memory because levels start on slice boundaries -- are staged into a
+//     ring of R shared-memory slots by 16-byte cp.async copies issued R - 1
+//     levels before the level runs, so a step waits for no global load;
+//   - a step is then one cp.async group wait, one __syncthreads, the row's
+//     shared-memory loads and arithmetic.
+// L1 prefetches in place of the ring measured slower than no prefetch at all
+// (plain_50 binary64: 529 against 402 us per application).
 //
 // Every row does exactly sweep_row's arithmetic (the reference's order of
 // terms: Prec_Solve.f90:46-67, Prec_Form.f90:32-40), so the results are
-// bitwise those of the per-level schedule.
+// bitwise those of the per-level schedule.  Every copy is a 16-byte aligned
+// cp.async of the block's own, in-bounds data and every wait is on the
+// thread's own copies: no wait depends on another block.
 #pragma once
+#include <type_traits>
+
 #include "tfs_kernels.cuh"
 
 namespace tfs {
 
-#define TFS_DICB_TPB 1024
-#ifndef DICB_AHEAD
-#define DICB_AHEAD 4
-#endif
+#define TFS_DICB_TPB 512
+#define TFS_DICB_MAX_SLOTS 8
 
-__device__ __forceinline__ void prefetch_l1(const void *p)
+// Byte offsets inside one ring slot of `rm` rows (rm a multiple of 32, so
+// every part starts on a 16-byte boundary): geometry, diagonal, right-hand
+// side, column indices and values of up to rm rows of one level.
+struct DicbSlot {
+    int rm, off_d, off_b, off_col, off_val, bytes;
+};
+
+template <typename T>
+__host__ __device__ inline DicbSlot dicb_slot(int rm, int W)
 {
-    asm volatile("prefetch.global.L1 [%0];" : : "l"(p));
+    DicbSlot s;
+    s.rm = rm;
+    s.off_d = rm * 4;
+    s.off_b = s.off_d + rm * (int)sizeof(T);
+    s.off_col = s.off_b + rm * (int)sizeof(T);
+    s.off_val = s.off_col + rm * W * 4;
+    s.bytes = s.off_val + rm * W * (int)sizeof(T);
+    return s;
 }
 
-// L1 prefetch of everything level l's rows read from global memory: their
-// SELL entries (column indices and values), geometry, diagonal and (forward)
-// right-hand side.  Levels start and end on slice boundaries (32 rows).
-template <typename T, int MODE>
-__device__ __forceinline__ void prefetch_level(const SellDev &A, const T *val, const T *d, const T *b,
-                                               const int *lvl_begin, int l)
+// Shared memory of the vector (n_rows values of T), rounded to 128 bytes.
+template <typename T>
+__host__ __device__ inline int dicb_vec_bytes(int n_rows)
 {
-    const int r0 = __ldg(lvl_begin + l), r1 = __ldg(lvl_begin + l + 1);
-    if (r1 <= r0) return;
-    const int e0 = A.width ? r0 * A.width : __ldg(A.slice_off + (r0 >> 5));
-    const int e1 = A.width ? r1 * A.width : __ldg(A.slice_off + (r1 >> 5));
-    const int tid = threadIdx.x;
-    for (int e = e0 + tid * 32; e < e1; e += TFS_DICB_TPB * 32) prefetch_l1(A.col + e);
-    for (int e = e0 + tid * (128 / (int)sizeof(T)); e < e1; e += TFS_DICB_TPB * (128 / (int)sizeof(T)))
-        prefetch_l1(val + e);
-    for (int i = r0 + tid * 32; i < r1; i += TFS_DICB_TPB * 32) prefetch_l1(A.rowinfo + i);
-    if (MODE != 2)
-        for (int i = r0 + tid * (128 / (int)sizeof(T)); i < r1; i += TFS_DICB_TPB * (128 / (int)sizeof(T))) {
-            prefetch_l1(d + i);
-            if (MODE == 0) prefetch_l1(b + i);
+    return (n_rows * (int)sizeof(T) + 127) & ~127;
+}
+
+__device__ __forceinline__ uint32_t dicb_smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void dicb_cp16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" : : "r"(dicb_smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void dicb_commit()
+{
+    asm volatile("cp.async.commit_group;" : : : "memory");
+}
+
+// Wait until at most n of the thread's committed copy groups are pending.
+__device__ __forceinline__ void dicb_wait(int n)
+{
+    switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;" : : : "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" : : : "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" : : : "memory"); break;
+    case 3: asm volatile("cp.async.wait_group 3;" : : : "memory"); break;
+    case 4: asm volatile("cp.async.wait_group 4;" : : : "memory"); break;
+    case 5: asm volatile("cp.async.wait_group 5;" : : : "memory"); break;
+    case 6: asm volatile("cp.async.wait_group 6;" : : : "memory"); break;
+    default: asm volatile("cp.async.wait_group 7;" : : : "memory"); break;
+    }
+}
+
+// Stage level l's rows into `slot` (every thread its share of 16-byte
+// chunks).  PART 0: forward (geometry, d, b, entries); 1: backward (no b);
+// 2: the recurrence (geometry and entries only).
+template <typename T, int PART>
+__device__ __forceinline__ void dicb_stage(unsigned char *slot, const DicbSlot &L, const SellDev &A,
+                                           const T *val, const T *d, const T *b, const int *lvl_begin, int l)
+{
+    const int r0 = __ldg(lvl_begin + l), nr = __ldg(lvl_begin + l + 1) - r0;
+    const int W = A.width;
+    auto copy = [&](unsigned char *dst, const void *src, int bytes) {
+        for (int o = (int)threadIdx.x * 16; o < bytes; o += TFS_DICB_TPB * 16)
+            dicb_cp16(dst + o, (const unsigned char *)src + o);
+    };
+    copy(slot, A.rowinfo + r0, nr * 4);
+    if (PART != 2) copy(slot + L.off_d, d + r0, nr * (int)sizeof(T));
+    if (PART == 0) copy(slot + L.off_b, b + r0, nr * (int)sizeof(T));
+    copy(slot + L.off_col, A.col + (size_t)r0 * W, nr * W * 4);
+    copy(slot + L.off_val, val + (size_t)r0 * W, nr * W * (int)sizeof(T));
+}
+
+// One sweep of k_dic_block over all levels, ascending (DIR > 0) or
+// descending, through the ring of R slots.
+template <typename T, int PART, int DIR>
+__device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
+                                           const T *val, const T *d, const T *b, const int *lvl_begin,
+                                           int n_levels)
+{
+    const int tid = threadIdx.x, W = A.width;
+    auto level_at = [&](int q) { return DIR > 0 ? q : n_levels - 1 - q; };
+    int staged = 0;
+    for (; staged < R - 1 && staged < n_levels; staged++) {
+        dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lvl_begin, level_at(staged));
+        dicb_commit();
+    }
+    for (int q = 0; q < n_levels; q++) {
+        dicb_wait(staged - q - 1);   // this thread's copies of level q
+        __syncthreads();             // everyone's copies; level q - 1 done, its slot free
+        if (staged < n_levels) {
+            dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lvl_begin,
+                                level_at(staged));
+            dicb_commit();
+            staged++;
         }
+        const unsigned char *slot = ring + (size_t)(q % R) * L.bytes;
+        const uint32_t *sinfo = reinterpret_cast<const uint32_t *>(slot);
+        const T *sd = reinterpret_cast<const T *>(slot + L.off_d);
+        const T *sb = reinterpret_cast<const T *>(slot + L.off_b);
+        const int *scol = reinterpret_cast<const int *>(slot + L.off_col);
+        const T *sval = reinterpret_cast<const T *>(slot + L.off_val);
+        const int l = level_at(q);
+        const int r0 = __ldg(lvl_begin + l), nr = __ldg(lvl_begin + l + 1) - r0;
+        for (int k = tid; k < nr; k += TFS_DICB_TPB) {
+            const uint32_t info = sinfo[k];
+            const int len = (int)(info & 0xffffu), dpos = (int)(info >> 16);
+            const int e0 = (k & ~31) * W + (k & 31);   // entry j at e0 + 32 j
+            const int i = r0 + k;
+            if (PART == 2) {
+                if (len == 0) { s[i] = (T)1; continue; }
+                T acc = sval[e0 + (dpos << 5)];
+                for (int j = 0; j < dpos; j++) {
+                    const T a = sval[e0 + (j << 5)];
+                    acc = acc - s[scol[e0 + (j << 5)]] * a * a;
+                }
+                s[i] = (T)1 / acc;
+            } else if (PART == 0) {
+                if (len == 0) { s[i] = (T)0; continue; }
+                T acc = sb[k];
+                for (int j = 0; j < dpos; j++) acc = acc - sval[e0 + (j << 5)] * s[scol[e0 + (j << 5)]];
+                s[i] = acc * sd[k];
+            } else {
+                if (len == 0) continue;   // 0 since the forward sweep
+                T acc = s[i];
+                for (int j = dpos + 1; j < len; j++) acc = acc - sval[e0 + (j << 5)] * s[scol[e0 + (j << 5)]];
+                s[i] = acc * sd[k];
+            }
+        }
+    }
+    dicb_wait(0);
+    __syncthreads();
 }
 
 // MODE 0: z = M^-1 b (forward sweep, scaling, backward sweep) with the
-// factor d; MODE 2: the DIC factor d from the matrix (binary64 only; b and z
-// unused).  One block of TFS_DICB_TPB threads; dynamic shared memory holds
-// lvl_begin[n_levels] values of T.  Rows past lvl_begin[n_levels] (the
-// layout's final padding) are never touched.
+// factor d; MODE 2: the DIC factor d from the matrix (binary64; b and z
+// unused).  One block of TFS_DICB_TPB threads on a uniform-width SELL
+// matrix; dynamic shared memory: the vector (dicb_vec_bytes) and R slots of
+// L.bytes.  Rows past lvl_begin[n_levels] (the layout's final padding) are
+// never touched.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(TFS_DICB_TPB, 1)
 k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const int *__restrict__ lvl_begin,
-            int n_levels, DevState *st)
+            int n_levels, DicbSlot L, int R, DevState *st)
 {
-    extern __shared__ __align__(16) unsigned char dicb_smem[];
+    extern __shared__ __align__(128) unsigned char dicb_smem[];
+    const int n_rows = __ldg(lvl_begin + n_levels);
     T *s = reinterpret_cast<T *>(dicb_smem);
+    unsigned char *ring = dicb_smem + dicb_vec_bytes<T>(n_rows);
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
     if (st->done) return;
     if (MODE == 0 && tid == 0) st->t_sweep0 = gtimer();
-    const int n_rows = __ldg(lvl_begin + n_levels);
-    for (int q = 0; q < DICB_AHEAD && q < n_levels; q++) prefetch_level<T, MODE>(A, val, d, b, lvl_begin, q);
-    // Forward sweep (or the recurrence), levels ascending.
-    for (int l = 0; l < n_levels; l++) {
-        if (l + DICB_AHEAD < n_levels) prefetch_level<T, MODE>(A, val, d, b, lvl_begin, l + DICB_AHEAD);
-        const int r1 = __ldg(lvl_begin + l + 1);
-        for (int i = __ldg(lvl_begin + l) + tid; i < r1; i += TFS_DICB_TPB) {
-            const RowGeom g = row_geom(A, i);
-            if (g.len == 0) {
-                s[i] = MODE == 2 ? (T)1 : (T)0;
-                continue;
-            }
-            if (MODE == 2) {
-                T acc = __ldg(val + g.off + (g.dpos << 5));
-                for (int j = 0; j < g.dpos; j++) {
-                    const int ee = g.off + (j << 5);
-                    const T a = __ldg(val + ee);
-                    acc = acc - s[__ldg(A.col + ee)] * a * a;
-                }
-                s[i] = (T)1 / acc;
-            } else {
-                T acc = __ldg(b + i);
-                for (int j = 0; j < g.dpos; j++) {
-                    const int ee = g.off + (j << 5);
-                    acc = acc - __ldg(val + ee) * s[__ldg(A.col + ee)];
-                }
-                s[i] = acc * __ldg(d + i);
-            }
-        }
-        __syncthreads();
-    }
     if (MODE == 2) {
+        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
         for (int i = tid; i < n_rows; i += TFS_DICB_TPB) d[i] = s[i];
         return;
     }
+    dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
     // Every row's backward start value y_i / (D_i + TINY) (Prec_Solve.f90:55-57).
     for (int i = tid; i < n_rows; i += TFS_DICB_TPB)
         if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
-    for (int q = 0; q < DICB_AHEAD && q < n_levels; q++)
-        prefetch_level<T, 1>(A, val, d, b, lvl_begin, n_levels - 1 - q);
     __syncthreads();
-    // Backward sweep, levels descending (Prec_Solve.f90:60-67).
-    for (int l = n_levels - 1; l >= 0; l--) {
-        if (l - DICB_AHEAD >= 0) prefetch_level<T, 1>(A, val, d, b, lvl_begin, l - DICB_AHEAD);
-        const int r1 = __ldg(lvl_begin + l + 1);
-        for (int i = __ldg(lvl_begin + l) + tid; i < r1; i += TFS_DICB_TPB) {
-            const RowGeom g = row_geom(A, i);
-            if (g.len == 0) continue;   // s[i] = 0 since the forward sweep
-            T acc = s[i];
-            for (int j = g.dpos + 1; j < g.len; j++) {
-                const int ee = g.off + (j << 5);
-                acc = acc - __ldg(val + ee) * s[__ldg(A.col + ee)];
-            }
-            s[i] = acc * __ldg(d + i);
-        }
-        __syncthreads();
-    }
+    dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
     for (int i = tid; i < n_rows; i += TFS_DICB_TPB) z[i] = s[i];
 }
 

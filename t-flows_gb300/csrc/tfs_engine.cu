@@ -132,6 +132,10 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
         const int bs = h->level_tpb;
         const int nb = (r1 - r0 + bs - 1) / bs;
         cudaError_t e;
+        if (h->profiling && MODE != 2) {
+            h->stamp_kind.push_back(MODE == 0 ? l : -1 - l);
+            first = (first & 1) | (h->stamp_next++ << 1);
+        }
         if ((MODE == 1 || MODE == 0) && prey) {
             // Backward levels after a tail that releases them only past its
             // own wait: start values computed before the dependency wait;
@@ -153,7 +157,7 @@ static int launch_levels(tfs_handle *h, cudaStream_t s, const T *val, T *d, cons
         else
             e = launch_ex(pdl, k_sweep_level<T, NR, MODE, 256>, nb, bs, s, A, val, d, b1, b2, o1, o2, y1, y2, r0, r1, h->st, first);
         if (e != cudaSuccess) return tfs_engine_error(e, "level launch");
-        first = 0;
+        first = 0;   // (and slot 0: stamps are recorded only while profiling)
         (*count)++;
     }
     if (MODE != 1) {
@@ -570,15 +574,30 @@ static int build_layout(tfs_handle *h, int kind)
         }
         h->pf_tail_level = l;
         h->pf_ok = l < nl && l <= h->tail_level;
-        // One-block DIC: the swept vector (every row of the levels) in the
-        // block's shared memory.
-        h->dicb_bytes64 = h->dicb_bytes32 = 0;
-        if (kind == TFS_LAYOUT_LEVELS) {
+        // One-block DIC: the swept vector (every row of the levels) and a
+        // ring of at least 3 (at most TFS_DICB_MAX_SLOTS) level slots of the
+        // widest level's rows in the block's shared memory; uniform slice
+        // width only (the staged slices are then contiguous).
+        h->dicb_bytes64 = h->dicb_bytes32 = h->dicb_slots64 = h->dicb_slots32 = h->dicb_rm = 0;
+        if (kind == TFS_LAYOUT_LEVELS && h->sell_width > 0) {
             int optin = 0;
             CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+            int rm = 32;
+            for (int l = 0; l < nl; l++) rm = std::max(rm, h->lvl_begin[l + 1] - h->lvl_begin[l]);
             const int64_t rows = h->lvl_begin[nl];
-            if (rows * 8 <= optin) h->dicb_bytes64 = (int)((rows * 8 + 15) & ~15ll);
-            if (rows * 4 <= optin) h->dicb_bytes32 = (int)((rows * 4 + 15) & ~15ll);
+            h->dicb_rm = rm;
+            auto fit = [&](int vec, int slot, int *bytes, int *slots) {
+                if (rows > INT32_MAX / 16) return;
+                const int64_t room = (int64_t)optin - vec;
+                const int64_t r = room > 0 ? std::min<int64_t>(TFS_DICB_MAX_SLOTS, room / slot) : 0;
+                if (r < 3) return;
+                *slots = (int)r;
+                *bytes = vec + (int)r * slot;
+            };
+            fit(dicb_vec_bytes<double>((int)rows), dicb_slot<double>(rm, h->sell_width).bytes, &h->dicb_bytes64,
+                &h->dicb_slots64);
+            fit(dicb_vec_bytes<float>((int)rows), dicb_slot<float>(rm, h->sell_width).bytes, &h->dicb_bytes32,
+                &h->dicb_slots32);
             static std::once_flag attr_once;
             std::call_once(attr_once, [optin] {
                 cudaFuncSetAttribute(k_dic_block<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -801,7 +820,9 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
     if (const int bytes = dic_block_bytes<double>(h)) {
         k_dic_block<double, 2><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), h->val, h->v.d, nullptr, nullptr,
-                                                              h->d_lvl_begin, h->n_levels, h->st);
+                                                              h->d_lvl_begin, h->n_levels,
+                                                              dicb_slot<double>(h->dicb_rm, h->sell_width),
+                                                              h->dicb_slots64, h->st);
         return 1;
     }
     int cnt = 0;
@@ -869,25 +890,34 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     else { val = (const T *)h->val32; d = (T *)h->f.d; }
     if (nr == 1 && !fuse_l0) {
         if (const int bytes = dic_block_bytes<T>(h)) {
-            k_dic_block<T, 0><<<1, TFS_DICB_TPB, bytes, s>>>(A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, h->st);
+            k_dic_block<T, 0><<<1, TFS_DICB_TPB, bytes, s>>>(
+                A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, dicb_slot<T>(h->dicb_rm, h->sell_width),
+                sizeof(T) == 8 ? h->dicb_slots64 : h->dicb_slots32, h->st);
+            h->dicb_used = 1;
             (*count)++;
             CKL("one-block DIC launch");
             return TFS_OK;
         }
     }
     // Forward levels, both tails in one block, backward levels.
+    h->dicb_used = 0;
     int rc;
     const int tail_at = sweep_tail_at(h, nr);
     const bool tails = tail_at < h->n_levels;
     auto tail2 = [&](auto kernel) -> int {
         if (!tails) return TFS_OK;
         cudaError_t e;
+        int slot = 0;
+        if (h->profiling) {
+            h->stamp_kind.push_back(1 << 20);
+            slot = h->stamp_next++;
+        }
         if (pf_tail(h, nr))
             e = launch_ex(h->use_pdl != 0, k_sweep_tail1<T>, 1, TFS_SWEEP_TPB, s, A, val, (const T *)d, b1,
-                          y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+                          y1, z1, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st, slot);
         else
             e = launch_ex(h->use_pdl != 0, kernel, 1, TFS_SWEEP_TPB, s, A, val, d, b1, b2, y1, y2, z1,
-                          z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st);
+                          z2, (const int *)h->d_lvl_begin, tail_at, h->n_levels, h->st, slot);
         (*count)++;
         return e == cudaSuccess ? TFS_OK : tfs_engine_error(e, "tail launch");
     };
@@ -1529,6 +1559,7 @@ extern "C" int tfs_get_stats(const tfs_handle *h, tfs_stats *out)
     *out = h->stats;
     out->spmv_kernel = h->spmv_kind;
     out->sell_width = h->sell_width;
+    out->dic_kernel = h->dicb_used;
     return TFS_OK;
 }
 
@@ -1603,6 +1634,72 @@ extern "C" int tfs_time_prec(tfs_handle *h, const double *val, int mode, int rep
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
     *ms = (double)t / reps;
+    return TFS_OK;
+}
+
+// One DIC application with every sweep launch stamped: for each launch
+// ("slot", in launch order) the global timer after its blocks' dependency
+// waits (earliest) and at their ends (latest), relative to the first stamp.
+// The kernels and the schedule are those of tfs_time_prec; the stamps add
+// one load of the state and, per block, one barrier and two stores.
+extern "C" int tfs_profile_prec(tfs_handle *h, const double *val, int mode, int max_slots, double *start_us,
+                                double *end_us, int32_t *kind, int32_t *n_slots)
+{
+    if (!h || !val || !start_us || !end_us || !kind || !n_slots || max_slots < 1 ||
+        (mode != TFS_FP64 && mode != TFS_MIXED))
+        return TFS_ERR_ARG;
+    double ms = 0.0;
+    int rc = tfs_time_prec(h, val, mode, 3, &ms);   // factor formed, warm
+    if (rc) return rc;
+    if (h->dicb_used) {
+        tfs_set_error_text("tfs_profile_prec: the one-block DIC has no level launches to stamp");
+        return TFS_ERR_ARG;
+    }
+    cudaStream_t s = h->stream;
+    int max_blocks = 1;
+    for (int l = 0; l < h->n_levels; l++)
+        max_blocks = std::max(max_blocks, (h->lvl_begin[l + 1] - h->lvl_begin[l] + h->level_tpb - 1) / h->level_tpb);
+    const int stride = 2 * max_blocks, slots = 2 * h->n_levels + 2;
+    unsigned long long *d_stamps = nullptr;
+    CK(cudaMalloc(&d_stamps, sizeof(unsigned long long) * (size_t)stride * slots));
+    CK(cudaMemsetAsync(d_stamps, 0, sizeof(unsigned long long) * (size_t)stride * slots, s));
+    CK(cudaMemcpyAsync(&h->st->stamps, &d_stamps, sizeof d_stamps, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(&h->st->stamp_stride, &stride, sizeof stride, cudaMemcpyHostToDevice, s));
+    h->profiling = true;
+    h->stamp_next = 0;
+    h->stamp_kind.clear();
+    int count = 0;
+    if (mode == TFS_FP64)
+        rc = launch_sweeps<double>(h, s, 1, h->v.r, nullptr, h->v.y, nullptr, h->v.z, nullptr, &count);
+    else
+        rc = launch_sweeps<float>(h, s, 1, h->f.r, nullptr, h->f.y, nullptr, h->f.z, nullptr, &count);
+    h->profiling = false;
+    std::vector<unsigned long long> host((size_t)stride * slots);
+    const unsigned long long *null_ptr = nullptr;
+    cudaError_t e = cudaMemcpyAsync(host.data(), d_stamps, sizeof(unsigned long long) * host.size(),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h->st->stamps, &null_ptr, sizeof null_ptr, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_stamps);
+    if (rc) return rc;
+    if (e != cudaSuccess) return tfs_engine_error(e, "tfs_profile_prec");
+    const int n = std::min(h->stamp_next, max_slots);
+    unsigned long long t_ref = ~0ull;
+    std::vector<unsigned long long> lo(n, ~0ull), hi(n, 0ull);
+    for (int k = 0; k < n; k++)
+        for (int b = 0; b < max_blocks; b++) {
+            const unsigned long long a = host[(size_t)k * stride + 2 * b], z = host[(size_t)k * stride + 2 * b + 1];
+            if (!a) continue;
+            lo[k] = std::min(lo[k], a);
+            hi[k] = std::max(hi[k], z);
+        }
+    for (int k = 0; k < n; k++) t_ref = std::min(t_ref, lo[k]);
+    for (int k = 0; k < n; k++) {
+        start_us[k] = lo[k] == ~0ull ? -1.0 : (double)(lo[k] - t_ref) * 1e-3;
+        end_us[k] = hi[k] == 0ull ? -1.0 : (double)(hi[k] - t_ref) * 1e-3;
+        kind[k] = h->stamp_kind[k];
+    }
+    *n_slots = n;
     return TFS_OK;
 }
 
@@ -1878,12 +1975,25 @@ extern "C" int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mo
 {
     if (!b || !d_val || !d_x || !d_r1 || !niter || !tol || !niter_out || !ini_res || !fin_res || !status)
         return TFS_ERR_ARG;
-    if ((method != TFS_CG && method != TFS_BICG) || (prec != 0 && prec != 1) ||
+    if ((method != TFS_CG && method != TFS_BICG) || prec < 0 || prec > 2 ||
         (mode != TFS_FP64 && mode != TFS_MIXED)) {
-        tfs_set_error_text("batches run CG or BiCG with no or diagonal preconditioning");
+        tfs_set_error_text("batches run CG or BiCG with no, diagonal or DIC preconditioning");
+        return TFS_ERR_ARG;
+    }
+    // BiCG iterates equal CG's (see tfs_solve_launch): one sequence suffices
+    // unless the first system's handle asks for the literal two sequences,
+    // which the batch runs with no or diagonal preconditioning only.
+    if (method == TFS_BICG && !b->hs[0]->bicg_literal) method = TFS_CG;
+    if (method == TFS_BICG && prec == 2) {
+        tfs_set_error_text("the batch runs DIC with the CG sequence only (TFS_OPT_BICG = 0)");
         return TFS_ERR_ARG;
     }
     CK(cudaSetDevice(b->device));
+    if (prec == 2)
+        for (int k = 0; k < b->n; k++) {
+            int rc = ensure_layout(b->hs[k], 2);   // the DIC level schedule
+            if (rc) return rc;
+        }
     int64_t max_nnz = 0;
     for (int k = 0; k < b->n; k++) {
         tfs_handle *h = b->hs[k];
@@ -1904,6 +2014,8 @@ extern "C" int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mo
         S.tol = tol[k];
         S.niter_max = niter[k];
         S.prec = prec;
+        S.lvl_begin = h->d_lvl_begin;
+        S.n_levels = prec == 2 ? h->n_levels : 0;
         if (h->nnz_pad > max_nnz) max_nnz = h->nnz_pad;
     }
     CK(cudaMemcpyAsync(b->d_sys, b->h_sys, sizeof(BatchSys) * (size_t)b->n, cudaMemcpyHostToDevice, b->stream));
@@ -1914,10 +2026,10 @@ extern "C" int tfs_batch_solve_device(tfs_batch *b, int method, int prec, int mo
     k_batch_gather<<<dim3((unsigned)gx, (unsigned)b->n), 256, 0, b->stream>>>(b->d_sys, b->d_ctl, mode == TFS_MIXED);
     CKL("batch gather");
     int rc;
-    // BiCG iterates equal CG's (see tfs_solve_launch): one sequence suffices
-    // unless the first system's handle asks for the literal two sequences.
-    if (method == TFS_BICG && !b->hs[0]->bicg_literal) method = TFS_CG;
-    if (method == TFS_CG) rc = mode == TFS_MIXED ? launch_batch_kernel<0, float>(b) : launch_batch_kernel<0, double>(b);
+    if (method == TFS_CG && prec == 2)
+        rc = mode == TFS_MIXED ? launch_batch_kernel<2, float>(b) : launch_batch_kernel<2, double>(b);
+    else if (method == TFS_CG)
+        rc = mode == TFS_MIXED ? launch_batch_kernel<0, float>(b) : launch_batch_kernel<0, double>(b);
     else rc = mode == TFS_MIXED ? launch_batch_kernel<1, float>(b) : launch_batch_kernel<1, double>(b);
     if (rc) return rc;
     CK(cudaEventRecord(b->ev1, b->stream));

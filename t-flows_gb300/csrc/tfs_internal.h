@@ -59,6 +59,11 @@ struct DevState {
     // global timer (ns) at the start of the solve's first kernel and at the
     // start of its epilogue
     unsigned long long t_begin, t_end;
+    // tfs_profile_prec only (else null): per sweep launch ("slot") and block,
+    // the global timer after the block's dependency wait and at its end
+    unsigned long long *stamps;
+    int stamp_stride;      // entries per slot (2 per block)
+    int pad3;
 };
 
 // Per-call arguments, written by the host before every graph launch.
@@ -128,9 +133,15 @@ struct tfs_handle {
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
     int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC (vector in shared memory) where it fits
+    int dicb_used = 0;                 // the last DIC application launched was the one-block kernel
+    int dicb_rm = 0;                   // one-block DIC: rows of a ring slot (the widest level)
+    int dicb_slots64 = 0, dicb_slots32 = 0;   // ring slots that fit (0: not used for that arithmetic)
+    bool profiling = false;            // tfs_profile_prec: number the sweep launches
+    int stamp_next = 0;                // next slot number while profiling
+    std::vector<int> stamp_kind;       // per slot: level (forward), -1 - level (backward), 1 << 20 tail
     int pf_tail_level = 0;             // first level of the prefetching tail
     bool pf_ok = false;                // the prefetching tail can run
-    int dicb_bytes64 = 0, dicb_bytes32 = 0;   // shared memory of the one-block DIC, 0: does not fit
+    int dicb_bytes64 = 0, dicb_bytes32 = 0;   // shared memory of the one-block DIC, 0: not used
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row

@@ -481,6 +481,20 @@ k_residual(SellDev A, const double *__restrict__ val, Vec64 V, DevState *st, dou
 
 // ------------------------------------------------------ sweep rows
 
+// Profiling stamps of one block of a sweep launch (tfs_profile_prec): the
+// global timer after the dependency wait (t0) and once every thread of the
+// block is done.
+__device__ __forceinline__ void stamp_block(unsigned long long *stp, int stride, int slot,
+                                            unsigned long long t0)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long *q = stp + (size_t)slot * stride + 2 * blockIdx.x;
+        q[0] = t0;
+        q[1] = gtimer();
+    }
+}
+
 // One row of a sweep.  MODE 0: forward y = (b - L y) * D; MODE 1: backward
 // z = (y/(D+TINY) - U z) * D; MODE 2: DIC form D_i = 1/(a_ii - sum D_k a^2).
 // The first NP entries may come prefetched in kk/aa.  With skip (a finished
@@ -630,8 +644,10 @@ __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__r
 template <typename T, int NR, int MODE, int BS = TFS_TPB, bool PREY = false>
 __global__ void __launch_bounds__(BS)
 k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
-              T *o2, const T *y1, const T *y2, int row0, int row1, DevState *st, int first)
+              T *o2, const T *y1, const T *y2, int row0, int row1, DevState *st, int tag)
 {
+    // tag = first launch of the application | slot << 1 (profiling stamps)
+    const int first = tag & 1;
     const int i = row0 + blockIdx.x * BS + threadIdx.x;
     const bool active = i < row1;
     RowGeom g{0, 0, 0};
@@ -679,6 +695,8 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();
     const bool skip = st->done != 0;
+    unsigned long long *const stp = st->stamps;
+    const unsigned long long t0 = stp ? gtimer() : 0ull;
     if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
     if (MODE == 1 && PREY) {
         if (active) sweep_row_bwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
@@ -687,6 +705,7 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     } else if (active) {
         sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
     }
+    if (stp) stamp_block(stp, st->stamp_stride, tag >> 1, t0);
 }
 
 // Levels [l_begin, l_end) of a sweep in one block (descending for MODE 1);
@@ -746,13 +765,15 @@ k_sweep_tail(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b
 template <typename T, int NR>
 __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *y1, T *y2,
-              T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
+              T *z1, T *z2, const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st, int slot)
 {
     // The trigger follows the wait: the backward level kernels launched
     // after a tail read the forward sweep's output before their own wait.
     cudaGridDependencySynchronize();
     cudaTriggerProgrammaticLaunchCompletion();
     const bool skip = st->done != 0;
+    unsigned long long *const stp = st->stamps;
+    const unsigned long long t0 = stp ? gtimer() : 0ull;
     const int nl = l_end - l_begin;
     for (int q = 0; q < nl; q++) {
         const int lev = l_begin + q;
@@ -772,6 +793,7 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
         }
         __syncthreads();
     }
+    if (stp) stamp_block(stp, st->stamp_stride, slot, t0);
 }
 
 // Both tails by one block when the tail has at most TFS_SWEEP_TPB rows in
@@ -785,7 +807,7 @@ k_sweep_tail2(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
 template <typename T>
 __global__ void __launch_bounds__(TFS_SWEEP_TPB)
 k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y, T *z,
-              const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st)
+              const int *__restrict__ lvl_begin, int l_begin, int l_end, DevState *st, int slot)
 {
     const int i = __ldg(lvl_begin + l_begin) + (int)threadIdx.x;
     const bool mine = i < __ldg(lvl_begin + l_end);
@@ -811,6 +833,8 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
     cudaGridDependencySynchronize();
     cudaTriggerProgrammaticLaunchCompletion();   // after the wait, as in k_sweep_tail2
     const bool skip = st->done != 0;
+    unsigned long long *const stp = st->stamps;
+    const unsigned long long t0 = stp ? gtimer() : 0ull;
     T yi = (T)0;
     for (int l = l_begin; l < l_end; l++) {
         if (lev == l) {
@@ -844,6 +868,7 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
         }
         __syncthreads();
     }
+    if (stp) stamp_block(stp, st->stamp_stride, slot, t0);
 }
 
 // rho after the sweeps: CG (r, z) (Cg.f90:108-112); BiCG (z1, r2) (Bicg.f90:113-117).

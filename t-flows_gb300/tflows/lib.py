@@ -39,7 +39,8 @@ class tfs_stats(C.Structure):
     _fields_ = [("iterations", i32), ("true_residuals", i32), ("n_levels", i32), ("status", i32),
                 ("solve_ms", dbl), ("spmv_ns_total", dbl), ("spmv_launches", i64),
                 ("sweep_ns_total", dbl), ("sweep_launches", i64), ("kernel_launches", i64),
-                ("device_bytes", i64), ("spmv_kernel", i32), ("sell_width", i32)]
+                ("device_bytes", i64), ("spmv_kernel", i32), ("sell_width", i32),
+                ("dic_kernel", i32), ("pad", i32)]
 
 
 class tfs_result(C.Structure):
@@ -82,6 +83,7 @@ SIGNATURES = {
     "tfs_get_levels": (C.c_int, [P_void, P_i32]),
     "tfs_time_spmv": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
     "tfs_time_prec": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl]),
+    "tfs_profile_prec": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, P_dbl, P_dbl, P_i32, P_i32]),
     "tfs_autotune": (C.c_int, [P_void, P_dbl, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "tfs_faces_register": (C.c_int, [P_void, C.c_int32, P_i32, P_i32]),
     "tfs_assemble_faces_device": (C.c_int, [P_void, P_void, P_void, P_void, P_void, P_void, P_void]),

@@ -205,6 +205,22 @@ class Solver:
                 "spmv_ms": {"direct_sm8": t.spmv_ms[0], "direct_chunks": t.spmv_ms[1],
                             "pipe_sm8": t.spmv_pipe_ms[0], "pipe_chunks": t.spmv_pipe_ms[1]}}
 
+    def profile_prec(self, val: np.ndarray, mode: int = TFS_FP64) -> list[dict]:
+        """Device stamps of one DIC application's level launches
+        (tfs_profile_prec): per launch, when its blocks passed their
+        dependency wait and when they had finished (us)."""
+        m = 4 * max(1, self.stats()["n_levels"]) + 8
+        st, en = np.zeros(m), np.zeros(m)
+        kd, n = np.zeros(m, np.int32), _i32(0)
+        check(self.lib.tfs_profile_prec(self.h, ptr(_vec(val, self.nnz, "val"), _dbl), mode, m, ptr(st, _dbl),
+                                        ptr(en, _dbl), ptr(kd, _i32), C.byref(n)), "tfs_profile_prec")
+        out = []
+        for k in range(n.value):
+            kind = int(kd[k])
+            what = "tail" if kind == 1 << 20 else (f"fwd {kind}" if kind >= 0 else f"bwd {-1 - kind}")
+            out.append({"launch": what, "start_us": float(st[k]), "end_us": float(en[k])})
+        return out
+
     def time_prec(self, val: np.ndarray, mode: int = TFS_FP64, reps: int = 20) -> float:
         """Milliseconds per DIC preconditioner application (both sweeps)."""
         ms = _dbl(0.0)

@@ -101,3 +101,49 @@ def test_batch_semantics_small_b_and_limit(systems):
         rs = [s.b.copy() for s, _ in sel]
         res = b.solve(TFS_CG, 1, [s.val for s, _ in sel], xs, rs, 5, [1e-30, 1e-30])
         assert list(res.niter) == [6, 6]
+
+
+@pytest.mark.parametrize("method", [TFS_CG, TFS_BICG])
+def test_batch_dic_matches_oracle(method, systems):
+    """DIC in the batch (the factor and both triangular sweeps level by level
+    inside each system's cluster): binary64 within the parity gates of the
+    oracle's DIC solve (BiCG is the CG sequence), mixed precision converged
+    on the binary64 true residual within 1e-6 of the oracle."""
+    from helpers import iter_ok_mixed
+    sel = [t for t in systems if t[0].kind == POISSON]
+    for mode in (TFS_FP64, TFS_MIXED):
+        with Batch([sv for _, sv in sel], cluster=4, threads=256) as b:
+            xs, rs, res = _run(b, sel, method, 2, mode)
+        for k, (s, _) in enumerate(sel):
+            ref = oracle_solve(s, method, 2)
+            assert res.status[k] == 0
+            if mode == TFS_FP64:
+                assert iter_ok(int(res.niter[k]), ref["niter"]), (k, res.niter[k], ref["niter"])
+                assert rel_l2(xs[k], ref["x"]) <= SOL_REL
+                assert res.ini_res[k] == pytest.approx(ref["ini"], rel=1e-13)
+            else:
+                assert iter_ok_mixed(int(res.niter[k]), ref["niter"]), (k, res.niter[k], ref["niter"])
+                assert res.fin_res[k] < 1e-8 * np.linalg.norm(s.b)
+                assert rel_l2(xs[k], ref["x"]) < 1e-6
+
+
+def test_batch_dic_alone_equals_in_mix(systems):
+    """With DIC too a system's result does not depend on the rest of the
+    batch (bitwise)."""
+    sel = [t for t in systems if t[0].kind == POISSON]
+    target = sel[2]
+    with Batch([target[1]], cluster=8, threads=512) as b:
+        xa, ra, resa = _run(b, [target], TFS_CG, 2, TFS_FP64)
+    with Batch([sv for _, sv in sel], cluster=8, threads=512) as b:
+        xm, rm, resm = _run(b, sel, TFS_CG, 2, TFS_FP64)
+    assert np.array_equal(xa[0], xm[2]) and np.array_equal(ra[0], rm[2])
+    assert resa.niter[0] == resm.niter[2]
+
+
+def test_batch_literal_bicg_refuses_dic(systems):
+    from tflows.lib import TFS_OPT_BICG, TfsError
+    s, _ = systems[0]
+    with Solver(s.matrix(), options={TFS_OPT_BICG: 1}) as sv:
+        with Batch([sv], cluster=2, threads=128) as b:
+            with pytest.raises(TfsError):
+                b.solve(TFS_BICG, 2, [s.val], [np.zeros(s.n)], [s.b.copy()], 100, [1e-8])

@@ -133,12 +133,14 @@ def test_one_block_dic_on_reference_mesh(name, gpu):
                 if mode == TFS_FP64:
                     d = sol.prec_form(s.val, 2)
                     z = sol.prec_solve(s.val, 2, b)
+                    assert sol.stats()["dic_kernel"] == blk
                     assert np.array_equal(d, O.prec_form(s.n, s.row, s.col, s.dia, s.val, 2))
                     assert np.array_equal(z, O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
                     res += [d, z]
                 x, r = np.zeros(s.n), s.b.copy()
                 st = sol.solve(TFS_CG, s.val, x, r, 2, 5000, ref["tol"])
                 assert st.status == 0 and st.fin_res < ref["tol"]
+                assert sol.stats()["dic_kernel"] == blk
                 if mode == TFS_FP64:
                     assert iter_ok(st.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= SOL_REL
                 res += [x, r, st.niter, st.fin_res]

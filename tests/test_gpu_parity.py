@@ -572,6 +572,7 @@ def test_one_block_dic_bitwise(kind, shape, gpu):
             with Solver(s.matrix(), precision=mode, options={TFS_OPT_DIC_BLOCK: blk, TFS_OPT_FUSE_L0: 0}) as sol:
                 if mode == TFS_FP64:
                     res += [sol.prec_form(s.val, 2), sol.prec_solve(s.val, 2, b)]
+                    assert sol.stats()["dic_kernel"] == blk
                 for method in methods:
                     if mode == TFS_MIXED and method == TFS_CGS:
                         continue
@@ -586,3 +587,25 @@ def test_one_block_dic_bitwise(kind, shape, gpu):
     assert np.array_equal(out[1][1], O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
     for a, c in zip(out[1], out[0]):
         assert np.array_equal(a, c)
+
+
+def test_profile_prec_stamps_every_level_launch(gpu):
+    """tfs_profile_prec stamps one DIC application's launches in order:
+    forward levels ascending, the one-block tail, backward levels
+    descending, each with a start before its end; the stamps do not change
+    the application's result (Prec_Solve still equals the oracle)."""
+    from tflows.lib import TFS_OPT_DIC_BLOCK
+    s = system(POISSON, 40, 40, 40)
+    b = np.random.default_rng(2).uniform(-1, 1, s.n)
+    with Solver(s.matrix(), options={TFS_OPT_DIC_BLOCK: 0}) as sol:
+        prof = sol.profile_prec(s.val, TFS_FP64)
+        assert np.array_equal(sol.prec_solve(s.val, 2, b), O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+        nl = sol.stats()["n_levels"]
+    kinds = [p["launch"] for p in prof]
+    fwd = [int(k.split()[1]) for k in kinds if k.startswith("fwd")]
+    bwd = [int(k.split()[1]) for k in kinds if k.startswith("bwd")]
+    assert fwd == sorted(fwd) and fwd[0] == 0 and bwd == sorted(bwd, reverse=True) and bwd[-1] == 0
+    assert kinds.count("tail") == 1 and kinds.index("tail") == len(fwd)
+    assert len(fwd) < nl
+    for p in prof:
+        assert 0.0 <= p["start_us"] <= p["end_us"], p

@@ -221,3 +221,23 @@ def test_continuous_batching_requests_overlap_on_the_device(gpu):
     finally:
         for a in arrs:
             a.free()
+
+
+def test_wait_timeout_is_reported_and_the_ticket_survives(gpu):
+    """A wait that runs out reports TFS_ERR_TIMEOUT (TimeoutError here) with
+    the request still running; the same ticket can be waited for again and
+    gives the solve's result.  The limit is the host's: no device wait is
+    involved."""
+    s = system(POISSON, 48, 48, 48, seed=21)
+    a = DevArrays(s)
+    try:
+        with Server(1 << 34) as srv:
+            sid = srv.add_system(s.n, s.row, s.col, s.dia)
+            tol = 1e-8 * np.linalg.norm(s.b)
+            t = srv.submit(sid, TFS_CG, 2, a.p["val"], a.p["x"], a.p["r"], 2000, tol)
+            with pytest.raises(TimeoutError):
+                srv.wait(t, timeout_s=0.0)
+            res = srv.wait(t)
+        assert res["status"] == 0 and res["fin_res"] < tol
+    finally:
+        a.free()
