@@ -229,8 +229,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     s = tflows.SynthSystem(kind, nside, jitter=0.2, seed=BASE_SEED + dist.rank)
     log(f"[bench] system {desc}: n={s.n} nnz={s.nnz} ({time.perf_counter() - t0:.1f}s)")
     t0 = time.perf_counter()
-    from tflows.lib import TFS_OPT_LAUNCH
-    sol = tflows.Solver(s.matrix(), options={TFS_OPT_LAUNCH: 1 if args.eager else 0})
+    import tflows.lib as L
+    opts = {L.TFS_OPT_LAUNCH: 1 if args.eager else 0}
+    for kv in args.option:
+        name, value = kv.split("=")
+        opts[getattr(L, "TFS_OPT_" + name.upper())] = int(value)
+    sol = tflows.Solver(s.matrix(), options=opts)
     log(f"[bench] registered: {sol.stats()['n_levels']} levels ({time.perf_counter() - t0:.1f}s)")
     # Launch shapes of the single-solve kernels, picked on this system
     # (tfs_autotune) before anything is timed.
@@ -455,6 +459,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded jittered-hex mesh, random cell numbering, RHS U[-1,1])",
         "config": workload_config(args, n, nnz),
+        "options": {kv.split("=")[0]: int(kv.split("=")[1]) for kv in args.option} or None,
         "p50_ms": round(mixed["p50_ms"], 4), "p99_ms": round(mixed["p99_ms"], 4),
         "fp64": results.get("fp64"), "mixed": results.get("mixed"),
         "mixed_over_fp64": round(mixed["solves_per_s"] / fp64["solves_per_s"], 4),
@@ -1383,6 +1388,8 @@ def main(argv=None) -> int:
                     help="skip the device topology / assembly measurements")
     ap.add_argument("--modes", default="fp64,mixed",
                     help="arithmetic legs to run (profiling runs may pick one)")
+    ap.add_argument("--option", action="append", default=[], metavar="NAME=VALUE",
+                    help="a TFS_OPT_* option of the single-system solver, e.g. SPMV_REVERSE=0 (repeatable)")
     ap.add_argument("--eager", action="store_true",
                     help="launch the solve kernels from a host loop instead of a CUDA graph "
                          "(TFS_OPT_LAUNCH = 1), for kernel-level profiling")

@@ -186,21 +186,30 @@ static void spmv_kind_setup(tfs_handle *h)
                                                                                 : TFS_SPMV_DIRECT;
 }
 
-template <typename VT, bool MIXED>
-static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
+template <typename VT, bool MIXED, bool REV>
+static void launch_spmv_pipe_w(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
 {
     const SellDev A = sell_of(h);
     const int G = h->grid_spmv;
     switch (h->sell_width) {
-    case 1: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 1>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 2: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 2>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 3: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 3>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 4: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 4>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 5: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 5>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 6: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 6>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 7: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 7>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    default: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 8>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 1: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 1, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 2: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 2, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 3: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 3, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 4: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 4, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 5: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 5, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 6: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 6, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 7: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 7, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    default: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 8, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
     }
+}
+
+// The software-pipelined SpMV, its chunks walked last to first on the DIC
+// level layout (TFS_OPT_SPMV_REVERSE, default on there).
+template <typename VT, bool MIXED>
+static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
+{
+    if (h->spmv_reverse && h->layout == TFS_LAYOUT_LEVELS) launch_spmv_pipe_w<VT, MIXED, true>(h, s, val, p, q, pdl);
+    else launch_spmv_pipe_w<VT, MIXED, false>(h, s, val, p, q, pdl);
 }
 
 // q = A p, (p, q) and alpha of a CG iteration on stream s, binary32 (mixed)
@@ -767,6 +776,7 @@ static int *option_field(tfs_handle *h, int option, bool (**ok)(int))
     case TFS_OPT_FWD_PRE: return &h->fwd_pre;
     case TFS_OPT_BWD_PRE: return &h->bwd_pre;
     case TFS_OPT_DIC_BLOCK: return &h->dic_block;
+    case TFS_OPT_SPMV_REVERSE: return &h->spmv_reverse;
     default: return nullptr;
     }
 }

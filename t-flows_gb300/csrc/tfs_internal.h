@@ -130,6 +130,7 @@ struct tfs_handle {
     int sell_uniform = 1;              // TFS_OPT_SELL_UNIFORM: one slice width when it costs <= 5% padding
     int spmv_pref = 1;                 // TFS_OPT_SPMV: 1 software-pipelined where possible, 0 direct
     int spmv_chunks = 0;               // TFS_OPT_SPMV_GRID: 1 one block per 256-row chunk
+    int spmv_reverse = 1;              // TFS_OPT_SPMV_REVERSE: level-layout SpMV walks its chunks last to first
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
     int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC (vector in shared memory) where it fits

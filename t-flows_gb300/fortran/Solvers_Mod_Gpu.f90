@@ -58,6 +58,12 @@
     type(c_ptr) function tfs_last_error() bind(C, name="tfs_last_error")
       import :: c_ptr
     end function
+    ! TFS_FP64 = 0, TFS_MIXED = 1 for every later Cg / Bicg / Cgs call
+    integer(c_int) function tfs_set_default_precision(mode)                 &
+                                   bind(C, name="tfs_set_default_precision")
+      import :: c_int
+      integer(c_int), value :: mode
+    end function
   end interface
 
   contains

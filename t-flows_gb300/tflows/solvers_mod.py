@@ -209,6 +209,7 @@ class Solver:
         """Device stamps of one DIC application's level launches
         (tfs_profile_prec): per launch, when its blocks passed their
         dependency wait and when they had finished (us)."""
+        self.levels()                       # builds the level layout first
         m = 4 * max(1, self.stats()["n_levels"]) + 8
         st, en = np.zeros(m), np.zeros(m)
         kd, n = np.zeros(m, np.int32), _i32(0)

@@ -113,10 +113,10 @@ def test_solve_from_reference_format_files(gpu):
             assert res.status == 0 and res.fin_res < ref["tol"] and rel_l2(x, ref["x"]) < 1e-6
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ["plain50"])
 def test_one_block_dic_on_reference_mesh(name, gpu):
     """The reference's meshes in their own numbering have deep level
-    schedules (plain_50: 148 levels of about 100 rows), which is what the
+    schedules (plain_50: 148 levels of at most 149 rows), which is what the
     one-block DIC (the swept vector in shared memory) is for: Prec_Form and
     Prec_Solve bitwise equal to the oracle, and DIC-CG solves in both
     arithmetics bitwise equal to the level kernels' (TFS_OPT_DIC_BLOCK = 0,
