@@ -161,12 +161,6 @@ int tfs_set_default_precision(int mode);
                                     ahead, where the vector and at least three
                                     level slots fit (deep schedules of narrow
                                     levels; default); 0 the level kernels       */
-#define TFS_OPT_SPMV_REVERSE 15  /* 1 on the DIC level layout the software-
-                                    pipelined SpMV walks its row chunks last to
-                                    first, so the first levels' matrix lines
-                                    are still in L2 for the next forward sweep
-                                    (default); 0 first to last.  Same q; (p, q)
-                                    summed in another order                     */
 
 /* One DIC application (the tfs_time_prec workload: factor from val, r = 1)
  * with its level launches stamped on the device: for slot k (launch order)

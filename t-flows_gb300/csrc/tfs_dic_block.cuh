@@ -11,13 +11,18 @@
 //   - the swept vector lives in shared memory (one value per row, in place:
 //     y, then y / (D + TINY), then z), so a step's gathers are shared-memory
 //     loads;
-//   - each level's rows -- their SELL slices of column indices and values,
-//     geometry, diagonal and (forward) right-hand side, contiguous in global
-//     memory because levels start on slice boundaries -- are staged into a
-//     ring of R shared-memory slots by 16-byte cp.async copies issued R - 1
-//     levels before the level runs, so a step waits for no global load;
-//   - a step is then one cp.async group wait, one __syncthreads, the row's
-//     shared-memory loads and arithmetic.
+//   - each level's rows -- their SELL slices of column indices and values
+//     (uniform or per-slice widths), geometry, diagonal and (forward)
+//     right-hand side, contiguous in global memory because levels start on
+//     slice boundaries -- are staged into a ring of R shared-memory slots by
+//     16-byte cp.async copies issued R - 1 levels before the level runs, so
+//     a step waits for no global load;
+//   - the block's threads are split: the first half sweeps the level's
+//     rows, the second half issues the copies (and waits for them), so the
+//     row threads' dependent chain per step holds no copy instructions; the
+//     level and slice-offset tables are copied into shared memory once;
+//   - a step is then one cp.async group wait (copy threads), one
+//     __syncthreads, the row's shared-memory loads and arithmetic.
 // L1 prefetches in place of the ring measured slower than no prefetch at all
 // (plain_50 binary64: 529 against 402 us per application).
 //
@@ -27,32 +32,34 @@
 // cp.async of the block's own, in-bounds data and every wait is on the
 // thread's own copies: no wait depends on another block.
 #pragma once
-#include <type_traits>
-
 #include "tfs_kernels.cuh"
 
 namespace tfs {
 
 #define TFS_DICB_TPB 512
+#define TFS_DICB_ROWS (TFS_DICB_TPB / 2)     // threads sweeping rows; the others stage levels
 #define TFS_DICB_MAX_SLOTS 8
+#define TFS_DICB_MAX_LEVELS 4096
 
-// Byte offsets inside one ring slot of `rm` rows (rm a multiple of 32, so
-// every part starts on a 16-byte boundary): geometry, diagonal, right-hand
-// side, column indices and values of up to rm rows of one level.
+// Byte offsets inside one ring slot of `rm` rows and `ents` SELL entries
+// (rm and ents multiples of 32, so every part starts on a 16-byte boundary):
+// geometry, diagonal, right-hand side, column indices and values of one
+// level.
 struct DicbSlot {
-    int rm, off_d, off_b, off_col, off_val, bytes;
+    int rm, ents, off_d, off_b, off_col, off_val, bytes;
 };
 
 template <typename T>
-__host__ __device__ inline DicbSlot dicb_slot(int rm, int W)
+__host__ __device__ inline DicbSlot dicb_slot(int rm, int ents)
 {
     DicbSlot s;
     s.rm = rm;
+    s.ents = ents;
     s.off_d = rm * 4;
     s.off_b = s.off_d + rm * (int)sizeof(T);
     s.off_col = s.off_b + rm * (int)sizeof(T);
-    s.off_val = s.off_col + rm * W * 4;
-    s.bytes = s.off_val + rm * W * (int)sizeof(T);
+    s.off_val = s.off_col + ents * 4;
+    s.bytes = s.off_val + ents * (int)sizeof(T);
     return s;
 }
 
@@ -61,6 +68,13 @@ template <typename T>
 __host__ __device__ inline int dicb_vec_bytes(int n_rows)
 {
     return (n_rows * (int)sizeof(T) + 127) & ~127;
+}
+
+// Shared memory of the level table (n_levels + 1 ints, padded to 4) and the
+// slice-offset table (n_rows / 32 + 1 ints), rounded to 16 bytes.
+__host__ __device__ inline int dicb_table_bytes(int n_levels, int n_rows)
+{
+    return ((((n_levels + 4) & ~3) + (n_rows >> 5) + 1) * 4 + 15) & ~15;
 }
 
 __device__ __forceinline__ uint32_t dicb_smem_addr(const void *p)
@@ -93,48 +107,59 @@ __device__ __forceinline__ void dicb_wait(int n)
     }
 }
 
-// Stage level l's rows into `slot` (every thread its share of 16-byte
-// chunks).  PART 0: forward (geometry, d, b, entries); 1: backward (no b);
-// 2: the recurrence (geometry and entries only).
+// Stage level l's rows into `slot` (each copy thread, ct = 0 ..
+// TFS_DICB_TPB - TFS_DICB_ROWS - 1, its share of 16-byte chunks).  PART 0:
+// forward (geometry, d, b, entries); 1: backward (no b); 2: the recurrence
+// (geometry and entries only).  lv: the level table, so: the slice-offset
+// table, both in shared memory.
 template <typename T, int PART>
 __device__ __forceinline__ void dicb_stage(unsigned char *slot, const DicbSlot &L, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int *lvl_begin, int l)
+                                           const T *val, const T *d, const T *b, const int *lv, const int *so,
+                                           int l, int ct)
 {
-    const int r0 = __ldg(lvl_begin + l), nr = __ldg(lvl_begin + l + 1) - r0;
-    const int W = A.width;
+    const int r0 = lv[l], nr = lv[l + 1] - r0;
+    const int e0 = so[r0 >> 5], ne = so[(r0 + nr) >> 5] - e0;
+    constexpr int NC = TFS_DICB_TPB - TFS_DICB_ROWS;
     auto copy = [&](unsigned char *dst, const void *src, int bytes) {
-        for (int o = (int)threadIdx.x * 16; o < bytes; o += TFS_DICB_TPB * 16)
+        for (int o = ct * 16; o < bytes; o += NC * 16)
             dicb_cp16(dst + o, (const unsigned char *)src + o);
     };
     copy(slot, A.rowinfo + r0, nr * 4);
     if (PART != 2) copy(slot + L.off_d, d + r0, nr * (int)sizeof(T));
     if (PART == 0) copy(slot + L.off_b, b + r0, nr * (int)sizeof(T));
-    copy(slot + L.off_col, A.col + (size_t)r0 * W, nr * W * 4);
-    copy(slot + L.off_val, val + (size_t)r0 * W, nr * W * (int)sizeof(T));
+    copy(slot + L.off_col, A.col + e0, ne * 4);
+    copy(slot + L.off_val, val + e0, ne * (int)sizeof(T));
 }
 
 // One sweep of k_dic_block over all levels, ascending (DIR > 0) or
 // descending, through the ring of R slots.
 template <typename T, int PART, int DIR>
 __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int *lvl_begin,
+                                           const T *val, const T *d, const T *b, const int *lv, const int *so,
                                            int n_levels)
 {
-    const int tid = threadIdx.x, W = A.width;
+    const int tid = threadIdx.x;
+    const bool copier = tid >= TFS_DICB_ROWS;
+    const int ct = tid - TFS_DICB_ROWS;
     auto level_at = [&](int q) { return DIR > 0 ? q : n_levels - 1 - q; };
-    int staged = 0;
+    int staged = 0;   // levels staged (= copy groups committed) by a copy thread
     for (; staged < R - 1 && staged < n_levels; staged++) {
-        dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lvl_begin, level_at(staged));
-        dicb_commit();
+        if (copier) {
+            dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lv, so, level_at(staged), ct);
+            dicb_commit();
+        }
     }
     for (int q = 0; q < n_levels; q++) {
-        dicb_wait(staged - q - 1);   // this thread's copies of level q
+        if (copier) dicb_wait(staged - q - 1);   // this thread's copies of level q
         __syncthreads();             // everyone's copies; level q - 1 done, its slot free
-        if (staged < n_levels) {
-            dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lvl_begin,
-                                level_at(staged));
-            dicb_commit();
-            staged++;
+        if (copier) {
+            if (staged < n_levels) {
+                dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lv, so,
+                                    level_at(staged), ct);
+                dicb_commit();
+                staged++;
+            }
+            continue;
         }
         const unsigned char *slot = ring + (size_t)(q % R) * L.bytes;
         const uint32_t *sinfo = reinterpret_cast<const uint32_t *>(slot);
@@ -143,11 +168,11 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
         const int *scol = reinterpret_cast<const int *>(slot + L.off_col);
         const T *sval = reinterpret_cast<const T *>(slot + L.off_val);
         const int l = level_at(q);
-        const int r0 = __ldg(lvl_begin + l), nr = __ldg(lvl_begin + l + 1) - r0;
-        for (int k = tid; k < nr; k += TFS_DICB_TPB) {
+        const int r0 = lv[l], nr = lv[l + 1] - r0, sb0 = so[r0 >> 5];
+        for (int k = tid; k < nr; k += TFS_DICB_ROWS) {
             const uint32_t info = sinfo[k];
             const int len = (int)(info & 0xffffu), dpos = (int)(info >> 16);
-            const int e0 = (k & ~31) * W + (k & 31);   // entry j at e0 + 32 j
+            const int e0 = so[(r0 + k) >> 5] - sb0 + (k & 31);   // entry j at e0 + 32 j
             const int i = r0 + k;
             if (PART == 2) {
                 if (len == 0) { s[i] = (T)1; continue; }
@@ -170,16 +195,16 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
             }
         }
     }
-    dicb_wait(0);
+    if (copier) dicb_wait(0);
     __syncthreads();
 }
 
 // MODE 0: z = M^-1 b (forward sweep, scaling, backward sweep) with the
 // factor d; MODE 2: the DIC factor d from the matrix (binary64; b and z
-// unused).  One block of TFS_DICB_TPB threads on a uniform-width SELL
-// matrix; dynamic shared memory: the vector (dicb_vec_bytes) and R slots of
-// L.bytes.  Rows past lvl_begin[n_levels] (the layout's final padding) are
-// never touched.
+// unused).  One block of TFS_DICB_TPB threads; dynamic shared memory: the
+// vector (dicb_vec_bytes), R slots of L.bytes and the level and slice-offset
+// tables (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS levels).  Rows past
+// lvl_begin[n_levels] (the layout's final padding) are never touched.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(TFS_DICB_TPB, 1)
 k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const int *__restrict__ lvl_begin,
@@ -189,21 +214,28 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     const int n_rows = __ldg(lvl_begin + n_levels);
     T *s = reinterpret_cast<T *>(dicb_smem);
     unsigned char *ring = dicb_smem + dicb_vec_bytes<T>(n_rows);
+    int *lv = reinterpret_cast<int *>(ring + (size_t)R * L.bytes);
+    int *so = lv + ((n_levels + 4) & ~3);
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
     if (st->done) return;
     if (MODE == 0 && tid == 0) st->t_sweep0 = gtimer();
+    for (int l = tid; l <= n_levels; l += TFS_DICB_TPB) lv[l] = __ldg(lvl_begin + l);
+    for (int q = tid; q <= (n_rows >> 5); q += TFS_DICB_TPB)
+        so[q] = A.width ? q * 32 * A.width : __ldg(A.slice_off + q);
+    __syncthreads();
     if (MODE == 2) {
-        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
+        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
         for (int i = tid; i < n_rows; i += TFS_DICB_TPB) d[i] = s[i];
         return;
     }
-    dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
+    dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
     // Every row's backward start value y_i / (D_i + TINY) (Prec_Solve.f90:55-57).
+#pragma unroll 4
     for (int i = tid; i < n_rows; i += TFS_DICB_TPB)
         if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
     __syncthreads();
-    dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lvl_begin, n_levels);
+    dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
     for (int i = tid; i < n_rows; i += TFS_DICB_TPB) z[i] = s[i];
 }
 

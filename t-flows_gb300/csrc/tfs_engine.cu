@@ -186,30 +186,21 @@ static void spmv_kind_setup(tfs_handle *h)
                                                                                 : TFS_SPMV_DIRECT;
 }
 
-template <typename VT, bool MIXED, bool REV>
-static void launch_spmv_pipe_w(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
+template <typename VT, bool MIXED>
+static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
 {
     const SellDev A = sell_of(h);
     const int G = h->grid_spmv;
     switch (h->sell_width) {
-    case 1: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 1, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 2: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 2, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 3: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 3, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 4: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 4, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 5: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 5, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 6: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 6, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    case 7: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 7, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
-    default: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 8, REV>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 1: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 1>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 2: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 2>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 3: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 3>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 4: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 4>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 5: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 5>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 6: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 6>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    case 7: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 7>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
+    default: launch_ex(pdl, k_spmv_pq_pipe<VT, MIXED, 8>, G, TFS_TPB, s, A, val, p, q, h->st, h->part); break;
     }
-}
-
-// The software-pipelined SpMV, its chunks walked last to first on the DIC
-// level layout (TFS_OPT_SPMV_REVERSE, default on there).
-template <typename VT, bool MIXED>
-static void launch_spmv_pipe(const tfs_handle *h, cudaStream_t s, const VT *val, const VT *p, VT *q, bool pdl)
-{
-    if (h->spmv_reverse && h->layout == TFS_LAYOUT_LEVELS) launch_spmv_pipe_w<VT, MIXED, true>(h, s, val, p, q, pdl);
-    else launch_spmv_pipe_w<VT, MIXED, false>(h, s, val, p, q, pdl);
 }
 
 // q = A p, (p, q) and alpha of a CG iteration on stream s, binary32 (mixed)
@@ -583,29 +574,35 @@ static int build_layout(tfs_handle *h, int kind)
         }
         h->pf_tail_level = l;
         h->pf_ok = l < nl && l <= h->tail_level;
-        // One-block DIC: the swept vector (every row of the levels) and a
-        // ring of at least 3 (at most TFS_DICB_MAX_SLOTS) level slots of the
-        // widest level's rows in the block's shared memory; uniform slice
-        // width only (the staged slices are then contiguous).
-        h->dicb_bytes64 = h->dicb_bytes32 = h->dicb_slots64 = h->dicb_slots32 = h->dicb_rm = 0;
-        if (kind == TFS_LAYOUT_LEVELS && h->sell_width > 0) {
+        // One-block DIC: the swept vector (every row of the levels), a ring
+        // of at least 3 (at most TFS_DICB_MAX_SLOTS) slots of the widest
+        // level's rows and entries, and the level and slice-offset tables in
+        // the block's shared memory.
+        h->dicb_bytes64 = h->dicb_bytes32 = h->dicb_slots64 = h->dicb_slots32 = h->dicb_rm = h->dicb_ents = 0;
+        if (kind == TFS_LAYOUT_LEVELS && nl <= TFS_DICB_MAX_LEVELS) {
             int optin = 0;
             CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-            int rm = 32;
-            for (int l = 0; l < nl; l++) rm = std::max(rm, h->lvl_begin[l + 1] - h->lvl_begin[l]);
+            int rm = 32, ents = 32;
+            for (int l = 0; l < nl; l++) {
+                const int a = h->lvl_begin[l], z = h->lvl_begin[l + 1];
+                rm = std::max(rm, z - a);
+                ents = std::max(ents, slice_off[z >> 5] - slice_off[a >> 5]);
+            }
             const int64_t rows = h->lvl_begin[nl];
             h->dicb_rm = rm;
+            h->dicb_ents = ents;
             auto fit = [&](int vec, int slot, int *bytes, int *slots) {
                 if (rows > INT32_MAX / 16) return;
-                const int64_t room = (int64_t)optin - vec;
+                const int tables = dicb_table_bytes(nl, (int)rows);
+                const int64_t room = (int64_t)optin - vec - tables;
                 const int64_t r = room > 0 ? std::min<int64_t>(TFS_DICB_MAX_SLOTS, room / slot) : 0;
                 if (r < 3) return;
                 *slots = (int)r;
-                *bytes = vec + (int)r * slot;
+                *bytes = vec + (int)r * slot + tables;
             };
-            fit(dicb_vec_bytes<double>((int)rows), dicb_slot<double>(rm, h->sell_width).bytes, &h->dicb_bytes64,
+            fit(dicb_vec_bytes<double>((int)rows), dicb_slot<double>(rm, ents).bytes, &h->dicb_bytes64,
                 &h->dicb_slots64);
-            fit(dicb_vec_bytes<float>((int)rows), dicb_slot<float>(rm, h->sell_width).bytes, &h->dicb_bytes32,
+            fit(dicb_vec_bytes<float>((int)rows), dicb_slot<float>(rm, ents).bytes, &h->dicb_bytes32,
                 &h->dicb_slots32);
             static std::once_flag attr_once;
             std::call_once(attr_once, [optin] {
@@ -776,7 +773,6 @@ static int *option_field(tfs_handle *h, int option, bool (**ok)(int))
     case TFS_OPT_FWD_PRE: return &h->fwd_pre;
     case TFS_OPT_BWD_PRE: return &h->bwd_pre;
     case TFS_OPT_DIC_BLOCK: return &h->dic_block;
-    case TFS_OPT_SPMV_REVERSE: return &h->spmv_reverse;
     default: return nullptr;
     }
 }
@@ -831,7 +827,7 @@ static int launch_dic_form(tfs_handle *h, cudaStream_t s)
     if (const int bytes = dic_block_bytes<double>(h)) {
         k_dic_block<double, 2><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), h->val, h->v.d, nullptr, nullptr,
                                                               h->d_lvl_begin, h->n_levels,
-                                                              dicb_slot<double>(h->dicb_rm, h->sell_width),
+                                                              dicb_slot<double>(h->dicb_rm, h->dicb_ents),
                                                               h->dicb_slots64, h->st);
         return 1;
     }
@@ -901,7 +897,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     if (nr == 1 && !fuse_l0) {
         if (const int bytes = dic_block_bytes<T>(h)) {
             k_dic_block<T, 0><<<1, TFS_DICB_TPB, bytes, s>>>(
-                A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, dicb_slot<T>(h->dicb_rm, h->sell_width),
+                A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, dicb_slot<T>(h->dicb_rm, h->dicb_ents),
                 sizeof(T) == 8 ? h->dicb_slots64 : h->dicb_slots32, h->st);
             h->dicb_used = 1;
             (*count)++;

@@ -130,12 +130,11 @@ struct tfs_handle {
     int sell_uniform = 1;              // TFS_OPT_SELL_UNIFORM: one slice width when it costs <= 5% padding
     int spmv_pref = 1;                 // TFS_OPT_SPMV: 1 software-pipelined where possible, 0 direct
     int spmv_chunks = 0;               // TFS_OPT_SPMV_GRID: 1 one block per 256-row chunk
-    int spmv_reverse = 1;              // TFS_OPT_SPMV_REVERSE: level-layout SpMV walks its chunks last to first
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
     int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC (vector in shared memory) where it fits
     int dicb_used = 0;                 // the last DIC application launched was the one-block kernel
-    int dicb_rm = 0;                   // one-block DIC: rows of a ring slot (the widest level)
+    int dicb_rm = 0, dicb_ents = 0;    // one-block DIC: rows and SELL entries of a ring slot (the widest level)
     int dicb_slots64 = 0, dicb_slots32 = 0;   // ring slots that fit (0: not used for that arithmetic)
     bool profiling = false;            // tfs_profile_prec: number the sweep launches
     int stamp_next = 0;                // next slot number while profiling

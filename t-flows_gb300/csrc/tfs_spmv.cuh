@@ -38,26 +38,18 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 #ifndef TFS_PIPE_MINB64
 #define TFS_PIPE_MINB64 1
 #endif
-//
-// REV: the chunks are walked from the last to the first (block b takes
-// chunks nch - 1 - b, nch - 1 - b - gridDim.x, ...), so the rows of the
-// first DIC levels are the matrix lines read last -- the ones still in L2
-// when the next forward sweep starts with those levels.  Same rows and
-// per-row arithmetic; the per-thread order of the (p, q) terms is reversed.
-template <typename VT, bool MIXED, int W, bool REV = false>
+template <typename VT, bool MIXED, int W>
 __global__ void __launch_bounds__(TFS_TPB, sizeof(VT) == 4 ? TFS_PIPE_MINB32 : TFS_PIPE_MINB64)
 k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, VT *__restrict__ q,
                DevState *st, double *part)
 {
     const int tid = threadIdx.x, nch = A.n_chunks;
-    // chunk index of the k-th step of this block (k = 0, 1, ...)
-    auto chunk = [&](int c) { return REV ? nch - 1 - c : c; };
     int c = blockIdx.x;
     // column indices and geometry of the thread's next row
     int nk[W];
     uint32_t ninfo = 0u;
     if (c < nch) {
-        const int i = chunk(c) * TFS_TPB + tid;
+        const int i = c * TFS_TPB + tid;
         const int off = (i & ~31) * W + (i & 31);
         ninfo = __ldg(A.rowinfo + i);
 #pragma unroll
@@ -70,7 +62,7 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
     if (blockIdx.x == 0 && tid == 0) st->t_spmv0 = gtimer();
     VT acc = (VT)0;
     for (; c < nch; c += gridDim.x) {
-        const int i = chunk(c) * TFS_TPB + tid;
+        const int i = c * TFS_TPB + tid;
         const int off = (i & ~31) * W + (i & 31);
         const int len = (int)(ninfo & 0xffffu);
         VT a[W], x[W];
@@ -86,7 +78,7 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
         const VT pi = p[i];
         const int cn = c + gridDim.x;
         if (cn < nch) {
-            const int in = chunk(cn) * TFS_TPB + tid;
+            const int in = cn * TFS_TPB + tid;
             const int offn = (in & ~31) * W + (in & 31);
             ninfo = __ldg(A.rowinfo + in);
 #pragma unroll

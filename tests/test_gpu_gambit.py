@@ -113,7 +113,7 @@ def test_solve_from_reference_format_files(gpu):
             assert res.status == 0 and res.fin_res < ref["tol"] and rel_l2(x, ref["x"]) < 1e-6
 
 
-@pytest.mark.parametrize("name", ["plain50"])
+@pytest.mark.parametrize("name", NAMES)
 def test_one_block_dic_on_reference_mesh(name, gpu):
     """The reference's meshes in their own numbering have deep level
     schedules (plain_50: 148 levels of at most 149 rows), which is what the

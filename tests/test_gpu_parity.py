@@ -17,7 +17,7 @@ from oracle import tfs_oracle as O
 from tflows import (TFS_BICG, TFS_CG, TFS_CGS, TFS_FP64, TFS_MIXED, Matrix_Type, Solver)
 from tflows.lib import (TFS_ERR_NONFINITE, TFS_OPT_BICG, TFS_OPT_BWD_PRE, TFS_OPT_FUSE_L0, TFS_OPT_FWD_PRE,
                         TFS_OPT_LEVEL_TPB, TFS_OPT_SELL_UNIFORM, TFS_OPT_SPMV, TFS_OPT_SPMV_GRID,
-                        TFS_OPT_SPMV_REVERSE, TFS_OPT_TAIL_PF)
+                        TFS_OPT_TAIL_PF)
 from tflows.synth import CONVDIFF, POISSON
 
 pytestmark = pytest.mark.gpu
@@ -333,8 +333,7 @@ def test_spmv_kernels_bitwise(grid, gpu):
     flight) takes the direct kernel's rows, dot-product order and reductions
     over the same grid (8 blocks per SM, or one block per chunk): q = A p and
     whole CG solves (binary64 and mixed, diagonal and DIC) are bitwise those
-    of the direct kernel (TFS_OPT_SPMV = 0), with the chunks walked in the
-    same order (TFS_OPT_SPMV_REVERSE = 0)."""
+    of the direct kernel (TFS_OPT_SPMV = 0)."""
     s = system(POISSON, 40, 40, 40)
     ref = oracle_solve(s, TFS_CG, 2)
     pv = np.random.default_rng(5).uniform(-1, 1, s.n)
@@ -342,7 +341,7 @@ def test_spmv_kernels_bitwise(grid, gpu):
     for k in (1, 0):
         res = []
         for mode in (TFS_FP64, TFS_MIXED):
-            opts = {TFS_OPT_SPMV: k, TFS_OPT_SPMV_GRID: grid, TFS_OPT_SPMV_REVERSE: 0}
+            opts = {TFS_OPT_SPMV: k, TFS_OPT_SPMV_GRID: grid}
             with Solver(s.matrix(), precision=mode, options=opts) as sol:
                 if mode == TFS_FP64:
                     res.append(sol.spmv(s.val, pv))
@@ -628,23 +627,3 @@ def test_one_block_dic_not_used_on_wide_levels(gpu):
         z = sol.prec_solve(s.val, 2, b)
         assert sol.stats()["dic_kernel"] == 0
     assert np.array_equal(z, O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
-
-
-def test_reverse_spmv_order(gpu):
-    """On the DIC level layout the SpMV walks its row chunks last to first
-    (TFS_OPT_SPMV_REVERSE, default): q = A p is bitwise the same, the (p, q)
-    terms are summed in another order, so DIC-CG solves differ from the
-    forward walk only within the parity gates of the oracle."""
-    s = system(POISSON, 40, 40, 40)
-    ref = oracle_solve(s, TFS_CG, 2)
-    pv = np.random.default_rng(15).uniform(-1, 1, s.n)
-    for mode, gate in ((TFS_FP64, SOL_REL), (TFS_MIXED, 1e-6)):
-        for rev in (1, 0):
-            with Solver(s.matrix(), precision=mode, options={TFS_OPT_SPMV_REVERSE: rev}) as sol:
-                sol.levels()                       # the level layout, as DIC builds it
-                if mode == TFS_FP64:
-                    assert np.array_equal(sol.spmv(s.val, pv), O.spmv(s.n, s.row, s.col, s.val, pv))
-                x, r = np.zeros(s.n), s.b.copy()
-                st = sol.solve(TFS_CG, s.val, x, r, 2, 2000, ref["tol"])
-                assert st.status == 0 and st.fin_res < ref["tol"]
-                assert iter_ok(st.niter, ref["niter"]) and rel_l2(x, ref["x"]) <= gate
