@@ -17,20 +17,34 @@
 //     slice boundaries -- are staged into a ring of R shared-memory slots by
 //     16-byte cp.async copies issued R - 1 levels before the level runs, so
 //     a step waits for no global load;
-//   - the block's threads are split: the first half sweeps the level's
-//     rows, the second half issues the copies (and waits for them), so the
-//     row threads' dependent chain per step holds no copy instructions; the
-//     level and slice-offset tables are copied into shared memory once;
-//   - a step is then one cp.async group wait (copy threads), one
-//     __syncthreads, the row's shared-memory loads and arithmetic.
+//   - the block's threads are split: the first half sweeps the levels'
+//     rows, the second half stages the levels, and the two halves meet only
+//     at per-slot mbarriers: a copy thread's cp.async.mbarrier.arrive fires
+//     on the slot's "full" barrier once its copies of the level have landed,
+//     and a row thread arrives on the slot's "empty" barrier once it is done
+//     with the level; the row threads synchronise among themselves with a
+//     named barrier (bar.sync, which orders their shared-memory stores);
+//     the level records (first row, rows, first entry, entries) and the
+//     slice-offset table are built in shared memory once;
+//   - a step of the row threads is then one completed-phase test of the
+//     slot's barrier, the row's shared-memory loads and arithmetic and one
+//     barrier of the 256 row threads.
+// Measured on plain_50 (binary32 application): one __syncthreads of the
+// whole block per level with the copies issued by every thread 336 us,
+// issued by the copy half 233 us.
 // L1 prefetches in place of the ring measured slower than no prefetch at all
 // (plain_50 binary64: 529 against 402 us per application).
 //
 // Every row does exactly sweep_row's arithmetic (the reference's order of
 // terms: Prec_Solve.f90:46-67, Prec_Form.f90:32-40), so the results are
 // bitwise those of the per-level schedule.  Every copy is a 16-byte aligned
-// cp.async of the block's own, in-bounds data and every wait is on the
-// thread's own copies: no wait depends on another block.
+// cp.async of the block's own, in-bounds data.  No wait depends on another
+// block: the mbarrier waits are on this block's own copies and row threads,
+// and each is bounded (TFS_DICB_WAIT_NS of global time); a wait that runs
+// out raises the block's abort flag, after which no thread waits on an
+// mbarrier again (the results are then garbage), every thread still passes
+// the same named barriers, the copy threads wait for their own copies before
+// they exit, and the solve ends with TFS_ERR_TIMEOUT.
 #pragma once
 #include "tfs_kernels.cuh"
 
@@ -40,6 +54,10 @@ namespace tfs {
 #define TFS_DICB_ROWS (TFS_DICB_TPB / 2)     // threads sweeping rows; the others stage levels
 #define TFS_DICB_MAX_SLOTS 8
 #define TFS_DICB_MAX_LEVELS 4096
+#define TFS_DICB_ROW_BAR 1                   // named barrier of the row threads
+#ifndef TFS_DICB_WAIT_NS
+#define TFS_DICB_WAIT_NS 500000000ull        // 0.5 s
+#endif
 
 // Byte offsets inside one ring slot of `rm` rows and `ents` SELL entries
 // (rm and ents multiples of 32, so every part starts on a 16-byte boundary):
@@ -70,11 +88,19 @@ __host__ __device__ inline int dicb_vec_bytes(int n_rows)
     return (n_rows * (int)sizeof(T) + 127) & ~127;
 }
 
-// Shared memory of the level table (n_levels + 1 ints, padded to 4) and the
-// slice-offset table (n_rows / 32 + 1 ints), rounded to 16 bytes.
+// Shared memory of the level records (one int4 per level: first row, rows,
+// first SELL entry, entries) and the slice-offset table (n_rows / 32 + 1
+// ints), rounded to 16 bytes.
 __host__ __device__ inline int dicb_table_bytes(int n_levels, int n_rows)
 {
-    return ((((n_levels + 4) & ~3) + (n_rows >> 5) + 1) * 4 + 15) & ~15;
+    return n_levels * 16 + (((n_rows >> 5) + 1) * 4 + 15) / 16 * 16;
+}
+
+// Shared memory of the ring's R full and R empty mbarriers and the abort
+// flag.
+__host__ __device__ inline int dicb_sync_bytes(int R)
+{
+    return 2 * R * 8 + 16;
 }
 
 __device__ __forceinline__ uint32_t dicb_smem_addr(const void *p)
@@ -92,33 +118,71 @@ __device__ __forceinline__ void dicb_commit()
     asm volatile("cp.async.commit_group;" : : : "memory");
 }
 
-// Wait until at most n of the thread's committed copy groups are pending.
-__device__ __forceinline__ void dicb_wait(int n)
+__device__ __forceinline__ void dicb_wait_all()
 {
-    switch (n) {
-    case 0: asm volatile("cp.async.wait_group 0;" : : : "memory"); break;
-    case 1: asm volatile("cp.async.wait_group 1;" : : : "memory"); break;
-    case 2: asm volatile("cp.async.wait_group 2;" : : : "memory"); break;
-    case 3: asm volatile("cp.async.wait_group 3;" : : : "memory"); break;
-    case 4: asm volatile("cp.async.wait_group 4;" : : : "memory"); break;
-    case 5: asm volatile("cp.async.wait_group 5;" : : : "memory"); break;
-    case 6: asm volatile("cp.async.wait_group 6;" : : : "memory"); break;
-    default: asm volatile("cp.async.wait_group 7;" : : : "memory"); break;
+    asm volatile("cp.async.wait_all;" : : : "memory");
+}
+
+__device__ __forceinline__ void dicb_mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(dicb_smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Arrive on bar once every cp.async the thread has issued so far has landed
+// (the pending count is not raised first: the barrier's expected count
+// includes this arrival).
+__device__ __forceinline__ void dicb_mbar_arrive_copies(uint64_t *bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" : : "r"(dicb_smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void dicb_mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(dicb_smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool dicb_mbar_test(uint64_t *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(ok) : "r"(dicb_smem_addr(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase of the given parity to complete, at most
+// TFS_DICB_WAIT_NS; false (and the abort flag raised) when it did not, or
+// at once when the flag is already up.
+__device__ __forceinline__ bool dicb_mbar_wait(uint64_t *bar, unsigned parity, volatile int *abort)
+{
+    if (dicb_mbar_test(bar, parity)) return true;
+    if (*abort) return false;
+    const unsigned long long t0 = gtimer();
+    for (unsigned k = 1;; k++) {
+        if (dicb_mbar_test(bar, parity)) return true;
+        if ((k & 255u) == 0u) {
+            if (*abort) return false;
+            if (gtimer() - t0 > TFS_DICB_WAIT_NS) {
+                *abort = 1;
+                return false;
+            }
+        }
     }
 }
 
-// Stage level l's rows into `slot` (each copy thread, ct = 0 ..
-// TFS_DICB_TPB - TFS_DICB_ROWS - 1, its share of 16-byte chunks).  PART 0:
-// forward (geometry, d, b, entries); 1: backward (no b); 2: the recurrence
-// (geometry and entries only).  lv: the level table, so: the slice-offset
-// table, both in shared memory.
+__device__ __forceinline__ void dicb_row_sync()
+{
+    asm volatile("bar.sync %0, %1;" : : "n"(TFS_DICB_ROW_BAR), "n"(TFS_DICB_ROWS) : "memory");
+}
+
+// Stage the level of record lr (first row, rows, first entry, entries)
+// into `slot` (each copy thread, ct = 0 .. TFS_DICB_TPB - TFS_DICB_ROWS - 1,
+// its share of 16-byte chunks).  PART 0: forward (geometry, d, b, entries);
+// 1: backward (no b); 2: the recurrence (geometry and entries only).
 template <typename T, int PART>
 __device__ __forceinline__ void dicb_stage(unsigned char *slot, const DicbSlot &L, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int *lv, const int *so,
-                                           int l, int ct)
+                                           const T *val, const T *d, const T *b, int4 lr, int ct)
 {
-    const int r0 = lv[l], nr = lv[l + 1] - r0;
-    const int e0 = so[r0 >> 5], ne = so[(r0 + nr) >> 5] - e0;
+    const int r0 = lr.x, nr = lr.y, e0 = lr.z, ne = lr.w;
     constexpr int NC = TFS_DICB_TPB - TFS_DICB_ROWS;
     auto copy = [&](unsigned char *dst, const void *src, int bytes) {
         for (int o = ct * 16; o < bytes; o += NC * 16)
@@ -131,79 +195,117 @@ __device__ __forceinline__ void dicb_stage(unsigned char *slot, const DicbSlot &
     copy(slot + L.off_val, val + e0, ne * (int)sizeof(T));
 }
 
-// One sweep of k_dic_block over all levels, ascending (DIR > 0) or
-// descending, through the ring of R slots.
-template <typename T, int PART, int DIR>
-__device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int *lv, const int *so,
-                                           int n_levels)
+// The ring's per-slot barriers and the block's abort flag.
+struct DicbSync {
+    uint64_t *full, *empty;   // R each
+    volatile int *abort;
+};
+
+// Row i's new value from its staged entries j0 <= j < j1 (at e0 + 32 j of
+// the slot): acc - sum a_j s[col_j] in ascending j (PART 0 and 1), or
+// acc - sum s[col_j] a_j a_j (PART 2); up to 8 entries have every column
+// index, value and gather issued before the in-order chain of updates.
+// Measured on plain_50: binary32 219 -> 189 us per application; with the
+// binary64 updates predicated like the binary32 ones, 286 -> 367 us.
+template <typename T, int PART>
+__device__ __forceinline__ T dicb_row(T acc, const T *s, const int *scol, const T *sval, int e0, int j0, int j1)
 {
-    const int tid = threadIdx.x;
-    const bool copier = tid >= TFS_DICB_ROWS;
-    const int ct = tid - TFS_DICB_ROWS;
-    auto level_at = [&](int q) { return DIR > 0 ? q : n_levels - 1 - q; };
-    int staged = 0;   // levels staged (= copy groups committed) by a copy thread
-    for (; staged < R - 1 && staged < n_levels; staged++) {
-        if (copier) {
-            dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lv, so, level_at(staged), ct);
-            dicb_commit();
+    int c[8];
+    T a[8], x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+        if (j0 + u < j1) {
+            c[u] = scol[e0 + ((j0 + u) << 5)];
+            a[u] = sval[e0 + ((j0 + u) << 5)];
+        }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+        if (j0 + u < j1) x[u] = s[c[u]];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (j0 + u < j1) acc = PART == 2 ? acc - x[u] * a[u] * a[u] : acc - a[u] * x[u];
+    } else {
+        // binary64: leave the chain at the row's last entry (GB300's narrow
+        // binary64 pipe would otherwise also run the absent entries' updates)
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (j0 + u >= j1) break;
+            acc = PART == 2 ? acc - x[u] * a[u] * a[u] : acc - a[u] * x[u];
         }
     }
-    for (int q = 0; q < n_levels; q++) {
-        if (copier) dicb_wait(staged - q - 1);   // this thread's copies of level q
-        __syncthreads();             // everyone's copies; level q - 1 done, its slot free
-        if (copier) {
-            if (staged < n_levels) {
-                dicb_stage<T, PART>(ring + (size_t)(staged % R) * L.bytes, L, A, val, d, b, lv, so,
-                                    level_at(staged), ct);
-                dicb_commit();
-                staged++;
-            }
-            continue;
+    for (int j = j0 + 8; j < j1; j++) {
+        const T v = sval[e0 + (j << 5)];
+        acc = PART == 2 ? acc - s[scol[e0 + (j << 5)]] * v * v : acc - v * s[scol[e0 + (j << 5)]];
+    }
+    return acc;
+}
+
+// One sweep of k_dic_block over all levels, ascending (DIR > 0) or
+// descending, through the ring of R slots.  g0: the number of levels staged
+// by the sweeps before this one (slot and barrier phase of the q-th level
+// of this sweep: (g0 + q) % R and (g0 + q) / R).  Copy threads stage the
+// levels, row threads sweep them; neither waits for the whole block.
+// lr: the level records in shared memory.
+template <typename T, int PART, int DIR>
+__device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
+                                           const T *val, const T *d, const T *b, const int4 *lr, const int *so,
+                                           int n_levels, int g0, const DicbSync &y)
+{
+    const int tid = threadIdx.x, W = A.width;
+    int slot = g0 % R;
+    unsigned ph = (unsigned)((g0 / R) & 1);   // phase parity of the slot's current use
+    int l = DIR > 0 ? 0 : n_levels - 1;
+    if (tid >= TFS_DICB_ROWS) {
+        const int ct = tid - TFS_DICB_ROWS;
+        for (int q = 0; q < n_levels; q++, l += DIR) {
+            // the slot's previous use (level g0 + q - R) must be done by the row threads
+            if (g0 + q >= R) dicb_mbar_wait(y.empty + slot, ph ^ 1u, y.abort);
+            dicb_stage<T, PART>(ring + (size_t)slot * L.bytes, L, A, val, d, b, lr[l], ct);
+            dicb_mbar_arrive_copies(y.full + slot);
+            if (++slot == R) { slot = 0; ph ^= 1u; }
         }
-        const unsigned char *slot = ring + (size_t)(q % R) * L.bytes;
-        const uint32_t *sinfo = reinterpret_cast<const uint32_t *>(slot);
-        const T *sd = reinterpret_cast<const T *>(slot + L.off_d);
-        const T *sb = reinterpret_cast<const T *>(slot + L.off_b);
-        const int *scol = reinterpret_cast<const int *>(slot + L.off_col);
-        const T *sval = reinterpret_cast<const T *>(slot + L.off_val);
-        const int l = level_at(q);
-        const int r0 = lv[l], nr = lv[l + 1] - r0, sb0 = so[r0 >> 5];
+        return;
+    }
+    for (int q = 0; q < n_levels; q++, l += DIR) {
+        const int4 rec = lr[l];
+        dicb_mbar_wait(y.full + slot, ph, y.abort);
+        const unsigned char *sl = ring + (size_t)slot * L.bytes;
+        const uint32_t *sinfo = reinterpret_cast<const uint32_t *>(sl);
+        const T *sd = reinterpret_cast<const T *>(sl + L.off_d);
+        const T *sb = reinterpret_cast<const T *>(sl + L.off_b);
+        const int *scol = reinterpret_cast<const int *>(sl + L.off_col);
+        const T *sval = reinterpret_cast<const T *>(sl + L.off_val);
+        const int r0 = rec.x, nr = rec.y, sb0 = rec.z;
         for (int k = tid; k < nr; k += TFS_DICB_ROWS) {
             const uint32_t info = sinfo[k];
             const int len = (int)(info & 0xffffu), dpos = (int)(info >> 16);
-            const int e0 = so[(r0 + k) >> 5] - sb0 + (k & 31);   // entry j at e0 + 32 j
+            // entry j of the row at e0 + 32 j of the slot
+            const int e0 = (W ? (k & ~31) * W : so[(r0 + k) >> 5] - sb0) + (k & 31);
             const int i = r0 + k;
             if (PART == 2) {
                 if (len == 0) { s[i] = (T)1; continue; }
-                T acc = sval[e0 + (dpos << 5)];
-                for (int j = 0; j < dpos; j++) {
-                    const T a = sval[e0 + (j << 5)];
-                    acc = acc - s[scol[e0 + (j << 5)]] * a * a;
-                }
-                s[i] = (T)1 / acc;
+                s[i] = (T)1 / dicb_row<T, 2>(sval[e0 + (dpos << 5)], s, scol, sval, e0, 0, dpos);
             } else if (PART == 0) {
                 if (len == 0) { s[i] = (T)0; continue; }
-                T acc = sb[k];
-                for (int j = 0; j < dpos; j++) acc = acc - sval[e0 + (j << 5)] * s[scol[e0 + (j << 5)]];
-                s[i] = acc * sd[k];
+                s[i] = dicb_row<T, 0>(sb[k], s, scol, sval, e0, 0, dpos) * sd[k];
             } else {
                 if (len == 0) continue;   // 0 since the forward sweep
-                T acc = s[i];
-                for (int j = dpos + 1; j < len; j++) acc = acc - sval[e0 + (j << 5)] * s[scol[e0 + (j << 5)]];
-                s[i] = acc * sd[k];
+                s[i] = dicb_row<T, 1>(s[i], s, scol, sval, e0, dpos + 1, len) * sd[k];
             }
         }
+        dicb_mbar_arrive(y.empty + slot);   // done with the slot
+        dicb_row_sync();                    // this level's rows visible to the next
+        if (++slot == R) { slot = 0; ph ^= 1u; }
     }
-    if (copier) dicb_wait(0);
-    __syncthreads();
 }
 
 // MODE 0: z = M^-1 b (forward sweep, scaling, backward sweep) with the
 // factor d; MODE 2: the DIC factor d from the matrix (binary64; b and z
 // unused).  One block of TFS_DICB_TPB threads; dynamic shared memory: the
-// vector (dicb_vec_bytes), R slots of L.bytes and the level and slice-offset
-// tables (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS levels).  Rows past
+// vector (dicb_vec_bytes), R slots of L.bytes, the level records and the
+// slice-offset table (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS levels) and the
+// ring's 2 R mbarriers and abort flag (dicb_sync_bytes).  Rows past
 // lvl_begin[n_levels] (the layout's final padding) are never touched.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(TFS_DICB_TPB, 1)
@@ -214,29 +316,57 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     const int n_rows = __ldg(lvl_begin + n_levels);
     T *s = reinterpret_cast<T *>(dicb_smem);
     unsigned char *ring = dicb_smem + dicb_vec_bytes<T>(n_rows);
-    int *lv = reinterpret_cast<int *>(ring + (size_t)R * L.bytes);
-    int *so = lv + ((n_levels + 4) & ~3);
+    int4 *lr = reinterpret_cast<int4 *>(ring + (size_t)R * L.bytes);
+    int *so = reinterpret_cast<int *>(lr + n_levels);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(lr) +
+                                                  dicb_table_bytes(n_levels, n_rows));
+    DicbSync y{bars, bars + R, reinterpret_cast<volatile int *>(bars + 2 * R)};
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
     if (st->done) return;
     if (MODE == 0 && tid == 0) st->t_sweep0 = gtimer();
-    for (int l = tid; l <= n_levels; l += TFS_DICB_TPB) lv[l] = __ldg(lvl_begin + l);
     for (int q = tid; q <= (n_rows >> 5); q += TFS_DICB_TPB)
         so[q] = A.width ? q * 32 * A.width : __ldg(A.slice_off + q);
     __syncthreads();
-    if (MODE == 2) {
-        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
-        for (int i = tid; i < n_rows; i += TFS_DICB_TPB) d[i] = s[i];
-        return;
+    for (int l = tid; l < n_levels; l += TFS_DICB_TPB) {
+        const int r0 = __ldg(lvl_begin + l), r1 = __ldg(lvl_begin + l + 1);
+        lr[l] = make_int4(r0, r1 - r0, so[r0 >> 5], so[r1 >> 5] - so[r0 >> 5]);
     }
-    dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
-    // Every row's backward start value y_i / (D_i + TINY) (Prec_Solve.f90:55-57).
-#pragma unroll 4
-    for (int i = tid; i < n_rows; i += TFS_DICB_TPB)
-        if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
+    if (tid == 0) {
+        for (int k = 0; k < R; k++) {
+            dicb_mbar_init(y.full + k, TFS_DICB_TPB - TFS_DICB_ROWS);
+            dicb_mbar_init(y.empty + k, TFS_DICB_ROWS);
+        }
+        *y.abort = 0;
+    }
     __syncthreads();
-    dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lv, so, n_levels);
-    for (int i = tid; i < n_rows; i += TFS_DICB_TPB) z[i] = s[i];
+    const bool row = tid < TFS_DICB_ROWS;
+    if (MODE == 2) {
+        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, 0, y);
+        if (row)
+            for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) d[i] = s[i];
+    } else {
+        dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, 0, y);
+        if (row) {
+            // Every row's backward start value y_i / (D_i + TINY)
+            // (Prec_Solve.f90:55-57), while the copy threads stage the
+            // backward sweep's first levels.
+#pragma unroll 4
+            for (int i = tid; i < n_rows; i += TFS_DICB_ROWS)
+                if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
+            dicb_row_sync();
+        }
+        dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, n_levels, y);
+        if (row)
+            for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) z[i] = s[i];
+    }
+    if (!row) dicb_wait_all();   // no copy of this block outlives it
+    __syncthreads();
+    if (tid == 0 && *y.abort) {
+        st->status = TFS_ERR_TIMEOUT;
+        st->done = 1;
+        st->niter_out = st->iter + 1;
+    }
 }
 
 }  // namespace tfs

@@ -593,7 +593,7 @@ static int build_layout(tfs_handle *h, int kind)
             h->dicb_ents = ents;
             auto fit = [&](int vec, int slot, int *bytes, int *slots) {
                 if (rows > INT32_MAX / 16) return;
-                const int tables = dicb_table_bytes(nl, (int)rows);
+                const int tables = dicb_table_bytes(nl, (int)rows) + dicb_sync_bytes(TFS_DICB_MAX_SLOTS);
                 const int64_t room = (int64_t)optin - vec - tables;
                 const int64_t r = room > 0 ? std::min<int64_t>(TFS_DICB_MAX_SLOTS, room / slot) : 0;
                 if (r < 3) return;
