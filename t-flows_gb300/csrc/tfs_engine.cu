@@ -811,24 +811,38 @@ extern "C" int tfs_get_option(const tfs_handle *h, int option, int *value)
 
 // ------------------------------------------------------ graph capture
 
-// DIC recurrence (Prec_Form.f90:32-40): one launch per large level, the tail
-// in one block.  Returns the number of kernels launched.
-// Bytes of shared memory of the one-block DIC for arithmetic T, 0 when it
-// does not run (the vector does not fit, or TFS_OPT_DIC_BLOCK = 0).
+// Whether the one-block DIC runs for arithmetic T (1) or not (0:
+// TFS_OPT_DIC_BLOCK = 0, or the vector and three level slots do not fit);
+// *bytes its dynamic shared memory.
 template <typename T>
-static int dic_block_bytes(const tfs_handle *h)
+static int dic_block_kind(const tfs_handle *h, int *bytes = nullptr)
 {
     if (!h->dic_block || h->layout != TFS_LAYOUT_LEVELS) return 0;
-    return sizeof(T) == 8 ? h->dicb_bytes64 : h->dicb_bytes32;
+    const int r = sizeof(T) == 8 ? h->dicb_bytes64 : h->dicb_bytes32;
+    if (!r) return 0;
+    if (bytes) *bytes = r;
+    return 1;
 }
 
+// One-block DIC application z1 = M^-1 b1 (MODE 0) or recurrence (MODE 2).
+template <typename T, int MODE>
+static cudaError_t launch_dic_one_block(tfs_handle *h, cudaStream_t s, int bytes, const T *val, T *d,
+                                        const T *b1, T *z1)
+{
+    k_dic_block<T, MODE><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), val, d, b1, z1, h->d_lvl_begin, h->n_levels,
+                                                        dicb_slot<T>(h->dicb_rm, h->dicb_ents),
+                                                        sizeof(T) == 8 ? h->dicb_slots64 : h->dicb_slots32, h->st);
+    return cudaGetLastError();
+}
+
+// DIC recurrence (Prec_Form.f90:32-40): one launch per large level, the tail
+// in one block, or the one-block kernel.  Returns the number of kernels
+// launched.
 static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
-    if (const int bytes = dic_block_bytes<double>(h)) {
-        k_dic_block<double, 2><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), h->val, h->v.d, nullptr, nullptr,
-                                                              h->d_lvl_begin, h->n_levels,
-                                                              dicb_slot<double>(h->dicb_rm, h->dicb_ents),
-                                                              h->dicb_slots64, h->st);
+    int bytes = 0;
+    if (dic_block_kind<double>(h, &bytes)) {
+        launch_dic_one_block<double, 2>(h, s, bytes, h->val, h->v.d, nullptr, nullptr);
         return 1;
     }
     int cnt = 0;
@@ -895,13 +909,12 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
     if constexpr (sizeof(T) == 8) { val = (const T *)h->val; d = (T *)h->v.d; }
     else { val = (const T *)h->val32; d = (T *)h->f.d; }
     if (nr == 1 && !fuse_l0) {
-        if (const int bytes = dic_block_bytes<T>(h)) {
-            k_dic_block<T, 0><<<1, TFS_DICB_TPB, bytes, s>>>(
-                A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, dicb_slot<T>(h->dicb_rm, h->dicb_ents),
-                sizeof(T) == 8 ? h->dicb_slots64 : h->dicb_slots32, h->st);
+        int bytes = 0;
+        if (dic_block_kind<T>(h, &bytes)) {
+            cudaError_t e = launch_dic_one_block<T, 0>(h, s, bytes, val, d, b1, z1);
+            if (e != cudaSuccess) return tfs_engine_error(e, "one-block DIC launch");
             h->dicb_used = 1;
             (*count)++;
-            CKL("one-block DIC launch");
             return TFS_OK;
         }
     }
@@ -966,7 +979,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
 static int dic_l0_rows(const tfs_handle *h, int method, int prec)
 {
     if (method != TFS_CG || prec != 2 || !h->fuse_l0) return 0;
-    if (h->precision == TFS_MIXED ? dic_block_bytes<float>(h) : dic_block_bytes<double>(h)) return 0;
+    if (h->precision == TFS_MIXED ? dic_block_kind<float>(h) : dic_block_kind<double>(h)) return 0;
     if (h->precision == TFS_MIXED && !h->vec4) return 0;
     if (h->precision != TFS_MIXED && h->fuse_l0 != 2) return 0;
     const int tail_at = sweep_tail_at(h, 1);
