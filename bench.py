@@ -1389,7 +1389,7 @@ def main(argv=None) -> int:
     ap.add_argument("--modes", default="fp64,mixed",
                     help="arithmetic legs to run (profiling runs may pick one)")
     ap.add_argument("--option", action="append", default=[], metavar="NAME=VALUE",
-                    help="a TFS_OPT_* option of the single-system solver, e.g. SPMV_REVERSE=0 (repeatable)")
+                    help="a TFS_OPT_* option of the single-system solver, e.g. PDL=0 (repeatable)")
     ap.add_argument("--eager", action="store_true",
                     help="launch the solve kernels from a host loop instead of a CUDA graph "
                          "(TFS_OPT_LAUNCH = 1), for kernel-level profiling")
