@@ -11,48 +11,57 @@
 //   - the swept vector lives in shared memory (one value per row, in place:
 //     y, then y / (D + TINY), then z), so a step's gathers are shared-memory
 //     loads;
-//   - each level's rows -- their SELL slices of column indices and values
-//     (uniform or per-slice widths), geometry, diagonal and (forward)
-//     right-hand side, contiguous in global memory because levels start on
-//     slice boundaries -- are staged into a ring of R shared-memory slots by
-//     16-byte cp.async copies issued R - 1 levels before the level runs, so
-//     a step waits for no global load;
-//   - the block's threads are split: the first half sweeps the levels'
-//     rows, the second half stages the levels, and the two halves meet only
-//     at per-slot mbarriers: a copy thread's cp.async.mbarrier.arrive fires
-//     on the slot's "full" barrier once its copies of the level have landed,
-//     and a row thread arrives on the slot's "empty" barrier once it is done
-//     with the level; the row threads synchronise among themselves with a
-//     named barrier (bar.sync, which orders their shared-memory stores);
-//     the level records (first row, rows, first entry, entries) and the
-//     slice-offset table are built in shared memory once;
-//   - a step of the row threads is then one completed-phase test of the
-//     slot's barrier, the row's shared-memory loads and arithmetic and one
-//     barrier of the 256 row threads.
-// Measured on plain_50 (binary32 application): one __syncthreads of the
-// whole block per level with the copies issued by every thread 336 us,
-// issued by the copy half 233 us.
-// L1 prefetches in place of the ring measured slower than no prefetch at all
-// (plain_50 binary64: 529 against 402 us per application).
+//   - consecutive levels are grouped (host side) so that a group's rows and
+//     SELL entries fit one of R ring slots; a group's rows -- geometry,
+//     diagonal, (forward) right-hand side, column indices and values, one
+//     contiguous range of each array because levels start on slice
+//     boundaries -- are staged into its slot by five bulk asynchronous copies
+//     (cp.async.bulk, completion counted in bytes on the slot's "full"
+//     mbarrier) that one lane of a copy warp issues as soon as the slot's
+//     previous group is done;
+//   - the 256 row threads sweep a group level by level with one named
+//     barrier (bar.sync) per level, test the slot's "full" barrier once per
+//     group and release the slot with one arrival on its "empty" barrier;
+//   - the level records (first row, rows, first entry, entries), the group
+//     table and the slice-offset table are built in shared memory once.
+// Measured on plain_50 per binary32 / binary64 application: one 16-byte
+// cp.async per thread and level with every copy thread's and row thread's
+// arrival on per-level barriers 189 / 245 us (the copies' 256 + 256 barrier
+// arrivals per level were the bound: 133 / 208 us with no row arithmetic at
+// all); one bulk copy set and one arrival per level 139 / 232 us (issuing a
+// level's five bulk copies takes the copy lane about 500 cycles, testing the
+// barrier and releasing the slot the row threads about 400); levels grouped
+// into two slots (this kernel) 113 / 228 us (3 or 4 slots: 116 / 239,
+// 119 / 242).  Loading each row thread's next-level operands from the slot
+// during the current level measured slower (129 / 252 us; 146 / 248 with the
+// gathers kept ahead of those loads).  Binary64 is bound by GB300's narrow
+// binary64 pipe: a row's chain of dependent binary64 operations sets each
+// level step.
 //
 // Every row does exactly sweep_row's arithmetic (the reference's order of
 // terms: Prec_Solve.f90:46-67, Prec_Form.f90:32-40), so the results are
-// bitwise those of the per-level schedule.  Every copy is a 16-byte aligned
-// cp.async of the block's own, in-bounds data.  No wait depends on another
-// block: the mbarrier waits are on this block's own copies and row threads,
-// and each is bounded (TFS_DICB_WAIT_NS of global time); a wait that runs
-// out raises the block's abort flag, after which no thread waits on an
-// mbarrier again (the results are then garbage), every thread still passes
-// the same named barriers, the copy threads wait for their own copies before
-// they exit, and the solve ends with TFS_ERR_TIMEOUT.
+// bitwise those of the per-level schedule.  Every bulk copy is of the
+// block's own, in-bounds data, 16-byte aligned at both ends (the host checks
+// the base addresses; the copy lane checks each group's and stops on a
+// misaligned one).  No wait depends on another block: the mbarrier waits
+// are on this block's own copies and row threads, and each is bounded
+// (TFS_DICB_WAIT_NS of global time); a wait that runs out raises the
+// block's abort flag, after which no thread waits on an mbarrier again, no
+// copy is issued and no row is read from a slot (a slot may then hold
+// another group's rows; the results are garbage), every row thread still
+// passes the same named barriers, the copy lane waits (bounded, regardless
+// of the flag) for the copies it issued to land before it leaves, and the
+// solve ends with TFS_ERR_TIMEOUT.
 #pragma once
 #include "tfs_kernels.cuh"
 
 namespace tfs {
 
-#define TFS_DICB_TPB 512
-#define TFS_DICB_ROWS (TFS_DICB_TPB / 2)     // threads sweeping rows; the others stage levels
-#define TFS_DICB_MAX_SLOTS 8
+#define TFS_DICB_ROWS 256                    // threads sweeping rows
+#define TFS_DICB_TPB (TFS_DICB_ROWS + 32)    // + one copy warp (its lane 0 issues the copies)
+#ifndef TFS_DICB_SLOTS
+#define TFS_DICB_SLOTS 2                     // ring slots (each holds one group of levels)
+#endif
 #define TFS_DICB_MAX_LEVELS 4096
 #define TFS_DICB_ROW_BAR 1                   // named barrier of the row threads
 #ifndef TFS_DICB_WAIT_NS
@@ -60,9 +69,9 @@ namespace tfs {
 #endif
 
 // Byte offsets inside one ring slot of `rm` rows and `ents` SELL entries
-// (rm and ents multiples of 32, so every part starts on a 16-byte boundary):
-// geometry, diagonal, right-hand side, column indices and values of one
-// level.
+// (rm and ents multiples of 32, so every part starts on a 128-byte
+// boundary): geometry, diagonal, right-hand side, column indices and values
+// of one group of levels.
 struct DicbSlot {
     int rm, ents, off_d, off_b, off_col, off_val, bytes;
 };
@@ -89,11 +98,12 @@ __host__ __device__ inline int dicb_vec_bytes(int n_rows)
 }
 
 // Shared memory of the level records (one int4 per level: first row, rows,
-// first SELL entry, entries) and the slice-offset table (n_rows / 32 + 1
-// ints), rounded to 16 bytes.
-__host__ __device__ inline int dicb_table_bytes(int n_levels, int n_rows)
+// first SELL entry, entries), the group table (first level of every group,
+// n_groups + 1 ints) and the slice-offset table (n_rows / 32 + 1 ints),
+// rounded to 16 bytes.
+__host__ __device__ inline int dicb_table_bytes(int n_levels, int n_groups, int n_rows)
 {
-    return n_levels * 16 + (((n_rows >> 5) + 1) * 4 + 15) / 16 * 16;
+    return n_levels * 16 + (((n_groups + 1) + (n_rows >> 5) + 1) * 4 + 15) / 16 * 16;
 }
 
 // Shared memory of the ring's R full and R empty mbarriers and the abort
@@ -108,37 +118,30 @@ __device__ __forceinline__ uint32_t dicb_smem_addr(const void *p)
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void dicb_cp16(void *dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" : : "r"(dicb_smem_addr(dst)), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void dicb_commit()
-{
-    asm volatile("cp.async.commit_group;" : : : "memory");
-}
-
-__device__ __forceinline__ void dicb_wait_all()
-{
-    asm volatile("cp.async.wait_all;" : : : "memory");
-}
-
 __device__ __forceinline__ void dicb_mbar_init(uint64_t *bar, unsigned count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(dicb_smem_addr(bar)), "r"(count) : "memory");
 }
 
-// Arrive on bar once every cp.async the thread has issued so far has landed
-// (the pending count is not raised first: the barrier's expected count
-// includes this arrival).
-__device__ __forceinline__ void dicb_mbar_arrive_copies(uint64_t *bar)
-{
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" : : "r"(dicb_smem_addr(bar)) : "memory");
-}
-
 __device__ __forceinline__ void dicb_mbar_arrive(uint64_t *bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(dicb_smem_addr(bar)) : "memory");
+}
+
+// Arrive on bar and raise its pending transaction count by `bytes`, the
+// bytes the bulk copies issued next will deliver.
+__device__ __forceinline__ void dicb_mbar_expect(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 : : "r"(dicb_smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+// from global to this block's shared memory, counted on bar when it lands.
+__device__ __forceinline__ void dicb_bulk(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 : : "r"(dicb_smem_addr(dst)), "l"(src), "r"(bytes), "r"(dicb_smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool dicb_mbar_test(uint64_t *bar, unsigned parity)
@@ -174,27 +177,6 @@ __device__ __forceinline__ void dicb_row_sync()
     asm volatile("bar.sync %0, %1;" : : "n"(TFS_DICB_ROW_BAR), "n"(TFS_DICB_ROWS) : "memory");
 }
 
-// Stage the level of record lr (first row, rows, first entry, entries)
-// into `slot` (each copy thread, ct = 0 .. TFS_DICB_TPB - TFS_DICB_ROWS - 1,
-// its share of 16-byte chunks).  PART 0: forward (geometry, d, b, entries);
-// 1: backward (no b); 2: the recurrence (geometry and entries only).
-template <typename T, int PART>
-__device__ __forceinline__ void dicb_stage(unsigned char *slot, const DicbSlot &L, const SellDev &A,
-                                           const T *val, const T *d, const T *b, int4 lr, int ct)
-{
-    const int r0 = lr.x, nr = lr.y, e0 = lr.z, ne = lr.w;
-    constexpr int NC = TFS_DICB_TPB - TFS_DICB_ROWS;
-    auto copy = [&](unsigned char *dst, const void *src, int bytes) {
-        for (int o = ct * 16; o < bytes; o += NC * 16)
-            dicb_cp16(dst + o, (const unsigned char *)src + o);
-    };
-    copy(slot, A.rowinfo + r0, nr * 4);
-    if (PART != 2) copy(slot + L.off_d, d + r0, nr * (int)sizeof(T));
-    if (PART == 0) copy(slot + L.off_b, b + r0, nr * (int)sizeof(T));
-    copy(slot + L.off_col, A.col + e0, ne * 4);
-    copy(slot + L.off_val, val + e0, ne * (int)sizeof(T));
-}
-
 // The ring's per-slot barriers and the block's abort flag.
 struct DicbSync {
     uint64_t *full, *empty;   // R each
@@ -205,8 +187,9 @@ struct DicbSync {
 // the slot): acc - sum a_j s[col_j] in ascending j (PART 0 and 1), or
 // acc - sum s[col_j] a_j a_j (PART 2); up to 8 entries have every column
 // index, value and gather issued before the in-order chain of updates.
-// Measured on plain_50: binary32 219 -> 189 us per application; with the
-// binary64 updates predicated like the binary32 ones, 286 -> 367 us.
+// Measured on plain_50 (ungrouped ring): binary32 219 -> 189 us per
+// application; with the binary64 updates predicated like the binary32
+// ones, 286 -> 367 us.
 template <typename T, int PART>
 __device__ __forceinline__ T dicb_row(T acc, const T *s, const int *scol, const T *sval, int e0, int j0, int j1)
 {
@@ -241,61 +224,105 @@ __device__ __forceinline__ T dicb_row(T acc, const T *s, const int *scol, const 
     return acc;
 }
 
-// One sweep of k_dic_block over all levels, ascending (DIR > 0) or
-// descending, through the ring of R slots.  g0: the number of levels staged
-// by the sweeps before this one (slot and barrier phase of the q-th level
-// of this sweep: (g0 + q) % R and (g0 + q) / R).  Copy threads stage the
-// levels, row threads sweep them; neither waits for the whole block.
-// lr: the level records in shared memory.
+// One sweep of k_dic_block over all groups of levels, ascending (DIR > 0)
+// or descending, through the ring of R slots.  g0: the number of groups
+// staged by the sweeps before this one (slot and barrier phase of the q-th
+// group of this sweep: (g0 + q) % R and (g0 + q) / R).  PART 0: forward
+// (geometry, d, b, entries staged); 1: backward (no b); 2: the recurrence
+// (geometry and entries only).  lr: level records, gs: group table, so:
+// slice offsets, all in shared memory.
 template <typename T, int PART, int DIR>
 __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int4 *lr, const int *so,
-                                           int n_levels, int g0, const DicbSync &y)
+                                           const T *val, const T *d, const T *b, const int4 *lr, const int *gs,
+                                           const int *so, int n_groups, int g0, const DicbSync &y)
 {
     const int tid = threadIdx.x, W = A.width;
     int slot = g0 % R;
     unsigned ph = (unsigned)((g0 / R) & 1);   // phase parity of the slot's current use
-    int l = DIR > 0 ? 0 : n_levels - 1;
     if (tid >= TFS_DICB_ROWS) {
-        const int ct = tid - TFS_DICB_ROWS;
-        for (int q = 0; q < n_levels; q++, l += DIR) {
-            // the slot's previous use (level g0 + q - R) must be done by the row threads
-            if (g0 + q >= R) dicb_mbar_wait(y.empty + slot, ph ^ 1u, y.abort);
-            dicb_stage<T, PART>(ring + (size_t)slot * L.bytes, L, A, val, d, b, lr[l], ct);
-            dicb_mbar_arrive_copies(y.full + slot);
+        if (tid != TFS_DICB_ROWS) return;
+        // the copy lane
+        int issued = 0;
+        for (int q = 0; q < n_groups; q++) {
+            const int g = DIR > 0 ? q : n_groups - 1 - q;
+            // the slot's previous group must be done by the row threads;
+            // after an abort no more copies
+            if ((g0 + q >= R && !dicb_mbar_wait(y.empty + slot, ph ^ 1u, y.abort)) || *y.abort) break;
+            const int4 first = lr[gs[g]], last = lr[gs[g + 1] - 1];
+            const int r0 = first.x, nr = last.x + last.y - first.x;
+            const int e0 = first.z, ne = last.z + last.w - first.z;
+            const unsigned bytes = (unsigned)nr * (4u + (PART != 2 ? (unsigned)sizeof(T) : 0u) +
+                                                   (PART == 0 ? (unsigned)sizeof(T) : 0u)) +
+                                   (unsigned)ne * (4u + (unsigned)sizeof(T));
+            const unsigned long long chk =
+                (unsigned long long)(A.rowinfo + r0) | (unsigned long long)(A.col + e0) |
+                (unsigned long long)(val + e0) | (PART != 2 ? (unsigned long long)(d + r0) : 0ull) |
+                (PART == 0 ? (unsigned long long)(b + r0) : 0ull) | (unsigned long long)(nr * 4) |
+                (unsigned long long)(ne * 4);
+            if ((chk & 15ull) || nr > L.rm || ne > L.ents) {
+                *y.abort = 1;
+                break;
+            }
+            unsigned char *sl = ring + (size_t)slot * L.bytes;
+            dicb_mbar_expect(y.full + slot, bytes);
+            dicb_bulk(sl, A.rowinfo + r0, nr * 4, y.full + slot);
+            if (PART != 2) dicb_bulk(sl + L.off_d, d + r0, nr * (int)sizeof(T), y.full + slot);
+            if (PART == 0) dicb_bulk(sl + L.off_b, b + r0, nr * (int)sizeof(T), y.full + slot);
+            if (ne) {
+                dicb_bulk(sl + L.off_col, A.col + e0, ne * 4, y.full + slot);
+                dicb_bulk(sl + L.off_val, val + e0, ne * (int)sizeof(T), y.full + slot);
+            }
+            issued++;
             if (++slot == R) { slot = 0; ph ^= 1u; }
+        }
+        if (*y.abort) {
+            // the copies of the last min(R, issued) groups may still be in
+            // flight: wait for them to land (bounded; the flag is not asked)
+            for (int k = 0; k < R && k < issued; k++) {
+                if (--slot < 0) { slot = R - 1; ph ^= 1u; }
+                const unsigned long long t0 = gtimer();
+                while (!dicb_mbar_test(y.full + slot, ph) && gtimer() - t0 < TFS_DICB_WAIT_NS) {
+                }
+            }
         }
         return;
     }
-    for (int q = 0; q < n_levels; q++, l += DIR) {
-        const int4 rec = lr[l];
-        dicb_mbar_wait(y.full + slot, ph, y.abort);
+    for (int q = 0; q < n_groups; q++) {
+        const int g = DIR > 0 ? q : n_groups - 1 - q;
+        const int la = gs[g], lb = gs[g + 1];
+        // after an abort the slot may hold another group's rows: no row reads it
+        const bool ok = dicb_mbar_wait(y.full + slot, ph, y.abort);
+        const int4 first = lr[la];
+        const int rg = first.x, sg = first.z;   // the group's first row and entry
         const unsigned char *sl = ring + (size_t)slot * L.bytes;
         const uint32_t *sinfo = reinterpret_cast<const uint32_t *>(sl);
         const T *sd = reinterpret_cast<const T *>(sl + L.off_d);
         const T *sb = reinterpret_cast<const T *>(sl + L.off_b);
         const int *scol = reinterpret_cast<const int *>(sl + L.off_col);
         const T *sval = reinterpret_cast<const T *>(sl + L.off_val);
-        const int r0 = rec.x, nr = rec.y, sb0 = rec.z;
-        for (int k = tid; k < nr; k += TFS_DICB_ROWS) {
-            const uint32_t info = sinfo[k];
-            const int len = (int)(info & 0xffffu), dpos = (int)(info >> 16);
-            // entry j of the row at e0 + 32 j of the slot
-            const int e0 = (W ? (k & ~31) * W : so[(r0 + k) >> 5] - sb0) + (k & 31);
-            const int i = r0 + k;
-            if (PART == 2) {
-                if (len == 0) { s[i] = (T)1; continue; }
-                s[i] = (T)1 / dicb_row<T, 2>(sval[e0 + (dpos << 5)], s, scol, sval, e0, 0, dpos);
-            } else if (PART == 0) {
-                if (len == 0) { s[i] = (T)0; continue; }
-                s[i] = dicb_row<T, 0>(sb[k], s, scol, sval, e0, 0, dpos) * sd[k];
-            } else {
-                if (len == 0) continue;   // 0 since the forward sweep
-                s[i] = dicb_row<T, 1>(s[i], s, scol, sval, e0, dpos + 1, len) * sd[k];
+        for (int lq = 0; lq < lb - la; lq++) {
+            const int4 rec = lr[DIR > 0 ? la + lq : lb - 1 - lq];
+            const int nr = ok ? rec.y : 0;
+            for (int k = tid; k < nr; k += TFS_DICB_ROWS) {
+                const int i = rec.x + k, kk = i - rg;   // row in the vector and in the slot
+                const uint32_t info = sinfo[kk];
+                const int len = (int)(info & 0xffffu), dpos = (int)(info >> 16);
+                // entry j of the row at e0 + 32 j of the slot
+                const int e0 = (W ? (kk & ~31) * W : so[i >> 5] - sg) + (kk & 31);
+                if (PART == 2) {
+                    if (len == 0) { s[i] = (T)1; continue; }
+                    s[i] = (T)1 / dicb_row<T, 2>(sval[e0 + (dpos << 5)], s, scol, sval, e0, 0, dpos);
+                } else if (PART == 0) {
+                    if (len == 0) { s[i] = (T)0; continue; }
+                    s[i] = dicb_row<T, 0>(sb[kk], s, scol, sval, e0, 0, dpos) * sd[kk];
+                } else {
+                    if (len == 0) continue;   // 0 since the forward sweep
+                    s[i] = dicb_row<T, 1>(s[i], s, scol, sval, e0, dpos + 1, len) * sd[kk];
+                }
             }
+            dicb_row_sync();   // this level's rows visible to the next
         }
-        dicb_mbar_arrive(y.empty + slot);   // done with the slot
-        dicb_row_sync();                    // this level's rows visible to the next
+        if (tid == TFS_DICB_ROWS - 32) dicb_mbar_arrive(y.empty + slot);   // done with the slot
         if (++slot == R) { slot = 0; ph ^= 1u; }
     }
 }
@@ -303,23 +330,26 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
 // MODE 0: z = M^-1 b (forward sweep, scaling, backward sweep) with the
 // factor d; MODE 2: the DIC factor d from the matrix (binary64; b and z
 // unused).  One block of TFS_DICB_TPB threads; dynamic shared memory: the
-// vector (dicb_vec_bytes), R slots of L.bytes, the level records and the
-// slice-offset table (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS levels) and the
-// ring's 2 R mbarriers and abort flag (dicb_sync_bytes).  Rows past
-// lvl_begin[n_levels] (the layout's final padding) are never touched.
+// vector (dicb_vec_bytes), R slots of L.bytes, the level records, the group
+// table (groups[0 .. n_groups]: first level of every group, then n_levels)
+// and the slice-offset table (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS
+// levels), the ring's 2 R mbarriers and the abort flag (dicb_sync_bytes).
+// Rows past lvl_begin[n_levels] (the layout's final padding) are never
+// touched.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(TFS_DICB_TPB, 1)
 k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const int *__restrict__ lvl_begin,
-            int n_levels, DicbSlot L, int R, DevState *st)
+            int n_levels, const int *__restrict__ groups, int n_groups, DicbSlot L, int R, DevState *st)
 {
     extern __shared__ __align__(128) unsigned char dicb_smem[];
     const int n_rows = __ldg(lvl_begin + n_levels);
     T *s = reinterpret_cast<T *>(dicb_smem);
     unsigned char *ring = dicb_smem + dicb_vec_bytes<T>(n_rows);
     int4 *lr = reinterpret_cast<int4 *>(ring + (size_t)R * L.bytes);
-    int *so = reinterpret_cast<int *>(lr + n_levels);
+    int *gs = reinterpret_cast<int *>(lr + n_levels);
+    int *so = gs + n_groups + 1;
     uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(lr) +
-                                                  dicb_table_bytes(n_levels, n_rows));
+                                                  dicb_table_bytes(n_levels, n_groups, n_rows));
     DicbSync y{bars, bars + R, reinterpret_cast<volatile int *>(bars + 2 * R)};
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
@@ -327,6 +357,7 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     if (MODE == 0 && tid == 0) st->t_sweep0 = gtimer();
     for (int q = tid; q <= (n_rows >> 5); q += TFS_DICB_TPB)
         so[q] = A.width ? q * 32 * A.width : __ldg(A.slice_off + q);
+    for (int q = tid; q <= n_groups; q += TFS_DICB_TPB) gs[q] = __ldg(groups + q);
     __syncthreads();
     for (int l = tid; l < n_levels; l += TFS_DICB_TPB) {
         const int r0 = __ldg(lvl_begin + l), r1 = __ldg(lvl_begin + l + 1);
@@ -334,33 +365,33 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     }
     if (tid == 0) {
         for (int k = 0; k < R; k++) {
-            dicb_mbar_init(y.full + k, TFS_DICB_TPB - TFS_DICB_ROWS);
-            dicb_mbar_init(y.empty + k, TFS_DICB_ROWS);
+            dicb_mbar_init(y.full + k, 1);    // the copy lane's arrival (+ the copies' bytes)
+            dicb_mbar_init(y.empty + k, 1);   // one row thread's arrival
         }
         *y.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
     }
     __syncthreads();
     const bool row = tid < TFS_DICB_ROWS;
     if (MODE == 2) {
-        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, 0, y);
+        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, 0, y);
         if (row)
             for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) d[i] = s[i];
     } else {
-        dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, 0, y);
+        dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, 0, y);
         if (row) {
             // Every row's backward start value y_i / (D_i + TINY)
-            // (Prec_Solve.f90:55-57), while the copy threads stage the
-            // backward sweep's first levels.
+            // (Prec_Solve.f90:55-57), while the copy lane stages the
+            // backward sweep's first groups.
 #pragma unroll 4
             for (int i = tid; i < n_rows; i += TFS_DICB_ROWS)
                 if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
             dicb_row_sync();
         }
-        dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lr, so, n_levels, n_levels, y);
+        dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, n_groups, y);
         if (row)
             for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) z[i] = s[i];
     }
-    if (!row) dicb_wait_all();   // no copy of this block outlives it
     __syncthreads();
     if (tid == 0 && *y.abort) {
         st->status = TFS_ERR_TIMEOUT;

@@ -575,35 +575,54 @@ static int build_layout(tfs_handle *h, int kind)
         h->pf_tail_level = l;
         h->pf_ok = l < nl && l <= h->tail_level;
         // One-block DIC: the swept vector (every row of the levels), a ring
-        // of at least 3 (at most TFS_DICB_MAX_SLOTS) slots of the widest
-        // level's rows and entries, and the level and slice-offset tables in
-        // the block's shared memory.
-        h->dicb_bytes64 = h->dicb_bytes32 = h->dicb_slots64 = h->dicb_slots32 = h->dicb_rm = h->dicb_ents = 0;
-        if (kind == TFS_LAYOUT_LEVELS && nl <= TFS_DICB_MAX_LEVELS) {
+        // of TFS_DICB_SLOTS slots, each holding one group of consecutive
+        // levels, and the level, group and slice-offset tables in the block's
+        // shared memory.  The slots share what the vector and the tables
+        // leave, rows and entries in the widest level's proportion; a slot
+        // must hold the widest level.  Groups are filled greedily.
+        h->dicb64 = h->dicb32 = tfs_handle::DicbPlan{};
+        h->lvl_tab.assign(h->lvl_begin.begin(), h->lvl_begin.end());
+        if (kind == TFS_LAYOUT_LEVELS && nl <= TFS_DICB_MAX_LEVELS && h->lvl_begin[nl] <= (1 << 24)) {
             int optin = 0;
             CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+            const int rows = h->lvl_begin[nl];
+            auto lvl_ents = [&](int l) { return slice_off[h->lvl_begin[l + 1] >> 5] - slice_off[h->lvl_begin[l] >> 5]; };
             int rm = 32, ents = 32;
             for (int l = 0; l < nl; l++) {
-                const int a = h->lvl_begin[l], z = h->lvl_begin[l + 1];
-                rm = std::max(rm, z - a);
-                ents = std::max(ents, slice_off[z >> 5] - slice_off[a >> 5]);
+                rm = std::max(rm, h->lvl_begin[l + 1] - h->lvl_begin[l]);
+                ents = std::max(ents, lvl_ents(l));
             }
-            const int64_t rows = h->lvl_begin[nl];
-            h->dicb_rm = rm;
-            h->dicb_ents = ents;
-            auto fit = [&](int vec, int slot, int *bytes, int *slots) {
-                if (rows > INT32_MAX / 16) return;
-                const int tables = dicb_table_bytes(nl, (int)rows) + dicb_sync_bytes(TFS_DICB_MAX_SLOTS);
-                const int64_t room = (int64_t)optin - vec - tables;
-                const int64_t r = room > 0 ? std::min<int64_t>(TFS_DICB_MAX_SLOTS, room / slot) : 0;
-                if (r < 3) return;
-                *slots = (int)r;
-                *bytes = vec + (int)r * slot + tables;
+            auto plan = [&](int tsize, tfs_handle::DicbPlan &P) {
+                const int R = TFS_DICB_SLOTS;
+                const int vec = (rows * tsize + 127) & ~127;
+                const int64_t room = (int64_t)optin - vec - dicb_table_bytes(nl, nl, rows) - dicb_sync_bytes(R);
+                const int64_t per_row = 4 + 2 * tsize, per_ent = 4 + tsize;
+                const int64_t widest = per_row * rm + per_ent * ents;
+                if (room < R * widest) return;
+                const double k = (double)(room / R) / (double)widest;   // >= 1
+                const int rm_c = std::max(rm, (int)(rm * k) & ~31), ents_c = std::max(ents, (int)(ents * k) & ~31);
+                if (per_row * rm_c + per_ent * ents_c > room / R) return;
+                P.rm = rm_c;
+                P.ents = ents_c;
+                P.group_off = (int)h->lvl_tab.size();
+                h->lvl_tab.push_back(0);
+                int gr = 0, ge = 0;
+                for (int l = 0; l < nl; l++) {
+                    const int lrows = h->lvl_begin[l + 1] - h->lvl_begin[l], lents = lvl_ents(l);
+                    if (l > 0 && (gr + lrows > rm_c || ge + lents > ents_c)) {
+                        h->lvl_tab.push_back(l);
+                        gr = ge = 0;
+                    }
+                    gr += lrows;
+                    ge += lents;
+                }
+                h->lvl_tab.push_back(nl);
+                P.n_groups = (int)h->lvl_tab.size() - P.group_off - 1;
+                P.bytes = vec + R * (int)(per_row * rm_c + per_ent * ents_c) + dicb_table_bytes(nl, P.n_groups, rows) +
+                          dicb_sync_bytes(R);
             };
-            fit(dicb_vec_bytes<double>((int)rows), dicb_slot<double>(rm, ents).bytes, &h->dicb_bytes64,
-                &h->dicb_slots64);
-            fit(dicb_vec_bytes<float>((int)rows), dicb_slot<float>(rm, ents).bytes, &h->dicb_bytes32,
-                &h->dicb_slots32);
+            plan(8, h->dicb64);
+            plan(4, h->dicb32);
             static std::once_flag attr_once;
             std::call_once(attr_once, [optin] {
                 cudaFuncSetAttribute(k_dic_block<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -611,8 +630,9 @@ static int build_layout(tfs_handle *h, int kind)
                 cudaFuncSetAttribute(k_dic_block<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
             });
         }
-        if ((rc = dalloc(h, &h->d_lvl_begin, nl + 1))) return rc;
-        CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_begin.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, h->stream));
+        if ((rc = dalloc(h, &h->d_lvl_begin, h->lvl_tab.size()))) return rc;
+        CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_tab.data(), sizeof(int) * h->lvl_tab.size(), cudaMemcpyHostToDevice,
+                           h->stream));
     }
     spmv_kind_setup(h);
     CK(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * n_int, cudaMemcpyHostToDevice, h->stream));
@@ -812,27 +832,36 @@ extern "C" int tfs_get_option(const tfs_handle *h, int option, int *value)
 // ------------------------------------------------------ graph capture
 
 // Whether the one-block DIC runs for arithmetic T (1) or not (0:
-// TFS_OPT_DIC_BLOCK = 0, or the vector and three level slots do not fit);
-// *bytes its dynamic shared memory.
+// TFS_OPT_DIC_BLOCK = 0, or the vector and two slots of the widest level do
+// not fit); *bytes its dynamic shared memory.
 template <typename T>
 static int dic_block_kind(const tfs_handle *h, int *bytes = nullptr)
 {
     if (!h->dic_block || h->layout != TFS_LAYOUT_LEVELS) return 0;
-    const int r = sizeof(T) == 8 ? h->dicb_bytes64 : h->dicb_bytes32;
-    if (!r) return 0;
-    if (bytes) *bytes = r;
+    const tfs_handle::DicbPlan &P = sizeof(T) == 8 ? h->dicb64 : h->dicb32;
+    if (!P.bytes) return 0;
+    if (bytes) *bytes = P.bytes;
     return 1;
 }
 
 // One-block DIC application z1 = M^-1 b1 (MODE 0) or recurrence (MODE 2).
+// Its bulk copies want 16-byte aligned sources: every array it stages is a
+// cudaMalloc base or one offset by a multiple of 32 elements, checked here
+// anyway -- cudaErrorMisalignedAddress, with nothing launched, sends the
+// caller to the level kernels.  A launch error stays pending for the
+// caller's check.
 template <typename T, int MODE>
 static cudaError_t launch_dic_one_block(tfs_handle *h, cudaStream_t s, int bytes, const T *val, T *d,
                                         const T *b1, T *z1)
 {
-    k_dic_block<T, MODE><<<1, TFS_DICB_TPB, bytes, s>>>(sell_of(h), val, d, b1, z1, h->d_lvl_begin, h->n_levels,
-                                                        dicb_slot<T>(h->dicb_rm, h->dicb_ents),
-                                                        sizeof(T) == 8 ? h->dicb_slots64 : h->dicb_slots32, h->st);
-    return cudaGetLastError();
+    const tfs_handle::DicbPlan &P = sizeof(T) == 8 ? h->dicb64 : h->dicb32;
+    const SellDev A = sell_of(h);
+    const uintptr_t chk = (uintptr_t)val | (uintptr_t)d | (uintptr_t)b1 | (uintptr_t)A.rowinfo | (uintptr_t)A.col;
+    if (chk & 15u) return cudaErrorMisalignedAddress;
+    k_dic_block<T, MODE><<<1, TFS_DICB_TPB, bytes, s>>>(A, val, d, b1, z1, h->d_lvl_begin, h->n_levels,
+                                                        h->d_lvl_begin + P.group_off, P.n_groups,
+                                                        dicb_slot<T>(P.rm, P.ents), TFS_DICB_SLOTS, h->st);
+    return cudaPeekAtLastError();
 }
 
 // DIC recurrence (Prec_Form.f90:32-40): one launch per large level, the tail
@@ -841,10 +870,9 @@ static cudaError_t launch_dic_one_block(tfs_handle *h, cudaStream_t s, int bytes
 static int launch_dic_form(tfs_handle *h, cudaStream_t s)
 {
     int bytes = 0;
-    if (dic_block_kind<double>(h, &bytes)) {
-        launch_dic_one_block<double, 2>(h, s, bytes, h->val, h->v.d, nullptr, nullptr);
+    if (dic_block_kind<double>(h, &bytes) &&
+        launch_dic_one_block<double, 2>(h, s, bytes, h->val, h->v.d, nullptr, nullptr) != cudaErrorMisalignedAddress)
         return 1;
-    }
     int cnt = 0;
     if (launch_levels<double, 1, 2>(h, s, h->val, h->v.d, nullptr, nullptr, nullptr, nullptr, nullptr,
                                     nullptr, &cnt))
@@ -912,10 +940,12 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
         int bytes = 0;
         if (dic_block_kind<T>(h, &bytes)) {
             cudaError_t e = launch_dic_one_block<T, 0>(h, s, bytes, val, d, b1, z1);
-            if (e != cudaSuccess) return tfs_engine_error(e, "one-block DIC launch");
-            h->dicb_used = 1;
-            (*count)++;
-            return TFS_OK;
+            if (e == cudaSuccess) {
+                h->dicb_used = 1;
+                (*count)++;
+                return TFS_OK;
+            }
+            if (e != cudaErrorMisalignedAddress) return tfs_engine_error(cudaGetLastError(), "one-block DIC launch");
         }
     }
     // Forward levels, both tails in one block, backward levels.

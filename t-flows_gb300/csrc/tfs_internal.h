@@ -132,16 +132,20 @@ struct tfs_handle {
     int spmv_chunks = 0;               // TFS_OPT_SPMV_GRID: 1 one block per 256-row chunk
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
-    int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC where the vector and three level slots fit
+    int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC where the vector and two slots of the widest level fit
     int dicb_used = 0;                 // the last DIC application launched was the one-block kernel
-    int dicb_rm = 0, dicb_ents = 0;    // one-block DIC: rows and SELL entries of a ring slot (the widest level)
-    int dicb_slots64 = 0, dicb_slots32 = 0;   // ring slots that fit (0: not used for that arithmetic)
+    // One-block DIC per arithmetic: shared memory (0: does not fit), ring
+    // slot capacity (rows and SELL entries), number of level groups and the
+    // offset of the group table in d_lvl_begin's allocation.
+    struct DicbPlan {
+        int bytes = 0, rm = 0, ents = 0, n_groups = 0, group_off = 0;
+    } dicb64, dicb32;
+    std::vector<int> lvl_tab;          // host copy of d_lvl_begin's allocation (levels, then both group tables)
     bool profiling = false;            // tfs_profile_prec: number the sweep launches
     int stamp_next = 0;                // next slot number while profiling
     std::vector<int> stamp_kind;       // per slot: level (forward), -1 - level (backward), 1 << 20 tail
     int pf_tail_level = 0;             // first level of the prefetching tail
     bool pf_ok = false;                // the prefetching tail can run
-    int dicb_bytes64 = 0, dicb_bytes32 = 0;   // shared memory of the one-block DIC, 0: does not fit
     int precision = TFS_FP64;
     std::vector<int> lvl_begin;        // internal row offset of every level (+end)
     std::vector<int32_t> levels_nat;   // level per natural row
