@@ -9,8 +9,8 @@
 // costs three L2 round trips (row geometry, entries, gathers of rows written
 // one step earlier by other threads): about 1.7 us.  Here:
 //   - the swept vector lives in shared memory (one value per row, in place:
-//     y, then y / (D + TINY), then z), so a step's gathers are shared-memory
-//     loads;
+//     y, then z; the backward start values y / (D + TINY) go through z in
+//     global memory), so a step's gathers are shared-memory loads;
 //   - consecutive levels are grouped (host side) so that a group's rows and
 //     SELL entries fit one of R ring slots; a group's rows -- geometry,
 //     diagonal, (forward) right-hand side, column indices and values, one
@@ -31,12 +31,17 @@
 // all); one bulk copy set and one arrival per level 139 / 232 us (issuing a
 // level's five bulk copies takes the copy lane about 500 cycles, testing the
 // barrier and releasing the slot the row threads about 400); levels grouped
-// into two slots (this kernel) 113 / 228 us (3 or 4 slots: 116 / 239,
-// 119 / 242).  Loading each row thread's next-level operands from the slot
-// during the current level measured slower (129 / 252 us; 146 / 248 with the
-// gathers kept ahead of those loads).  Binary64 is bound by GB300's narrow
-// binary64 pipe: a row's chain of dependent binary64 operations sets each
-// level step.
+// into two slots 113 / 228 us (3 or 4 slots: 116 / 239, 119 / 242), of
+// which the scaling pass between the sweeps (global loads of the geometry
+// and D, one division per row) took 24 / 48 us.  The scaling now runs in
+// the forward sweep, right after each row's value, for binary32 (the
+// backward sweep stages the start values from z like the right-hand side):
+// 106 us; for binary64 a division per row inside the sweep holds each level
+// back on the narrow binary64 pipe (245 us), so the binary64 application is
+// split into a forward kernel, a scaling grid over every SM and a backward
+// kernel: 186 us.  Loading each row thread's next-level operands from the
+// slot during the current level measured slower (129 / 252 us; 146 / 248
+// with the gathers kept ahead of those loads).
 //
 // Every row does exactly sweep_row's arithmetic (the reference's order of
 // terms: Prec_Solve.f90:46-67, Prec_Form.f90:32-40), so the results are
@@ -59,6 +64,9 @@ namespace tfs {
 
 #define TFS_DICB_ROWS 256                    // threads sweeping rows
 #define TFS_DICB_TPB (TFS_DICB_ROWS + 32)    // + one copy warp (its lane 0 issues the copies)
+#ifndef TFS_DICB_SPLIT64
+#define TFS_DICB_SPLIT64 1                   // binary64 application as forward kernel, scaling grid, backward kernel
+#endif
 #ifndef TFS_DICB_SLOTS
 #define TFS_DICB_SLOTS 2                     // ring slots (each holds one group of levels)
 #endif
@@ -228,13 +236,16 @@ __device__ __forceinline__ T dicb_row(T acc, const T *s, const int *scol, const 
 // or descending, through the ring of R slots.  g0: the number of groups
 // staged by the sweeps before this one (slot and barrier phase of the q-th
 // group of this sweep: (g0 + q) % R and (g0 + q) / R).  PART 0: forward
-// (geometry, d, b, entries staged); 1: backward (no b); 2: the recurrence
-// (geometry and entries only).  lr: level records, gs: group table, so:
-// slice offsets, all in shared memory.
-template <typename T, int PART, int DIR>
+// (geometry, d, the right-hand side b and entries staged; every row's
+// backward start value y_i / (D_i + TINY) (Prec_Solve.f90:55-57) also
+// written to t); 1: backward (geometry, d, the start values b and entries
+// staged); 2: the recurrence (geometry and entries only).  START = false:
+// the forward sweep leaves the start values to k_dic_scale.  lr: level
+// records, gs: group table, so: slice offsets, all in shared memory.
+template <typename T, int PART, int DIR, bool START = true>
 __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const DicbSlot &L, int R, const SellDev &A,
-                                           const T *val, const T *d, const T *b, const int4 *lr, const int *gs,
-                                           const int *so, int n_groups, int g0, const DicbSync &y)
+                                           const T *val, const T *d, const T *b, T *t, const int4 *lr,
+                                           const int *gs, const int *so, int n_groups, int g0, const DicbSync &y)
 {
     const int tid = threadIdx.x, W = A.width;
     int slot = g0 % R;
@@ -243,6 +254,11 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
         if (tid != TFS_DICB_ROWS) return;
         // the copy lane
         int issued = 0;
+        // the backward sweep stages the start values the forward sweep wrote:
+        // its first group is the forward sweep's last, so wait for the
+        // forward sweep's last release (use g0 - 1 of the ring)
+        if (PART == 1 && g0 > 0 && !dicb_mbar_wait(y.empty + (g0 - 1) % R, (unsigned)(((g0 - 1) / R) & 1), y.abort))
+            return;
         for (int q = 0; q < n_groups; q++) {
             const int g = DIR > 0 ? q : n_groups - 1 - q;
             // the slot's previous group must be done by the row threads;
@@ -251,13 +267,12 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
             const int4 first = lr[gs[g]], last = lr[gs[g + 1] - 1];
             const int r0 = first.x, nr = last.x + last.y - first.x;
             const int e0 = first.z, ne = last.z + last.w - first.z;
-            const unsigned bytes = (unsigned)nr * (4u + (PART != 2 ? (unsigned)sizeof(T) : 0u) +
-                                                   (PART == 0 ? (unsigned)sizeof(T) : 0u)) +
+            const unsigned bytes = (unsigned)nr * (4u + (PART != 2 ? 2u * (unsigned)sizeof(T) : 0u)) +
                                    (unsigned)ne * (4u + (unsigned)sizeof(T));
             const unsigned long long chk =
                 (unsigned long long)(A.rowinfo + r0) | (unsigned long long)(A.col + e0) |
                 (unsigned long long)(val + e0) | (PART != 2 ? (unsigned long long)(d + r0) : 0ull) |
-                (PART == 0 ? (unsigned long long)(b + r0) : 0ull) | (unsigned long long)(nr * 4) |
+                (PART != 2 ? (unsigned long long)(b + r0) : 0ull) | (unsigned long long)(nr * 4) |
                 (unsigned long long)(ne * 4);
             if ((chk & 15ull) || nr > L.rm || ne > L.ents) {
                 *y.abort = 1;
@@ -267,7 +282,7 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
             dicb_mbar_expect(y.full + slot, bytes);
             dicb_bulk(sl, A.rowinfo + r0, nr * 4, y.full + slot);
             if (PART != 2) dicb_bulk(sl + L.off_d, d + r0, nr * (int)sizeof(T), y.full + slot);
-            if (PART == 0) dicb_bulk(sl + L.off_b, b + r0, nr * (int)sizeof(T), y.full + slot);
+            if (PART != 2) dicb_bulk(sl + L.off_b, b + r0, nr * (int)sizeof(T), y.full + slot);
             if (ne) {
                 dicb_bulk(sl + L.off_col, A.col + e0, ne * 4, y.full + slot);
                 dicb_bulk(sl + L.off_val, val + e0, ne * (int)sizeof(T), y.full + slot);
@@ -314,12 +329,17 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
                     s[i] = (T)1 / dicb_row<T, 2>(sval[e0 + (dpos << 5)], s, scol, sval, e0, 0, dpos);
                 } else if (PART == 0) {
                     if (len == 0) { s[i] = (T)0; continue; }
-                    s[i] = dicb_row<T, 0>(sb[kk], s, scol, sval, e0, 0, dpos) * sd[kk];
+                    const T yi = dicb_row<T, 0>(sb[kk], s, scol, sval, e0, 0, dpos) * sd[kk];
+                    s[i] = yi;
+                    if (START) t[i] = yi / (sd[kk] + (T)TINY);   // not read by this sweep
                 } else {
-                    if (len == 0) continue;   // 0 since the forward sweep
-                    s[i] = dicb_row<T, 1>(s[i], s, scol, sval, e0, dpos + 1, len) * sd[kk];
+                    if (len == 0) { s[i] = (T)0; continue; }
+                    s[i] = dicb_row<T, 1>(sb[kk], s, scol, sval, e0, dpos + 1, len) * sd[kk];
                 }
             }
+            // the start values written to t must be visible to the bulk
+            // copies that stage them for the backward sweep
+            if (PART == 0 && START && lq == lb - la - 1) asm volatile("fence.proxy.async.global;" : : : "memory");
             dicb_row_sync();   // this level's rows visible to the next
         }
         if (tid == TFS_DICB_ROWS - 32) dicb_mbar_arrive(y.empty + slot);   // done with the slot
@@ -329,7 +349,10 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
 
 // MODE 0: z = M^-1 b (forward sweep, scaling, backward sweep) with the
 // factor d; MODE 2: the DIC factor d from the matrix (binary64; b and z
-// unused).  One block of TFS_DICB_TPB threads; dynamic shared memory: the
+// unused); MODE 3: the forward sweep alone, z = y; MODE 4: the backward
+// sweep alone from the start values in z (MODE 3, k_dic_scale, MODE 4 is
+// the binary64 application: the divisions of the scaling then run on every
+// SM instead of taking this block's narrow binary64 pipe).  One block of TFS_DICB_TPB threads; dynamic shared memory: the
 // vector (dicb_vec_bytes), R slots of L.bytes, the level records, the group
 // table (groups[0 .. n_groups]: first level of every group, then n_levels)
 // and the slice-offset table (dicb_table_bytes; at most TFS_DICB_MAX_LEVELS
@@ -354,7 +377,7 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
     if (st->done) return;
-    if (MODE == 0 && tid == 0) st->t_sweep0 = gtimer();
+    if ((MODE == 0 || MODE == 3) && tid == 0) st->t_sweep0 = gtimer();
     for (int q = tid; q <= (n_rows >> 5); q += TFS_DICB_TPB)
         so[q] = A.width ? q * 32 * A.width : __ldg(A.slice_off + q);
     for (int q = tid; q <= n_groups; q += TFS_DICB_TPB) gs[q] = __ldg(groups + q);
@@ -374,21 +397,20 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     __syncthreads();
     const bool row = tid < TFS_DICB_ROWS;
     if (MODE == 2) {
-        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, 0, y);
+        dicb_sweep<T, 2, 1>(s, ring, L, R, A, val, d, b, nullptr, lr, gs, so, n_groups, 0, y);
         if (row)
             for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) d[i] = s[i];
+    } else if (MODE == 0) {
+        // z holds the backward start values between the sweeps
+        dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, z, lr, gs, so, n_groups, 0, y);
+        dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, z, nullptr, lr, gs, so, n_groups, n_groups, y);
+        if (row)
+            for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) z[i] = s[i];
     } else {
-        dicb_sweep<T, 0, 1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, 0, y);
-        if (row) {
-            // Every row's backward start value y_i / (D_i + TINY)
-            // (Prec_Solve.f90:55-57), while the copy lane stages the
-            // backward sweep's first groups.
-#pragma unroll 4
-            for (int i = tid; i < n_rows; i += TFS_DICB_ROWS)
-                if (__ldg(A.rowinfo + i) & 0xffffu) s[i] = s[i] / (__ldg(d + i) + (T)TINY);
-            dicb_row_sync();
-        }
-        dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, b, lr, gs, so, n_groups, n_groups, y);
+        if (MODE == 3)
+            dicb_sweep<T, 0, 1, false>(s, ring, L, R, A, val, d, b, nullptr, lr, gs, so, n_groups, 0, y);
+        else
+            dicb_sweep<T, 1, -1>(s, ring, L, R, A, val, d, z, nullptr, lr, gs, so, n_groups, 0, y);
         if (row)
             for (int i = tid; i < n_rows; i += TFS_DICB_ROWS) z[i] = s[i];
     }
@@ -398,6 +420,19 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
         st->done = 1;
         st->niter_out = st->iter + 1;
     }
+}
+
+// The scaling between the sweeps of a split application (MODE 3 and 4 of
+// k_dic_block): z_i = y_i / (D_i + TINY) for every row with entries
+// (Prec_Solve.f90:55-57).
+template <typename T>
+__global__ void k_dic_scale(const uint32_t *__restrict__ rowinfo, const T *__restrict__ d, T *z, int n_rows,
+                            const DevState *st)
+{
+    cudaGridDependencySynchronize();   // z is the forward sweep's
+    if (st->done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x)
+        if (__ldg(rowinfo + i) & 0xffffu) z[i] = z[i] / (__ldg(d + i) + (T)TINY);
 }
 
 }  // namespace tfs

@@ -102,6 +102,24 @@ static cudaError_t launch_ex(bool pdl, void (*kernel)(KArgs...), int grid, int b
     return cudaLaunchKernelEx(&cfg, kernel, ((KArgs)args)...);
 }
 
+// launch_ex with dynamic shared memory.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_ex_smem(bool pdl, void (*kernel)(KArgs...), int grid, int block, int smem,
+                                  cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, ((KArgs)args)...);
+}
+
 // One kernel per large level (PDL-chained), then the tail levels in one
 // block; MODE 1 runs the tail first and the levels in descending order.
 template <typename T, int NR, int MODE>
@@ -627,6 +645,8 @@ static int build_layout(tfs_handle *h, int kind)
             std::call_once(attr_once, [optin] {
                 cudaFuncSetAttribute(k_dic_block<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
                 cudaFuncSetAttribute(k_dic_block<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
                 cudaFuncSetAttribute(k_dic_block<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
             });
         }
@@ -856,11 +876,25 @@ static cudaError_t launch_dic_one_block(tfs_handle *h, cudaStream_t s, int bytes
 {
     const tfs_handle::DicbPlan &P = sizeof(T) == 8 ? h->dicb64 : h->dicb32;
     const SellDev A = sell_of(h);
-    const uintptr_t chk = (uintptr_t)val | (uintptr_t)d | (uintptr_t)b1 | (uintptr_t)A.rowinfo | (uintptr_t)A.col;
+    const uintptr_t chk = (uintptr_t)val | (uintptr_t)d | (uintptr_t)b1 | (uintptr_t)z1 | (uintptr_t)A.rowinfo |
+                          (uintptr_t)A.col;
     if (chk & 15u) return cudaErrorMisalignedAddress;
-    k_dic_block<T, MODE><<<1, TFS_DICB_TPB, bytes, s>>>(A, val, d, b1, z1, h->d_lvl_begin, h->n_levels,
-                                                        h->d_lvl_begin + P.group_off, P.n_groups,
-                                                        dicb_slot<T>(P.rm, P.ents), TFS_DICB_SLOTS, h->st);
+    const DicbSlot L = dicb_slot<T>(P.rm, P.ents);
+    const int *groups = h->d_lvl_begin + P.group_off;
+    if constexpr (MODE == 0 && sizeof(T) == 8 && TFS_DICB_SPLIT64) {
+        // binary64: forward sweep, the scaling on every SM, backward sweep
+        const bool pdl = h->use_pdl != 0;
+        const int rows = h->lvl_begin[h->n_levels];
+        launch_ex_smem(false, k_dic_block<T, 3>, 1, TFS_DICB_TPB, bytes, s, A, val, d, b1, z1,
+                       (const int *)h->d_lvl_begin, h->n_levels, groups, P.n_groups, L, TFS_DICB_SLOTS, h->st);
+        launch_ex(pdl, k_dic_scale<T>, std::min(h->grid, (rows + 255) / 256), 256, s, (const uint32_t *)A.rowinfo,
+                  (const T *)d, z1, rows, (const DevState *)h->st);
+        launch_ex_smem(pdl, k_dic_block<T, 4>, 1, TFS_DICB_TPB, bytes, s, A, val, d, b1, z1,
+                       (const int *)h->d_lvl_begin, h->n_levels, groups, P.n_groups, L, TFS_DICB_SLOTS, h->st);
+        return cudaPeekAtLastError();
+    }
+    k_dic_block<T, MODE><<<1, TFS_DICB_TPB, bytes, s>>>(A, val, d, b1, z1, h->d_lvl_begin, h->n_levels, groups,
+                                                        P.n_groups, L, TFS_DICB_SLOTS, h->st);
     return cudaPeekAtLastError();
 }
 
@@ -942,7 +976,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
             cudaError_t e = launch_dic_one_block<T, 0>(h, s, bytes, val, d, b1, z1);
             if (e == cudaSuccess) {
                 h->dicb_used = 1;
-                (*count)++;
+                *count += (sizeof(T) == 8 && TFS_DICB_SPLIT64) ? 3 : 1;
                 return TFS_OK;
             }
             if (e != cudaErrorMisalignedAddress) return tfs_engine_error(cudaGetLastError(), "one-block DIC launch");
