@@ -33,15 +33,16 @@
 // barrier and releasing the slot the row threads about 400); levels grouped
 // into two slots 113 / 228 us (3 or 4 slots: 116 / 239, 119 / 242), of
 // which the scaling pass between the sweeps (global loads of the geometry
-// and D, one division per row) took 24 / 48 us.  The scaling now runs in
-// the forward sweep, right after each row's value, for binary32 (the
-// backward sweep stages the start values from z like the right-hand side):
-// 106 us; for binary64 a division per row inside the sweep holds each level
-// back on the narrow binary64 pipe (245 us), so the binary64 application is
-// split into a forward kernel, a scaling grid over every SM and a backward
-// kernel: 186 us.  Loading each row thread's next-level operands from the
-// slot during the current level measured slower (129 / 252 us; 146 / 248
-// with the gathers kept ahead of those loads).
+// and D, one division per row) took 24 / 48 us.  With the scaling in the
+// forward sweep, right after each row's value (the backward sweep staging
+// the start values from z like the right-hand side): 106 / 245 us (a
+// division per row inside the sweep holds each level back on the narrow
+// binary64 pipe).  Split into a forward kernel, a scaling grid over every
+// SM and a backward kernel (MODE 3, k_dic_scale, MODE 4): 98 / 186 us, the
+// default for binary64 and for deep binary32 schedules (dicb_split).
+// Loading each row thread's next-level operands from the slot during the
+// current level measured slower (129 / 252 us; 146 / 248 with the gathers
+// kept ahead of those loads).
 //
 // Every row does exactly sweep_row's arithmetic (the reference's order of
 // terms: Prec_Solve.f90:46-67, Prec_Form.f90:32-40), so the results are
@@ -64,9 +65,6 @@ namespace tfs {
 
 #define TFS_DICB_ROWS 256                    // threads sweeping rows
 #define TFS_DICB_TPB (TFS_DICB_ROWS + 32)    // + one copy warp (its lane 0 issues the copies)
-#ifndef TFS_DICB_SPLIT64
-#define TFS_DICB_SPLIT64 1                   // binary64 application as forward kernel, scaling grid, backward kernel
-#endif
 #ifndef TFS_DICB_SLOTS
 #define TFS_DICB_SLOTS 2                     // ring slots (each holds one group of levels)
 #endif
@@ -75,6 +73,19 @@ namespace tfs {
 #ifndef TFS_DICB_WAIT_NS
 #define TFS_DICB_WAIT_NS 500000000ull        // 0.5 s
 #endif
+
+// Whether an application in arithmetic T over n_levels levels runs as three
+// kernels (forward sweep, scaling grid, backward sweep) instead of one:
+// always in binary64; in binary32 for deep schedules (measured per DIC-CG
+// solve, split against one kernel: plain_50 8.66 / 9.31 ms, a 23x19x17
+// lexicographic system 3.75 / 3.88 ms, chan 0.974 / 0.990 ms; a randomly
+// numbered 16^3 system, 15 levels, 2.60 / 2.46 ms).
+#define TFS_DICB_SPLIT32_LEVELS 24
+template <typename T>
+__host__ __device__ inline bool dicb_split(int n_levels)
+{
+    return sizeof(T) == 8 || n_levels >= TFS_DICB_SPLIT32_LEVELS;
+}
 
 // Byte offsets inside one ring slot of `rm` rows and `ents` SELL entries
 // (rm and ents multiples of 32, so every part starts on a 128-byte

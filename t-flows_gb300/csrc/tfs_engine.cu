@@ -648,6 +648,8 @@ static int build_layout(tfs_handle *h, int kind)
                 cudaFuncSetAttribute(k_dic_block<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
                 cudaFuncSetAttribute(k_dic_block<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
                 cudaFuncSetAttribute(k_dic_block<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                cudaFuncSetAttribute(k_dic_block<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
             });
         }
         if ((rc = dalloc(h, &h->d_lvl_begin, h->lvl_tab.size()))) return rc;
@@ -881,8 +883,8 @@ static cudaError_t launch_dic_one_block(tfs_handle *h, cudaStream_t s, int bytes
     if (chk & 15u) return cudaErrorMisalignedAddress;
     const DicbSlot L = dicb_slot<T>(P.rm, P.ents);
     const int *groups = h->d_lvl_begin + P.group_off;
-    if constexpr (MODE == 0 && sizeof(T) == 8 && TFS_DICB_SPLIT64) {
-        // binary64: forward sweep, the scaling on every SM, backward sweep
+    if (MODE == 0 && dicb_split<T>(h->n_levels)) {
+        // forward sweep, the scaling on every SM, backward sweep
         const bool pdl = h->use_pdl != 0;
         const int rows = h->lvl_begin[h->n_levels];
         launch_ex_smem(false, k_dic_block<T, 3>, 1, TFS_DICB_TPB, bytes, s, A, val, d, b1, z1,
@@ -976,7 +978,7 @@ static int launch_sweeps(tfs_handle *h, cudaStream_t s, int nr, const T *b1, con
             cudaError_t e = launch_dic_one_block<T, 0>(h, s, bytes, val, d, b1, z1);
             if (e == cudaSuccess) {
                 h->dicb_used = 1;
-                *count += (sizeof(T) == 8 && TFS_DICB_SPLIT64) ? 3 : 1;
+                *count += dicb_split<T>(h->n_levels) ? 3 : 1;
                 return TFS_OK;
             }
             if (e != cudaErrorMisalignedAddress) return tfs_engine_error(cudaGetLastError(), "one-block DIC launch");
@@ -1108,13 +1110,16 @@ static int tfs_mixed_body(tfs_handle *h, cudaStream_t s, int method, int prec,
             launch_ex(pv, k_mx_true<0, false>, G, T, s, A, (const double *)h->val, V, F, h->st, h->part, prec, cond, l0);
             *count += 5;
         } else if (prec == 2) {
+            // (the one-block DIC, or levels that cannot take level 0 into the
+            // CG kernels) the vector kernels PDL-chained
+            const bool pv = h->use_pdl && h->pdl_vec;
             if ((rc = launch_sweeps<float>(h, s, 1, F.r, nullptr, F.y, nullptr, F.z, nullptr, count))) return rc;
-            k_mx_dot_rho4<<<G4, T, 0, s>>>(n4, F, h->st, h->part);
-            k_mx_cg_p4<<<G4, T, 0, s>>>(n4, F, h->st);
-            launch_spmv_pq(h, s, true);
-            k_mx_cg_update4<false><<<G4, T, 0, s>>>(n4, F, h->st, h->part);
-            k_mx_fold4<<<G4, T, 0, s>>>(n4, V, F, h->st);
-            k_mx_true<0, false><<<G, T, 0, s>>>(A, h->val, V, F, h->st, h->part, prec, cond);
+            launch_ex(pv, k_mx_dot_rho4, G4, T, s, n4, F, h->st, h->part);
+            launch_ex(pv, k_mx_cg_p4, G4, T, s, n4, F, (const DevState *)h->st);
+            launch_spmv_pq(h, s, true, pv);
+            launch_ex(pv, k_mx_cg_update4<false>, G4, T, s, n4, F, h->st, h->part, 0);
+            launch_ex(pv, k_mx_fold4, G4, T, s, n4, V, F, (const DevState *)h->st);
+            launch_ex(pv, k_mx_true<0, false>, G, T, s, A, (const double *)h->val, V, F, h->st, h->part, prec, cond, 0);
             *count += 6;
         } else {
             // Diagonal (or no) preconditioner: the whole body PDL-chained.

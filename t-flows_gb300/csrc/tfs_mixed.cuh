@@ -271,6 +271,10 @@ __global__ void __launch_bounds__(TFS_TPB) k_mx_cg_p4(int n4, Vec32 F, const Dev
 
 __global__ void __launch_bounds__(TFS_TPB) k_mx_dot_rho4(int n4, Vec32 F, DevState *st, double *part)
 {
+    // PDL secondary (a no-op when launched plainly): wait for the
+    // predecessor before reading anything, then let the successor launch.
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
     const bool stop = (st->done | st->need_true) != 0;
     const float4 *r4 = (const float4 *)F.r, *z4 = (const float4 *)F.z;
     float acc = 0.f;
