@@ -155,12 +155,16 @@ int tfs_set_default_precision(int mode);
                                     their dependency wait (default); 0          */
 #define TFS_OPT_BWD_PRE      13  /* 1 backward level kernels compute their start
                                     values before the wait (default); 0         */
-#define TFS_OPT_DIC_BLOCK    14  /* 1 the whole DIC application (and Prec_Form)
-                                    in one thread block, the vector in shared
-                                    memory and each level's rows staged there
-                                    ahead, where the vector and at least three
-                                    level slots fit (deep schedules of narrow
+#define TFS_OPT_DIC_BLOCK    14  /* 1 each DIC sweep (and Prec_Form) in one
+                                    thread block, the vector in shared memory
+                                    and groups of levels staged there ahead,
+                                    where the vector and two slots of the
+                                    widest level fit (deep schedules of narrow
                                     levels; default); 0 the level kernels       */
+#define TFS_OPT_L2_WINDOW    15  /* 1 the column indices in an L2 persisting
+                                    access window of the solve kernels (a
+                                    limit of the calling process's context;
+                                    default); 0 none                           */
 
 /* One DIC application (the tfs_time_prec workload: factor from val, r = 1)
  * with its level launches stamped on the device: for slot k (launch order)

@@ -133,6 +133,7 @@ struct tfs_handle {
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
     int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC where the vector and two slots of the widest level fit
+    int l2_window = 1;                 // TFS_OPT_L2_WINDOW: 1 the column indices persisting in L2
     int dicb_used = 0;                 // the last DIC application launched was the one-block kernel
     // One-block DIC per arithmetic: shared memory (0: does not fit), ring
     // slot capacity (rows and SELL entries), number of level groups and the

@@ -146,6 +146,9 @@ static bool try_start(tfs_server *S, Request *r)
         // could use the slots (measured 232 against 252 solves/s on the
         // serving trace), so the server's handles launch them plainly.
         sy.h->pdl_vec = 0;
+        // Nor do they mark their column indices persisting in L2: the
+        // resident systems would compete for the one set-aside.
+        sy.h->l2_window = 0;
         sy.bytes = need;
         S->resident += need;
         S->stats.registrations++;

@@ -18,7 +18,7 @@ TFS_SYNTH_POISSON, TFS_SYNTH_CONVDIFF = 0, 1
 # options of a handle (tfs_set_option)
 (TFS_OPT_LAUNCH, TFS_OPT_LAYOUT, TFS_OPT_BICG, TFS_OPT_SELL_UNIFORM, TFS_OPT_SPMV, TFS_OPT_SPMV_GRID,
  TFS_OPT_LEVEL_TPB, TFS_OPT_TAIL_PF, TFS_OPT_FUSE_L0, TFS_OPT_PDL, TFS_OPT_PDL_VEC, TFS_OPT_FWD_PRE,
- TFS_OPT_BWD_PRE, TFS_OPT_DIC_BLOCK) = range(1, 15)
+ TFS_OPT_BWD_PRE, TFS_OPT_DIC_BLOCK, TFS_OPT_L2_WINDOW) = range(1, 16)
 
 _PKG = Path(__file__).resolve().parent
 # TFS_LIBRARY selects another build of the library (same ABI).

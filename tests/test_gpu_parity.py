@@ -627,3 +627,27 @@ def test_one_block_dic_not_used_on_wide_levels(gpu):
         z = sol.prec_solve(s.val, 2, b)
         assert sol.stats()["dic_kernel"] == 0
     assert np.array_equal(z, O.prec_solve(s.n, s.row, s.col, s.dia, s.val, 2, b))
+
+
+@pytest.mark.parametrize("launch", [0, 1])
+def test_l2_window_changes_no_result(launch, gpu):
+    """The column indices marked persisting in L2 (TFS_OPT_L2_WINDOW = 1,
+    the default) change where the cache keeps them, not what any kernel
+    computes: DIC-CG and diagonal CGS solves in both arithmetics, in the
+    CUDA graph and launched eagerly, bitwise equal to TFS_OPT_L2_WINDOW = 0."""
+    from tflows.lib import TFS_OPT_L2_WINDOW, TFS_OPT_LAUNCH
+    s = system(POISSON, 24, 24, 24)
+    tol = 1e-8 * float(np.linalg.norm(s.b))
+    out = {}
+    for win in (1, 0):
+        res = []
+        for mode in (TFS_FP64, TFS_MIXED):
+            with Solver(s.matrix(), precision=mode, options={TFS_OPT_L2_WINDOW: win, TFS_OPT_LAUNCH: launch}) as sol:
+                for method, prec in ((TFS_CG, 2), (TFS_CGS, 1)):
+                    x, r = np.zeros(s.n), s.b.copy()
+                    st = sol.solve(method, s.val, x, r, prec, 2000, tol)
+                    assert st.status == 0
+                    res += [x, r, st.niter]
+        out[win] = res
+    for a, c in zip(out[1], out[0]):
+        assert np.array_equal(a, c)
