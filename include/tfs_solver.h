@@ -183,6 +183,15 @@ int tfs_profile_prec(tfs_handle *h, const double *val, int mode, int max_slots, 
 int tfs_set_option(tfs_handle *h, int option, int value);
 int tfs_get_option(const tfs_handle *h, int option, int *value);
 
+/* Diagnostics of the one-block DIC's bounded waits: with wait_ns > 0 (at
+ * most 1e9), the solves of this handle that follow run the one-block DIC
+ * with its copy lane staging nothing and every wait limited to wait_ns, so
+ * its first wait runs out: the kernel raises its abort flag, no thread
+ * waits or reads a slot again, and the solve returns TFS_ERR_TIMEOUT with
+ * the GPU unaffected.  wait_ns = 0 restores the normal limit (0.5 s).
+ * Replaces nothing in the reference. */
+int tfs_diag_dic_timeout(tfs_handle *h, long long wait_ns);
+
 /* ---- solves ------------------------------------------------------------- */
 
 /* One preconditioned Krylov solve with host arrays (val, x, r1 host memory).

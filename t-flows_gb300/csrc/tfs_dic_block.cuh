@@ -171,10 +171,11 @@ __device__ __forceinline__ bool dicb_mbar_test(uint64_t *bar, unsigned parity)
     return ok != 0;
 }
 
-// Wait for the phase of the given parity to complete, at most
-// TFS_DICB_WAIT_NS; false (and the abort flag raised) when it did not, or
-// at once when the flag is already up.
-__device__ __forceinline__ bool dicb_mbar_wait(uint64_t *bar, unsigned parity, volatile int *abort)
+// Wait for the phase of the given parity to complete, at most wait_ns;
+// false (and the abort flag raised) when it did not, or at once when the
+// flag is already up.
+__device__ __forceinline__ bool dicb_mbar_wait(uint64_t *bar, unsigned parity, volatile int *abort,
+                                               unsigned long long wait_ns)
 {
     if (dicb_mbar_test(bar, parity)) return true;
     if (*abort) return false;
@@ -183,7 +184,7 @@ __device__ __forceinline__ bool dicb_mbar_wait(uint64_t *bar, unsigned parity, v
         if (dicb_mbar_test(bar, parity)) return true;
         if ((k & 255u) == 0u) {
             if (*abort) return false;
-            if (gtimer() - t0 > TFS_DICB_WAIT_NS) {
+            if (gtimer() - t0 > wait_ns) {
                 *abort = 1;
                 return false;
             }
@@ -196,10 +197,14 @@ __device__ __forceinline__ void dicb_row_sync()
     asm volatile("bar.sync %0, %1;" : : "n"(TFS_DICB_ROW_BAR), "n"(TFS_DICB_ROWS) : "memory");
 }
 
-// The ring's per-slot barriers and the block's abort flag.
+// The ring's per-slot barriers, the block's abort flag and the wait limit
+// (TFS_DICB_WAIT_NS, or the diagnostic limit under which the copy lane
+// stages nothing: tfs_diag_dic_timeout).
 struct DicbSync {
     uint64_t *full, *empty;   // R each
     volatile int *abort;
+    unsigned long long wait_ns;
+    bool starve;
 };
 
 // Row i's new value from its staged entries j0 <= j < j1 (at e0 + 32 j of
@@ -262,19 +267,19 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
     int slot = g0 % R;
     unsigned ph = (unsigned)((g0 / R) & 1);   // phase parity of the slot's current use
     if (tid >= TFS_DICB_ROWS) {
-        if (tid != TFS_DICB_ROWS) return;
+        if (tid != TFS_DICB_ROWS || y.starve) return;
         // the copy lane
         int issued = 0;
         // the backward sweep stages the start values the forward sweep wrote:
         // its first group is the forward sweep's last, so wait for the
         // forward sweep's last release (use g0 - 1 of the ring)
-        if (PART == 1 && g0 > 0 && !dicb_mbar_wait(y.empty + (g0 - 1) % R, (unsigned)(((g0 - 1) / R) & 1), y.abort))
+        if (PART == 1 && g0 > 0 && !dicb_mbar_wait(y.empty + (g0 - 1) % R, (unsigned)(((g0 - 1) / R) & 1), y.abort, y.wait_ns))
             return;
         for (int q = 0; q < n_groups; q++) {
             const int g = DIR > 0 ? q : n_groups - 1 - q;
             // the slot's previous group must be done by the row threads;
             // after an abort no more copies
-            if ((g0 + q >= R && !dicb_mbar_wait(y.empty + slot, ph ^ 1u, y.abort)) || *y.abort) break;
+            if ((g0 + q >= R && !dicb_mbar_wait(y.empty + slot, ph ^ 1u, y.abort, y.wait_ns)) || *y.abort) break;
             const int4 first = lr[gs[g]], last = lr[gs[g + 1] - 1];
             const int r0 = first.x, nr = last.x + last.y - first.x;
             const int e0 = first.z, ne = last.z + last.w - first.z;
@@ -307,7 +312,7 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
             for (int k = 0; k < R && k < issued; k++) {
                 if (--slot < 0) { slot = R - 1; ph ^= 1u; }
                 const unsigned long long t0 = gtimer();
-                while (!dicb_mbar_test(y.full + slot, ph) && gtimer() - t0 < TFS_DICB_WAIT_NS) {
+                while (!dicb_mbar_test(y.full + slot, ph) && gtimer() - t0 < y.wait_ns) {
                 }
             }
         }
@@ -317,7 +322,7 @@ __device__ __forceinline__ void dicb_sweep(T *s, unsigned char *ring, const Dicb
         const int g = DIR > 0 ? q : n_groups - 1 - q;
         const int la = gs[g], lb = gs[g + 1];
         // after an abort the slot may hold another group's rows: no row reads it
-        const bool ok = dicb_mbar_wait(y.full + slot, ph, y.abort);
+        const bool ok = dicb_mbar_wait(y.full + slot, ph, y.abort, y.wait_ns);
         const int4 first = lr[la];
         const int rg = first.x, sg = first.z;   // the group's first row and entry
         const unsigned char *sl = ring + (size_t)slot * L.bytes;
@@ -384,10 +389,12 @@ k_dic_block(SellDev A, const T *__restrict__ val, T *d, const T *b, T *z, const 
     int *so = gs + n_groups + 1;
     uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(lr) +
                                                   dicb_table_bytes(n_levels, n_groups, n_rows));
-    DicbSync y{bars, bars + R, reinterpret_cast<volatile int *>(bars + 2 * R)};
     const int tid = threadIdx.x;
     cudaGridDependencySynchronize();   // PDL secondary: a no-op when launched plainly
     if (st->done) return;
+    const unsigned long long diag_ns = st->dicb_wait_ns;
+    DicbSync y{bars, bars + R, reinterpret_cast<volatile int *>(bars + 2 * R),
+               diag_ns ? diag_ns : TFS_DICB_WAIT_NS, diag_ns != 0};
     if ((MODE == 0 || MODE == 3) && tid == 0) st->t_sweep0 = gtimer();
     for (int q = tid; q <= (n_rows >> 5); q += TFS_DICB_TPB)
         so[q] = A.width ? q * 32 * A.width : __ldg(A.slice_off + q);

@@ -842,6 +842,13 @@ extern "C" int tfs_set_option(tfs_handle *h, int option, int value)
     return TFS_OK;
 }
 
+extern "C" int tfs_diag_dic_timeout(tfs_handle *h, long long wait_ns)
+{
+    if (!h || wait_ns < 0 || wait_ns > 1000000000LL) return TFS_ERR_ARG;
+    h->dicb_diag_ns = (unsigned long long)wait_ns;
+    return TFS_OK;
+}
+
 extern "C" int tfs_get_option(const tfs_handle *h, int option, int *value)
 {
     if (!h || !value) return TFS_ERR_ARG;
@@ -1461,6 +1468,7 @@ int tfs_solve_launch(int method, tfs_handle *h, const double *val, double *x, do
     P.b = device_ptrs ? (b_in ? b_in : r1) : h->stage_b;
     P.x = device_ptrs ? x : h->stage_x;
     P.r_out = device_ptrs ? r1 : h->stage_b;
+    P.dicb_wait_ns = h->dicb_diag_ns;
     CK(cudaMemcpyAsync(h->params, h->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s));
     if (!device_ptrs) {
         CK(cudaMemcpyAsync(h->stage_val, val, sizeof(double) * (size_t)h->nnz, cudaMemcpyHostToDevice, s));
@@ -1616,6 +1624,7 @@ static int prepare_values(tfs_handle *h, const double *val, int prec = 0)
     P.b = h->stage_b;
     P.x = h->stage_x;
     P.r_out = h->stage_b;
+    P.dicb_wait_ns = 0;
     CK(cudaMemcpyAsync(h->params, h->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->stage_val, val, sizeof(double) * (size_t)h->nnz, cudaMemcpyHostToDevice, s));
     int gv = (h->nnz_pad + 255) / 256;

@@ -64,6 +64,10 @@ struct DevState {
     unsigned long long *stamps;
     int stamp_stride;      // entries per slot (2 per block)
     int pad3;
+    // tfs_diag_dic_timeout: > 0, the one-block DIC's waits give up after
+    // this many ns and its copy lane stages nothing (its first wait runs
+    // out); 0, the normal limit
+    unsigned long long dicb_wait_ns;
 };
 
 // Per-call arguments, written by the host before every graph launch.
@@ -75,6 +79,7 @@ struct DevParams {
     const double *b;         // natural order, n (r1 on entry)
     double *x;               // natural order, n (in/out)
     double *r_out;           // natural order, n (r1 on return)
+    unsigned long long dicb_wait_ns;   // DevState::dicb_wait_ns of the call
 };
 
 struct SellDev {
@@ -133,6 +138,7 @@ struct tfs_handle {
     int eager = 0;                     // TFS_OPT_LAUNCH: 1 launch kernels from a host loop, no CUDA graph
     int bicg_literal = 0;              // TFS_OPT_BICG: 1 BiCG runs its shadow sequence explicitly
     int dic_block = 1;                 // TFS_OPT_DIC_BLOCK: 1 one-block DIC where the vector and two slots of the widest level fit
+    unsigned long long dicb_diag_ns = 0;   // tfs_diag_dic_timeout
     int l2_window = 1;                 // TFS_OPT_L2_WINDOW: 1 the column indices persisting in L2
     int dicb_used = 0;                 // the last DIC application launched was the one-block kernel
     // One-block DIC per arithmetic: shared memory (0: does not fit), ring

@@ -351,6 +351,7 @@ __global__ void k_init(DevState *st, const DevParams *prm, int prec)
     s.loop_limit = (prm->niter_max > 0 ? prm->niter_max : 0) + 8;
     s.delta = 0.1;
     s.t_begin = gtimer();
+    s.dicb_wait_ns = prm->dicb_wait_ns;
     *st = s;
 }
 

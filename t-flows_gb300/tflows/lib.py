@@ -69,6 +69,7 @@ SIGNATURES = {
     "tfs_set_default_precision": (C.c_int, [C.c_int]),
     "tfs_set_option": (C.c_int, [P_void, C.c_int, C.c_int]),
     "tfs_get_option": (C.c_int, [P_void, C.c_int, C.POINTER(C.c_int)]),
+    "tfs_diag_dic_timeout": (C.c_int, [P_void, C.c_longlong]),
     "tfs_solve": (C.c_int, [C.c_int, P_void, i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl,
                             i32, P_i32, dbl, P_dbl, P_dbl]),
     "tfs_cg": (C.c_int, [i32, i32, P_i32, P_i32, P_i32, P_dbl, P_dbl, P_dbl, i32, P_i32, dbl, P_dbl, P_dbl]),

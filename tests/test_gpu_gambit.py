@@ -147,3 +147,32 @@ def test_one_block_dic_on_reference_mesh(name, gpu):
         out[blk] = res
     for a, c in zip(out[1], out[0]):
         assert np.array_equal(a, c)
+
+
+def test_one_block_dic_wait_runs_out(gpu):
+    """The one-block DIC's bounded waits: with its copy lane staging nothing
+    and a 2 ms limit (tfs_diag_dic_timeout), its first wait runs out and the
+    solve returns TFS_ERR_TIMEOUT promptly; with the normal limit restored
+    the same handle solves as before, bit for bit (the GPU still answers and
+    nothing of the aborted launch lingers)."""
+    import time
+    from tflows.lib import TFS_ERR_TIMEOUT, TfsError, load_library
+    lib = load_library()
+    s = load("plain50")
+    ref = oracle(s, TFS_CG, 2)
+    with Solver(s.matrix()) as sol:
+        x, r = np.zeros(s.n), s.b.copy()
+        good = sol.solve(TFS_CG, s.val, x, r, 2, 5000, ref["tol"])
+        assert good.status == 0 and sol.stats()["dic_kernel"] == 1
+        assert lib.tfs_diag_dic_timeout(sol.h, 2_000_000) == 0
+        t = time.perf_counter()
+        with pytest.raises(TfsError) as e:
+            sol.solve(TFS_CG, s.val, np.zeros(s.n), s.b.copy(), 2, 5000, ref["tol"])
+        assert e.value.status == TFS_ERR_TIMEOUT
+        assert time.perf_counter() - t < 5.0
+        assert lib.tfs_diag_dic_timeout(sol.h, 0) == 0
+        x2, r2 = np.zeros(s.n), s.b.copy()
+        again = sol.solve(TFS_CG, s.val, x2, r2, 2, 5000, ref["tol"])
+        assert again.status == 0 and again.niter == good.niter
+        assert np.array_equal(x2, x) and np.array_equal(r2, r)
+        assert lib.tfs_diag_dic_timeout(sol.h, -1) != 0
