@@ -642,6 +642,7 @@ __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__r
 // only once it has passed its own wait, so the forward sweep is complete
 // when this kernel starts): the row's start value y_i / (D_i + TINY) is
 // computed before the wait, taking the division off the dependent chain.
+#define TFS_FWD_PRE_SLOTS 6   // forward level kernels: slots loaded before the dependency wait
 template <typename T, int NR, int MODE, int BS = TFS_TPB, bool PREY = false>
 __global__ void __launch_bounds__(BS)
 k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
@@ -652,17 +653,22 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     const int i = row0 + blockIdx.x * BS + threadIdx.x;
     const bool active = i < row1;
     RowGeom g{0, 0, 0};
-    int kk[4] = {0, 0, 0, 0};
-    T aa[4] = {(T)0, (T)0, (T)0, (T)0};
+    int kk[TFS_FWD_PRE_SLOTS] = {};
+    T aa[TFS_FWD_PRE_SLOTS] = {};
     if (active) {
         if (MODE == 0 && A.width > 0) {
-            // Uniform slice width: the first four slots are where they are
+            // Uniform slice width: the first slots are where they are
             // whatever the row's geometry says, so their loads do not wait
             // for it (slots past the row's length hold column 0, value 0).
+            // Six slots hold every lower entry of a 7-entry row: measured on
+            // the 128^3 system 4 / 6 / 8 slots 126.2 / 116.9 / 119.3 us per
+            // DIC application (14.92 / 15.54 / 15.31 solves/s mixed);
+            // backward levels, whose loads wait for the geometry anyway,
+            // keep four (six: 14.74 mixed).
             const int off = (i & ~31) * A.width + (i & 31);
             g = row_geom(A, i);
 #pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int q = 0; q < TFS_FWD_PRE_SLOTS; q++)
                 if (q < A.width) {
                     kk[q] = __ldg(A.col + off + (q << 5));
                     aa[q] = __ldg(val + off + (q << 5));
@@ -670,8 +676,9 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
         } else {
             g = row_geom(A, i);
             const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
+            // as many as the forward row routine below takes from kk / aa
 #pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int q = 0; q < (MODE == 0 && PREY ? TFS_FWD_PRE_SLOTS : 4); q++)
                 if (j0 + q < j1) {
                     int ee = g.off + ((j0 + q) << 5);
                     kk[q] = __ldg(A.col + ee);
@@ -702,7 +709,7 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     if (MODE == 1 && PREY) {
         if (active) sweep_row_bwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
     } else if (MODE == 0 && PREY) {
-        if (active) sweep_row_fwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
+        if (active) sweep_row_fwd_pre<T, NR, TFS_FWD_PRE_SLOTS>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
     } else if (active) {
         sweep_row<T, NR, MODE, 4>(A, val, d, b1, b2, o1, o2, y1, y2, i, g, kk, aa, skip);
     }
