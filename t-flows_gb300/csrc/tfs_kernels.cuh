@@ -643,8 +643,13 @@ __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__r
 // when this kernel starts): the row's start value y_i / (D_i + TINY) is
 // computed before the wait, taking the division off the dependent chain.
 #define TFS_FWD_PRE_SLOTS 6   // forward level kernels: slots loaded before the dependency wait
+// Level kernels of 256 threads: binary64 held to 40 registers (6 blocks per
+// SM; the backward kernel would take 48, 5 blocks): 7.43 against 7.36
+// binary64 solves/s at 128^3; binary32 to 32 (8 blocks per SM, what the
+// compiler picks unbounded; allowed 40 it took 40 and lost 7%).  Other
+// block sizes (TFS_OPT_LEVEL_TPB) at most 64 registers.
 template <typename T, int NR, int MODE, int BS = TFS_TPB, bool PREY = false>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, BS == 256 ? (sizeof(T) == 8 ? 6 : 8) : (BS >= 1024 ? 1 : 1024 / BS))
 k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *b2, T *o1,
               T *o2, const T *y1, const T *y2, int row0, int row1, DevState *st, int tag)
 {
