@@ -1350,7 +1350,7 @@ def legs(args, dist: Dist, line: dict | None) -> None:
                      f"(--workload {SERVE_WORKLOAD} runs {args.serve_requests} over {args.serve_pool})")
     line["batched"] = b
     line["serving"] = sv
-    line["north_star"] = {
+    line["target_mixed_over_fp64"] = {
         "target": "mixed, batched, served path >= 1.7x the plain binary64 GPU path's solves/s",
         "batched_mixed_over_plain_fp64": b["mixed_batched_over_plain_fp64"],
         "served_mixed_over_fp64": sv["mixed_over_fp64"],
