@@ -178,8 +178,6 @@ def measured_peak_gbs() -> tuple[float, str]:
 SPMV_KERNEL_NAMES = {
     0: ("k_mx_spmv_pq", "direct: per-row dependent loads"),
     1: ("k_spmv_pq_pipe<float,true,W>", "software-pipelined: next row's columns loaded during the gathers"),
-    2: ("k_spmv_pq_bulk<float,true>", "matrix tiles staged in shared memory by cp.async.bulk"),
-    3: ("k_spmv_pq_async<float,true,S>", "matrix tiles staged in shared memory by cp.async"),
 }
 
 

@@ -270,7 +270,7 @@ typedef struct tfs_tuning {
     double  prec_ms[4];       /* DIC application, level_tpb 128/256/512/1024 */
     double  spmv_ms[2];       /* direct SpMV kernel, spmv_chunks 0 / 1       */
     int32_t spmv_kernel;      /* SpMV kernel kept: 0 direct, 1 software-
-                                 pipelined, 2 bulk-copy, 3 cp.async-staged  */
+                                 pipelined                                  */
     int32_t pad;
     double  spmv_pipe_ms[2];  /* software-pipelined SpMV, spmv_chunks 0 / 1
                                  (0: matrix not of uniform slice width)     */
