@@ -848,18 +848,32 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
     const bool skip = st->done != 0;
     unsigned long long *const stp = st->stamps;
     const unsigned long long t0 = stp ? gtimer() : 0ull;
+    // The tail's own rows keep their values in shared memory as well (a
+    // level's gathers of rows of earlier tail levels are shared-memory loads
+    // after the block barrier); the values of rows below the tail, final
+    // since the dependency wait, are all gathered at once right after it.
+    __shared__ T ty[TFS_SWEEP_TPB], tz[TFS_SWEEP_TPB];
+    const int r0 = __ldg(lvl_begin + l_begin);
+    T xv[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        xv[j] = (T)0;
+        if (mine && j < g.dpos && kk[j] < r0) xv[j] = __ldcg(y + kk[j]);
+    }
     T yi = (T)0;
     for (int l = l_begin; l < l_end; l++) {
         if (lev == l) {
             if (g.len == 0) {
                 if (!skip) y[i] = (T)0;
+                ty[threadIdx.x] = (T)0;
             } else {
                 T s = bi;
 #pragma unroll
                 for (int j = 0; j < 8; j++)
-                    if (j < g.dpos) s = s - aa[j] * __ldcg(y + kk[j]);
+                    if (j < g.dpos) s = s - aa[j] * (kk[j] < r0 ? xv[j] : ty[kk[j] - r0]);
                 yi = s * di;
                 if (!skip) y[i] = yi;
+                ty[threadIdx.x] = yi;
             }
         }
         __syncthreads();
@@ -871,12 +885,15 @@ k_sweep_tail1(SellDev A, const T *__restrict__ val, const T *d, const T *b, T *y
         if (lev == l) {
             if (g.len == 0) {
                 if (!skip) z[i] = (T)0;
+                tz[threadIdx.x] = (T)0;
             } else {
                 T s = q0;
 #pragma unroll
                 for (int j = 0; j < 8; j++)
-                    if (j > g.dpos && j < g.len) s = s - aa[j] * __ldcg(z + kk[j]);
-                if (!skip) z[i] = s * di;
+                    if (j > g.dpos && j < g.len) s = s - aa[j] * (kk[j] >= r0 ? tz[kk[j] - r0] : __ldcg(z + kk[j]));
+                const T zi = s * di;
+                if (!skip) z[i] = zi;
+                tz[threadIdx.x] = zi;
             }
         }
         __syncthreads();
