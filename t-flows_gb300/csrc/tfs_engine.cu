@@ -844,7 +844,10 @@ extern "C" int tfs_set_option(tfs_handle *h, int option, int value)
 
 extern "C" int tfs_diag_dic_timeout(tfs_handle *h, long long wait_ns)
 {
-    if (!h || wait_ns < 0 || wait_ns > 1000000000LL) return TFS_ERR_ARG;
+    if (!h || wait_ns < 0 || wait_ns > 1000000000LL) {
+        tfs_set_error_text("tfs_diag_dic_timeout: null handle or wait_ns outside [0, 1e9]");
+        return TFS_ERR_ARG;
+    }
     h->dicb_diag_ns = (unsigned long long)wait_ns;
     return TFS_OK;
 }

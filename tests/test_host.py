@@ -237,3 +237,12 @@ def test_noalloc_rejections_set_error_text(case):
     assert st == TFS_ERR_ARG
     from tflows.lib import last_error
     assert want in last_error()
+
+
+def test_diag_dic_timeout_rejects_without_a_device():
+    """The one-block DIC's timeout diagnostic refuses a null handle and a
+    limit outside [0, 1e9] ns, with its error text, before any CUDA call."""
+    from tflows.lib import last_error
+    lib = load_library()
+    assert lib.tfs_diag_dic_timeout(None, 1000) == TFS_ERR_ARG
+    assert "tfs_diag_dic_timeout" in last_error()
