@@ -22,6 +22,41 @@
 
 namespace tfs {
 
+#ifndef TFS_SPMV_NOALLOC
+#define TFS_SPMV_NOALLOC 1
+#endif
+// Read-once matrix stream (values, column indices, geometry) loaded without
+// allocating in L1, so that L1 holds the gathered p: binary32 SpMV 31.2
+// against 32.8 us on the 128^3 system (binary64 unchanged, 73.8 us).
+__device__ __forceinline__ int ld_stream(const int *a)
+{
+    int v;
+    if (TFS_SPMV_NOALLOC) asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
+    else v = __ldg(a);
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *a)
+{
+    uint32_t v;
+    if (TFS_SPMV_NOALLOC) asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
+    else v = __ldg(a);
+    return v;
+}
+__device__ __forceinline__ float ld_stream(const float *a)
+{
+    float v;
+    if (TFS_SPMV_NOALLOC) asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(a));
+    else v = __ldg(a);
+    return v;
+}
+__device__ __forceinline__ double ld_stream(const double *a)
+{
+    double v;
+    if (TFS_SPMV_NOALLOC) asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(a));
+    else v = __ldg(a);
+    return v;
+}
+
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
@@ -51,9 +86,9 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
     if (c < nch) {
         const int i = c * TFS_TPB + tid;
         const int off = (i & ~31) * W + (i & 31);
-        ninfo = __ldg(A.rowinfo + i);
+        ninfo = ld_stream(A.rowinfo + i);
 #pragma unroll
-        for (int j = 0; j < W; j++) nk[j] = __ldg(A.col + off + 32 * j);
+        for (int j = 0; j < W; j++) nk[j] = ld_stream(A.col + off + 32 * j);
     }
     cudaGridDependencySynchronize();   // PDL secondary of the p update (a no-op when launched plainly)
     cudaTriggerProgrammaticLaunchCompletion();
@@ -72,7 +107,7 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
             x[j] = (VT)0;
             if (j < len) {
                 x[j] = gather<TFS_SPMV_NC>(p + nk[j]);
-                a[j] = __ldg(val + off + 32 * j);
+                a[j] = ld_stream(val + off + 32 * j);
             }
         }
         const VT pi = p[i];
@@ -80,9 +115,9 @@ k_spmv_pq_pipe(SellDev A, const VT *__restrict__ val, const VT *__restrict__ p, 
         if (cn < nch) {
             const int in = cn * TFS_TPB + tid;
             const int offn = (in & ~31) * W + (in & 31);
-            ninfo = __ldg(A.rowinfo + in);
+            ninfo = ld_stream(A.rowinfo + in);
 #pragma unroll
-            for (int j = 0; j < W; j++) nk[j] = __ldg(A.col + offn + 32 * j);
+            for (int j = 0; j < W; j++) nk[j] = ld_stream(A.col + offn + 32 * j);
         }
         VT s = (VT)0;
 #pragma unroll
