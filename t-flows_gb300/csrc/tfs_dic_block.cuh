@@ -60,6 +60,7 @@
 // solve ends with TFS_ERR_TIMEOUT.
 #pragma once
 #include "tfs_kernels.cuh"
+#include "tfs_dicb_plan.h"
 
 namespace tfs {
 
@@ -85,51 +86,6 @@ template <typename T>
 __host__ __device__ inline bool dicb_split(int n_levels)
 {
     return sizeof(T) == 8 || n_levels >= TFS_DICB_SPLIT32_LEVELS;
-}
-
-// Byte offsets inside one ring slot of `rm` rows and `ents` SELL entries
-// (rm and ents multiples of 32, so every part starts on a 128-byte
-// boundary): geometry, diagonal, right-hand side, column indices and values
-// of one group of levels.
-struct DicbSlot {
-    int rm, ents, off_d, off_b, off_col, off_val, bytes;
-};
-
-template <typename T>
-__host__ __device__ inline DicbSlot dicb_slot(int rm, int ents)
-{
-    DicbSlot s;
-    s.rm = rm;
-    s.ents = ents;
-    s.off_d = rm * 4;
-    s.off_b = s.off_d + rm * (int)sizeof(T);
-    s.off_col = s.off_b + rm * (int)sizeof(T);
-    s.off_val = s.off_col + ents * 4;
-    s.bytes = s.off_val + ents * (int)sizeof(T);
-    return s;
-}
-
-// Shared memory of the vector (n_rows values of T), rounded to 128 bytes.
-template <typename T>
-__host__ __device__ inline int dicb_vec_bytes(int n_rows)
-{
-    return (n_rows * (int)sizeof(T) + 127) & ~127;
-}
-
-// Shared memory of the level records (one int4 per level: first row, rows,
-// first SELL entry, entries), the group table (first level of every group,
-// n_groups + 1 ints) and the slice-offset table (n_rows / 32 + 1 ints),
-// rounded to 16 bytes.
-__host__ __device__ inline int dicb_table_bytes(int n_levels, int n_groups, int n_rows)
-{
-    return n_levels * 16 + (((n_groups + 1) + (n_rows >> 5) + 1) * 4 + 15) / 16 * 16;
-}
-
-// Shared memory of the ring's R full and R empty mbarriers and the abort
-// flag.
-__host__ __device__ inline int dicb_sync_bytes(int R)
-{
-    return 2 * R * 8 + 16;
 }
 
 __device__ __forceinline__ uint32_t dicb_smem_addr(const void *p)

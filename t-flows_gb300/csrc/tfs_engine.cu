@@ -592,65 +592,31 @@ static int build_layout(tfs_handle *h, int kind)
         }
         h->pf_tail_level = l;
         h->pf_ok = l < nl && l <= h->tail_level;
-        // One-block DIC: the swept vector (every row of the levels), a ring
-        // of TFS_DICB_SLOTS slots, each holding one group of consecutive
-        // levels, and the level, group and slice-offset tables in the block's
-        // shared memory.  The slots share what the vector and the tables
-        // leave, rows and entries in the widest level's proportion; a slot
-        // must hold the widest level.  Groups are filled greedily.
+        // One-block DIC: the plan per arithmetic (tfs_dicb_plan.h); the
+        // group tables follow the level table in d_lvl_begin's allocation.
         h->dicb64 = h->dicb32 = tfs_handle::DicbPlan{};
         h->lvl_tab.assign(h->lvl_begin.begin(), h->lvl_begin.end());
-        if (kind == TFS_LAYOUT_LEVELS && nl <= TFS_DICB_MAX_LEVELS && h->lvl_begin[nl] <= (1 << 24)) {
+        if (kind == TFS_LAYOUT_LEVELS) {
             int optin = 0;
             CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-            const int rows = h->lvl_begin[nl];
-            auto lvl_ents = [&](int l) { return slice_off[h->lvl_begin[l + 1] >> 5] - slice_off[h->lvl_begin[l] >> 5]; };
-            int rm = 32, ents = 32;
-            for (int l = 0; l < nl; l++) {
-                rm = std::max(rm, h->lvl_begin[l + 1] - h->lvl_begin[l]);
-                ents = std::max(ents, lvl_ents(l));
-            }
-            auto plan = [&](int tsize, tfs_handle::DicbPlan &P) {
-                const int R = TFS_DICB_SLOTS;
-                const int vec = (rows * tsize + 127) & ~127;
-                const int64_t room = (int64_t)optin - vec - dicb_table_bytes(nl, nl, rows) - dicb_sync_bytes(R);
-                const int64_t per_row = 4 + 2 * tsize, per_ent = 4 + tsize;
-                const int64_t widest = per_row * rm + per_ent * ents;
-                if (room < R * widest) return;
-                const double k = (double)(room / R) / (double)widest;   // >= 1
-                const int rm_c = std::max(rm, (int)(rm * k) & ~31), ents_c = std::max(ents, (int)(ents * k) & ~31);
-                if (per_row * rm_c + per_ent * ents_c > room / R) return;
-                P.rm = rm_c;
-                P.ents = ents_c;
+            auto keep = [&](const DicbPlanResult &r, tfs_handle::DicbPlan &P) {
+                if (!r.bytes) return;
+                P.bytes = r.bytes;
+                P.rm = r.rm;
+                P.ents = r.ents;
+                P.n_groups = (int)r.groups.size() - 1;
                 P.group_off = (int)h->lvl_tab.size();
-                h->lvl_tab.push_back(0);
-                int gr = 0, ge = 0;
-                for (int l = 0; l < nl; l++) {
-                    const int lrows = h->lvl_begin[l + 1] - h->lvl_begin[l], lents = lvl_ents(l);
-                    if (l > 0 && (gr + lrows > rm_c || ge + lents > ents_c)) {
-                        h->lvl_tab.push_back(l);
-                        gr = ge = 0;
-                    }
-                    gr += lrows;
-                    ge += lents;
-                }
-                h->lvl_tab.push_back(nl);
-                P.n_groups = (int)h->lvl_tab.size() - P.group_off - 1;
-                P.bytes = vec + R * (int)(per_row * rm_c + per_ent * ents_c) + dicb_table_bytes(nl, P.n_groups, rows) +
-                          dicb_sync_bytes(R);
+                h->lvl_tab.insert(h->lvl_tab.end(), r.groups.begin(), r.groups.end());
             };
-            plan(8, h->dicb64);
-            plan(4, h->dicb32);
-            static std::once_flag attr_once;
-            std::call_once(attr_once, [optin] {
-                cudaFuncSetAttribute(k_dic_block<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-                cudaFuncSetAttribute(k_dic_block<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-            });
+            keep(dicb_plan<double>(h->lvl_begin, slice_off, optin, TFS_DICB_SLOTS, TFS_DICB_MAX_LEVELS), h->dicb64);
+            keep(dicb_plan<float>(h->lvl_begin, slice_off, optin, TFS_DICB_SLOTS, TFS_DICB_MAX_LEVELS), h->dicb32);
+            // (a function attribute of the current device's context: set on
+            // every layout build)
+            const void *fns[] = {(const void *)k_dic_block<double, 0>, (const void *)k_dic_block<double, 2>,
+                                 (const void *)k_dic_block<double, 3>, (const void *)k_dic_block<double, 4>,
+                                 (const void *)k_dic_block<float, 0>, (const void *)k_dic_block<float, 3>,
+                                 (const void *)k_dic_block<float, 4>};
+            for (const void *f : fns) CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
         }
         if ((rc = dalloc(h, &h->d_lvl_begin, h->lvl_tab.size()))) return rc;
         CK(cudaMemcpyAsync(h->d_lvl_begin, h->lvl_tab.data(), sizeof(int) * h->lvl_tab.size(), cudaMemcpyHostToDevice,

@@ -222,6 +222,21 @@ def test_noalloc_scratch_address_is_cached_per_context(tmp_path):
     assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
 
 
+def test_one_block_dic_plan_invariants(tmp_path):
+    """The one-block DIC plan groups the level schedule into ring-slot
+    stages: every group fits a slot (rows and entries), the groups cover all
+    levels in order and each is greedy, the slot capacity is a multiple of 32,
+    the layout adds up to a byte count within the opt-in shared memory, and a
+    schedule whose vector or widest level does not fit gets no plan (the
+    level kernels run instead).  The planner is compiled on the host."""
+    import subprocess
+    exe = tmp_path / "dicb_plan_check"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", str(REPO / "t-flows_gb300" / "csrc"),
+                    str(REPO / "tests" / "native" / "dicb_plan_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
+
+
 @pytest.mark.parametrize("case", ["n0", "null"])
 def test_noalloc_rejections_set_error_text(case):
     """Every refusal of the no-allocation entry point says why (no GPU call
