@@ -64,9 +64,12 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 // 256 + tid, c = blockIdx.x, blockIdx.x + gridDim.x, ... (the direct
 // kernels' rows and order).  W: the matrix's uniform slice width.
 // Minimum resident blocks per SM asked of the compiler (register cap).
-// Unconstrained (1) measured best on the 128^3 system: binary32 35.7 us at
-// 40 registers against 36.9 us capped to 32 (8 blocks, with spills);
-// binary64 74.6 against 75.4 us at 56.
+// Unconstrained (1) is kept: on the 128^3 system the binary32 kernel runs
+// at 52 registers (4 blocks per SM) in 31.5 us; capped to 47 or 40
+// registers (5 or 6 blocks, no spills) with the grid at 5 or 6 blocks per
+// SM it took 30.8-30.9 us, inside the run-to-run spread, and capped to 32
+// (8 blocks, with spills) 36.9 us; binary64 73.8 us at 64 registers
+// against 73.8 us at 48 (5 blocks, small spills).
 #ifndef TFS_PIPE_MINB32
 #define TFS_PIPE_MINB32 1
 #endif
