@@ -568,7 +568,14 @@ __device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict_
 // slower on the 128^3 system, since a thread's rows then run their dependent
 // gathers one after the other.
 // Backward row (MODE 1 of sweep_row) whose start value s = y_i / (D_i +
-// TINY) and D_i were computed before the dependency wait.
+// TINY) and D_i were computed before the dependency wait.  The gathers of
+// the prefetched entries are all issued before the first update (here and
+// in sweep_row_fwd_pre): __ldcg is a volatile load, so one guarded by its
+// own entry test and followed by its update went out only after the
+// previous update, one memory round trip per entry.  Issued together they
+// cost one round trip per row: on the 128^3 system a binary32 DIC
+// application took 97.8 against 115.2 us, with the same arithmetic in the
+// same order.
 template <typename T, int NR, int NP>
 __device__ __forceinline__ void sweep_row_bwd_pre(const SellDev &A, const T *__restrict__ val, T *o1, T *o2,
                                                   int i, const RowGeom &g, const int *kk, const T *aa, T s1,
@@ -580,16 +587,24 @@ __device__ __forceinline__ void sweep_row_bwd_pre(const SellDev &A, const T *__r
         if (NR == 2) o2[i] = (T)0;
         return;
     }
-    int j = g.dpos + 1;
-    const int j1 = g.len;
+    const int j0 = g.dpos + 1, j1 = g.len;
+    T x1[NP], x2[NP];
 #pragma unroll
     for (int q = 0; q < NP; q++) {
-        if (j < j1) {
-            s1 = s1 - aa[q] * __ldcg(o1 + kk[q]);
-            if (NR == 2) s2 = s2 - aa[q] * __ldcg(o2 + kk[q]);
-            j++;
+        x1[q] = (T)0;
+        x2[q] = (T)0;
+        if (j0 + q < j1) {
+            x1[q] = __ldcg(o1 + kk[q]);
+            if (NR == 2) x2[q] = __ldcg(o2 + kk[q]);
         }
     }
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+        if (j0 + q < j1) {
+            s1 = s1 - aa[q] * x1[q];
+            if (NR == 2) s2 = s2 - aa[q] * x2[q];
+        }
+    int j = j0 + NP < j1 ? j0 + NP : j1;
     for (; j < j1; j++) {
         const int ee = g.off + (j << 5);
         const int k = __ldg(A.col + ee);
@@ -603,7 +618,7 @@ __device__ __forceinline__ void sweep_row_bwd_pre(const SellDev &A, const T *__r
 }
 
 // Forward row (MODE 0 of sweep_row) whose right-hand side b_i and D_i were
-// loaded before the dependency wait.
+// loaded before the dependency wait; gathers issued as in sweep_row_bwd_pre.
 template <typename T, int NR, int NP>
 __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__restrict__ val, T *o1, T *o2,
                                                   int i, const RowGeom &g, const int *kk, const T *aa, T s1,
@@ -615,16 +630,24 @@ __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__r
         if (NR == 2) o2[i] = (T)0;
         return;
     }
-    int j = 0;
     const int j1 = g.dpos;
+    T x1[NP], x2[NP];
 #pragma unroll
     for (int q = 0; q < NP; q++) {
-        if (j < j1) {
-            s1 = s1 - aa[q] * __ldcg(o1 + kk[q]);
-            if (NR == 2) s2 = s2 - aa[q] * __ldcg(o2 + kk[q]);
-            j++;
+        x1[q] = (T)0;
+        x2[q] = (T)0;
+        if (q < j1) {
+            x1[q] = __ldcg(o1 + kk[q]);
+            if (NR == 2) x2[q] = __ldcg(o2 + kk[q]);
         }
     }
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+        if (q < j1) {
+            s1 = s1 - aa[q] * x1[q];
+            if (NR == 2) s2 = s2 - aa[q] * x2[q];
+        }
+    int j = j1 < NP ? j1 : NP;
     for (; j < j1; j++) {
         const int ee = g.off + (j << 5);
         const int k = __ldg(A.col + ee);

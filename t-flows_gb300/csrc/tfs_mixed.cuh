@@ -395,11 +395,20 @@ k_sweep0_rho(SellDev A, const T *__restrict__ val, const T *d, const T *r, T *z,
                 else acc = fma(r[i], (T)0, acc);
             }
         } else {
+            // the prefetched entries' gathers all issued before the first
+            // update (as in the level kernels' row routines)
             T sv = s0;
-            int j = g.dpos + 1;
+            const int j0 = g.dpos + 1;
+            T xz[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                xz[q] = (T)0;
+                if (j0 + q < g.len) xz[q] = __ldcg(z + kk[q]);
+            }
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (j < g.len) { sv = sv - aa[q] * __ldcg(z + kk[q]); j++; }
+                if (j0 + q < g.len) sv = sv - aa[q] * xz[q];
+            int j = j0 + 4 < g.len ? j0 + 4 : g.len;
             for (; j < g.len; j++) {
                 const int ee = g.off + (j << 5);
                 sv = sv - __ldg(val + ee) * __ldcg(z + __ldg(A.col + ee));
