@@ -666,6 +666,11 @@ __device__ __forceinline__ void sweep_row_fwd_pre(const SellDev &A, const T *__r
 // when this kernel starts): the row's start value y_i / (D_i + TINY) is
 // computed before the wait, taking the division off the dependent chain.
 #define TFS_FWD_PRE_SLOTS 6   // forward level kernels: slots loaded before the dependency wait
+// Backward level kernels (PREY): binary32 six (mixed 128^3 DIC-CG 17.31
+// against 17.14 solves/s with four), binary64 four (six spill at its
+// 40-register cap: 7.46 against 7.68 solves/s).
+#define TFS_BWD_PRE_SLOTS 6
+#define TFS_BWD_SLOTS(T) (sizeof(T) == 4 ? TFS_BWD_PRE_SLOTS : 4)
 // Level kernels of 256 threads: binary64 held to 40 registers (6 blocks per
 // SM; the backward kernel would take 48, 5 blocks): 7.43 against 7.36
 // binary64 solves/s at 128^3; binary32 to 32 (8 blocks per SM, what the
@@ -706,7 +711,7 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
             const int j0 = MODE == 1 ? g.dpos + 1 : 0, j1 = MODE == 1 ? g.len : g.dpos;
             // as many as the forward row routine below takes from kk / aa
 #pragma unroll
-            for (int q = 0; q < (MODE == 0 && PREY ? TFS_FWD_PRE_SLOTS : 4); q++)
+            for (int q = 0; q < (MODE == 0 && PREY ? TFS_FWD_PRE_SLOTS : MODE == 1 && PREY ? TFS_BWD_SLOTS(T) : 4); q++)
                 if (j0 + q < j1) {
                     int ee = g.off + ((j0 + q) << 5);
                     kk[q] = __ldg(A.col + ee);
@@ -735,7 +740,7 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
     const unsigned long long t0 = stp ? gtimer() : 0ull;
     if (MODE == 0 && first && blockIdx.x == 0 && threadIdx.x == 0) st->t_sweep0 = gtimer();
     if (MODE == 1 && PREY) {
-        if (active) sweep_row_bwd_pre<T, NR, 4>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
+        if (active) sweep_row_bwd_pre<T, NR, TFS_BWD_SLOTS(T)>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
     } else if (MODE == 0 && PREY) {
         if (active) sweep_row_fwd_pre<T, NR, TFS_FWD_PRE_SLOTS>(A, val, o1, o2, i, g, kk, aa, ps1, ps2, pdi, skip);
     } else if (active) {

@@ -362,12 +362,12 @@ k_sweep0_rho(SellDev A, const T *__restrict__ val, const T *d, const T *r, T *z,
     const int i = blockIdx.x * TFS_TPB + threadIdx.x;
     const bool active = i < l0_rows;
     RowGeom g{0, 0, 0};
-    int kk[4] = {0, 0, 0, 0};
-    T aa[4] = {(T)0, (T)0, (T)0, (T)0};
+    int kk[TFS_BWD_PRE_SLOTS] = {};
+    T aa[TFS_BWD_PRE_SLOTS] = {};
     if (active) {
         g = row_geom(A, i);
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < TFS_BWD_SLOTS(T); q++)
             if (g.dpos + 1 + q < g.len) {
                 const int ee = g.off + ((g.dpos + 1 + q) << 5);
                 kk[q] = __ldg(A.col + ee);
@@ -399,16 +399,17 @@ k_sweep0_rho(SellDev A, const T *__restrict__ val, const T *d, const T *r, T *z,
             // update (as in the level kernels' row routines)
             T sv = s0;
             const int j0 = g.dpos + 1;
-            T xz[4];
+            constexpr int NP = TFS_BWD_SLOTS(T);
+            T xz[NP];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < NP; q++) {
                 xz[q] = (T)0;
                 if (j0 + q < g.len) xz[q] = __ldcg(z + kk[q]);
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int q = 0; q < NP; q++)
                 if (j0 + q < g.len) sv = sv - aa[q] * xz[q];
-            int j = j0 + 4 < g.len ? j0 + 4 : g.len;
+            int j = j0 + NP < g.len ? j0 + NP : g.len;
             for (; j < g.len; j++) {
                 const int ee = g.off + (j << 5);
                 sv = sv - __ldg(val + ee) * __ldcg(z + __ldg(A.col + ee));
