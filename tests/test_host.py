@@ -237,6 +237,48 @@ def test_one_block_dic_plan_invariants(tmp_path):
     assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
 
 
+def test_reference_arm_line_without_the_solver_library():
+    """`bench.py --impl reference` on the 32^3 workload prints one JSON line
+    with the keys of the bench contract, the `config` our arm reports for the
+    same workload and no host-device bytes; it never loads the GPU solver
+    library: the path to it points nowhere in the child's environment (any
+    load would fail the run, workers included) and the main process's
+    mappings hold no copy of it."""
+    import os
+    import subprocess
+    import sys
+    code = ("import runpy, sys\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'poisson32_diag_cg',"
+            " '--steps', '1', '--warmup', '3']\n"
+            "try:\n"
+            "    runpy.run_path('bench.py', run_name='__main__')\n"
+            "except SystemExit as e:\n"
+            "    assert not e.code, e.code\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('MAPPED' if 'libtfs_gb300' in maps else 'CLEAN', file=sys.stderr)\n")
+    env = dict(os.environ, TFS_LIBRARY=str(REPO / "nonexistent" / "libtfs_gb300.so"))
+    out = subprocess.run([sys.executable, "-c", code], cwd=REPO, env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stderr.strip().splitlines()[-1] == "CLEAN", out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"] == d["e2e"]["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    import argparse
+    sys.path.insert(0, str(REPO))
+    import bench
+    args = argparse.Namespace(workload="poisson32_diag_cg", niter=5000)
+    s = SynthSystem(*bench.WORKLOADS["poisson32_diag_cg"][:2], jitter=0.2, seed=bench.BASE_SEED)
+    assert d["config"] == bench.workload_config(args, s.n, s.nnz)
+
+
 @pytest.mark.parametrize("case", ["n0", "null"])
 def test_noalloc_rejections_set_error_text(case):
     """Every refusal of the no-allocation entry point says why (no GPU call
