@@ -557,8 +557,9 @@ __device__ __forceinline__ void sweep_row(const SellDev &A, const T *__restrict_
 //
 // The default schedule: one kernel per large level, launched with
 // programmatic dependent launch (PDL).  A level kernel first reads what does
-// not depend on the previous level (row geometry and its first four column
-// indices and values), then lets the next level's kernel start
+// not depend on the previous level (row geometry and its first column
+// indices and values: TFS_FWD_PRE_SLOTS forward, TFS_BWD_SLOTS backward,
+// four otherwise), then lets the next level's kernel start
 // (cudaTriggerProgrammaticLaunchCompletion) and waits for the previous one
 // (cudaGridDependencySynchronize), so launch latency and prefetch overlap the
 // previous level.  The small trailing levels run in one single-block kernel
