@@ -39,6 +39,24 @@ def test_library_exports_every_declared_symbol():
     assert declared <= set(SIGNATURES), sorted(declared - set(SIGNATURES))
 
 
+def test_header_constants_match_the_python_mirror():
+    """Every numeric constant of include/tfs_solver.h that the Python side
+    mirrors has the header's value, and every option, status, method,
+    preconditioner and arithmetic code is mirrored."""
+    import tflows.lib as L
+    text = (REPO / "include" / "tfs_solver.h").read_text()
+    defs = {m.group(1): int(m.group(2))
+            for m in re.finditer(r"^#define\s+(TFS_[A-Z0-9_]+)\s+(-?\d+)\b", text, flags=re.M)}
+    assert len(defs) >= 30
+    for name, value in defs.items():
+        if hasattr(L, name):
+            assert getattr(L, name) == value, name
+    required = [n for n in defs if n.startswith(("TFS_OPT_", "TFS_ERR_", "TFS_PREC_"))]
+    required += ["TFS_OK", "TFS_CG", "TFS_BICG", "TFS_CGS", "TFS_FP64", "TFS_MIXED"]
+    missing = [n for n in required if not hasattr(L, n)]
+    assert not missing, missing
+
+
 def test_synth_library_exports_its_header_and_nothing_of_the_solver():
     """The seeded systems come from a host-only library, so a process that
     only builds inputs (the CPU reference arm of the benchmark) never loads
