@@ -696,9 +696,9 @@ k_sweep_level(SellDev A, const T *__restrict__ val, T *d, const T *b1, const T *
             // for it (slots past the row's length hold column 0, value 0).
             // Six slots hold every lower entry of a 7-entry row: measured on
             // the 128^3 system 4 / 6 / 8 slots 126.2 / 116.9 / 119.3 us per
-            // DIC application (14.92 / 15.54 / 15.31 solves/s mixed);
-            // backward levels, whose loads wait for the geometry anyway,
-            // keep four (six: 14.74 mixed).
+            // DIC application (14.92 / 15.54 / 15.31 solves/s mixed, before
+            // the row routines issued their gathers together).  Backward
+            // levels load their slots after the geometry (TFS_BWD_SLOTS).
             const int off = (i & ~31) * A.width + (i & 31);
             g = row_geom(A, i);
 #pragma unroll
