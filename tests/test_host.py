@@ -71,6 +71,26 @@ def test_synth_library_exports_its_header_and_nothing_of_the_solver():
     assert not hasattr(lib, "tfs_synth_create")
 
 
+def test_product_never_reaches_the_oracle():
+    """The oracle is the checker only: no module or source of the product
+    package mentions it (the build script compiles it for the tests, which is
+    not a use), the solver library does not link it and exports none of its
+    functions."""
+    import subprocess
+    pkg = REPO / "t-flows_gb300"
+    for p in sorted(pkg.rglob("*")):
+        if p.suffix not in (".py", ".cu", ".cuh", ".cpp", ".h", ".f90") or p.name == "build.py":
+            continue
+        text = p.read_text(errors="replace")
+        assert "oracle" not in text.lower() and "tfo_" not in text, p
+    lib = load_library()
+    dyn = subprocess.run(["readelf", "-d", str(lib._name)], capture_output=True, text=True, check=True).stdout
+    assert "oracle" not in dyn, dyn
+    syms = subprocess.run(["nm", "-D", "--defined-only", str(lib._name)], capture_output=True, text=True,
+                          check=True).stdout
+    assert not re.search(r"\btfo_", syms)
+
+
 def test_library_is_in_tree_and_built_for_sm103a():
     from tflows import build
     assert lib_path.is_relative_to(REPO)
