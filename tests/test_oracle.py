@@ -177,12 +177,12 @@ def test_scipy_jacobi_cgs_cross_check():
     assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-8
 
 
-def _textbook(method, A, b, dinv, k):
+def _textbook(method, A, b, minv, k):
     """k iterations from x0 = 0 of the published preconditioned CG
     (Hestenes-Stiefel) or CGS (Sonneveld) recurrences, as Barrett et al.,
     Templates for the Solution of Linear Systems (SIAM 1994), state them,
-    with the preconditioner M = diag(1/dinv); numpy, independent of the
-    oracle's code."""
+    with the preconditioner applied by minv(v) = M^-1 v; numpy, independent
+    of the oracle's code."""
     x = np.zeros_like(b)
     r = b.copy()
     rt = r.copy()
@@ -190,7 +190,7 @@ def _textbook(method, A, b, dinv, k):
     p = q = None
     for _ in range(k):
         if method == 0:
-            z = dinv * r
+            z = minv(r)
             rho = r @ z
             p = z if rho_old is None else z + (rho / rho_old) * p
             qv = A @ p
@@ -206,19 +206,42 @@ def _textbook(method, A, b, dinv, k):
                 beta = rho / rho_old
                 u = r + beta * q
                 p = u + beta * (q + beta * p)
-            vh = A @ (dinv * p)
+            vh = A @ minv(p)
             alpha = rho / (rt @ vh)
             q = u - alpha * vh
-            uh = dinv * (u + q)
+            uh = minv(u + q)
             x = x + alpha * uh
             r = r - alpha * (A @ uh)
         rho_old = rho
     return x
 
 
+def _dic_inverse(A):
+    """M^-1 of the diagonal incomplete Cholesky preconditioner written from
+    its definition, independent of the oracle: A = L + diag(A) + U,
+    D_i = 1 / (a_ii - sum_{k<i} D_k a_ik^2) over the stored lower entries of
+    row i, M = (D^-1 + L) D (D^-1 + U); applied as two triangular solves
+    (scipy) and a scaling."""
+    from scipy.sparse import diags, tril, triu
+    from scipy.sparse.linalg import spsolve_triangular
+    A = A.tocsr()
+    n = A.shape[0]
+    d = np.zeros(n)
+    for i in range(n):
+        s = A[i, i]
+        for jj in range(A.indptr[i], A.indptr[i + 1]):
+            k = A.indices[jj]
+            if k < i:
+                s = s - d[k] * A.data[jj] * A.data[jj]
+        d[i] = 1.0 / s
+    lower = (diags(1.0 / d) + tril(A, k=-1)).tocsr()
+    upper = (diags(1.0 / d) + triu(A, k=1)).tocsr()
+    return lambda v: spsolve_triangular(upper, spsolve_triangular(lower, v, lower=True) / d, lower=False)
+
+
 @pytest.mark.parametrize("method,kind,book", [(0, 0, 0), (1, 0, 0), (2, 1, 2)],
                          ids=["cg-poisson", "bicg-poisson", "cgs-convdiff"])
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_iterates_follow_the_published_recurrence(method, kind, book, prec):
     """After each of the first iterations the oracle's x equals the iterate
     of the published recurrence (to rounding: the sums run in another
@@ -232,11 +255,11 @@ def test_iterates_follow_the_published_recurrence(method, kind, book, prec):
     from tflows import SynthSystem
     s = SynthSystem(kind, 7, 6, 5)
     A = sp.csr_matrix((s.val, s.col - 1, s.row - 1), shape=(s.n, s.n))
-    dinv = 1.0 / A.diagonal() if prec == 1 else np.ones(s.n)
+    minv = _dic_inverse(A) if prec == 2 else (lambda v, d=A.diagonal() if prec == 1 else 1.0: v / d)
     for k in range(1, 7):
         x, r = np.zeros(s.n), s.b.copy()
         O.solve(method, s.n, s.row, s.col, s.dia, s.val, x, r, prec, k, 1e-300)
-        xt = _textbook(book, A, s.b, dinv, k)
+        xt = _textbook(book, A, s.b, minv, k)
         assert np.linalg.norm(x - xt) <= 1e-11 * np.linalg.norm(xt), (k, np.linalg.norm(x - xt))
 
 
