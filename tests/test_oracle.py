@@ -330,6 +330,29 @@ def test_golden_topology():
         assert np.array_equal(col[pos[:, 0] - 1], f[:, 1]) and np.array_equal(col[pos[:, 1] - 1], f[:, 0])
 
 
+@pytest.mark.parametrize("kind,dims", [(0, (6, 5, 4)), (1, (5, 5, 7))])
+def test_topology_pattern_from_an_independent_construction(kind, dims):
+    """The oracle's Topology.f90 restatement gives the sorted compressed-row
+    pattern that scipy builds from the same faces (every cell's diagonal,
+    both directions of every interior face), mir pairs (i, j) with (j, i)
+    and dia points at the diagonal."""
+    sp = pytest.importorskip("scipy.sparse")
+    from tflows import SynthSystem
+    s = SynthSystem(kind, *dims, seed=9, permute=True)
+    f = s.faces_c
+    inner = f[:, 1] > 0
+    c1, c2 = f[inner, 0] - 1, f[inner, 1] - 1
+    i = np.concatenate([np.arange(s.n), c1, c2])
+    j = np.concatenate([np.arange(s.n), c2, c1])
+    P = sp.csr_matrix((np.ones(i.size), (i, j)), shape=(s.n, s.n))
+    P.sort_indices()
+    row, col, dia, mir, pos = O.topology(s.n, f)
+    assert np.array_equal(row - 1, P.indptr) and np.array_equal(col - 1, P.indices)
+    rows_of = np.repeat(np.arange(1, s.n + 1), np.diff(row))
+    assert np.array_equal(col[dia - 1], np.arange(1, s.n + 1))
+    assert np.array_equal(rows_of[mir - 1], col) and np.array_equal(col[mir - 1], rows_of)
+
+
 def test_assemble_faces_known_answer():
     """Face-loop assembly (NewUVW.f90:366-384, :500-505) on a three-cell
     chain with two boundary faces, against the matrix written out by hand."""
