@@ -402,27 +402,6 @@ k_load(SellDev A, const double *__restrict__ val, const int *__restrict__ perm,
     }
 }
 
-// Diagonal incomplete Cholesky, one level of rows (Prec_Form.f90:32-40):
-// D_i = 1 / (a_ii - sum_{lower j} D_col(j) a_j a_j).
-__global__ void __launch_bounds__(TFS_TPB)
-k_dic_form(SellDev A, const double *__restrict__ val, double *d, int row0, int row1,
-           const DevState *st)
-{
-    if (st->done) return;
-    int i = row0 + blockIdx.x * TFS_TPB + threadIdx.x;
-    if (i >= row1) return;
-    RowGeom g = row_geom(A, i);
-    if (g.len == 0) { d[i] = 1.0; return; }
-    double sum1 = __ldg(val + g.off + (g.dpos << 5));
-    for (int j = 0; j < g.dpos; j++) {
-        int e = g.off + (j << 5);
-        int k = __ldg(A.col + e);
-        double a = __ldg(val + e);
-        sum1 = sum1 - d[k] * a * a;
-    }
-    d[i] = 1.0 / sum1;
-}
-
 // r1 <- r1 - A x (Residual.f90:22-27), ||r0|| and the second early exit
 // (Cg.f90:63-90).  For BiCG/CGS also r2 = r1 (Bicg.f90:91-93, Cgs.f90:71-73).
 // rho of the first iteration is computed here when it needs no sweep.
